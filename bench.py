@@ -1,0 +1,450 @@
+"""Benchmark of the GB300 stencil backend on the 512x512x80 fp64 roofline set.
+
+One step = one horizontal-diffusion launch (inp, coeff -> out) followed by
+one vertical-advection launch (u component, in place), both on the interior
+512 x 512 x 80 in fp64, with the reference's halos (2 in i/j for hdiff, 1 in
+i for vadv) and seeded inputs drawn from the distributions of the workload
+(hdiff fields U[0,1); vadv stage/pos/tens/tensstage U[-1,1), wcon
+U[-0.5,0.5)).  The fields of one step occupy ~1.35 GB, far above the 129 MB
+L2, so no L2 flush is needed between steps.
+
+Printed JSON line (rank 0):
+  value        grid points per second over the whole job (hdiff + vadv points,
+               i.e. 2 * 512*512*80 per step per GPU), inputs resident in HBM
+  e2e          the same metric through the C ABI with pinned host buffers:
+               every step uploads the step's inputs and downloads its outputs
+  roofline     the dominant kernel's compulsory HBM bytes per launch / its
+               average CUDA-event duration, against the measured copy peak
+  cpu_baseline the C restatement of the reference arithmetic (OpenMP, all
+               host cores) on the same workload
+  stream_triad STREAM triad on 2^29 fp64 (the bandwidth calibration kernel)
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Multi-GPU (torchrun, one rank per GPU): every rank runs an independent
+replica of the workload (weak scaling); ranks meet at a barrier around the
+timed region and the maximum time over ranks is reported.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+NI, NJ, NK = 512, 512, 80
+HDIFF_HALO = (2, 2, 0)
+VADV_HALO = (1, 1, 0)
+POINTS = NI * NJ * NK
+TRIAD_N = 1 << 29
+METRIC = "hdiff+vadv GPoints/s (fp64, 512x512x80)"
+UNIT = "GPoints/s"
+
+
+def compulsory_bytes(kind, s=8):
+    """Algorithmic HBM bytes per launch (each input read once, output written once)."""
+    if kind == "hdiff":  # inp with its 2-point i/j halo, coeff, out
+        return s * ((NI + 4) * (NJ + 4) * NK + 2 * NI * NJ * NK)
+    if kind == "vadv":  # ustage, upos, utens, utensstage (read + write), wcon incl. column i+1
+        return s * (5 * NI * NJ * NK + (NI + 1) * NJ * NK)
+    raise ValueError(kind)
+
+
+def measured_peaks():
+    path = ROOT / "MEASURED_PEAKS.json"
+    if path.exists():
+        try:
+            data = json.loads(path.read_text())
+            return float(data["hbm_gbs"]), "measured"
+        except Exception:  # noqa: BLE001
+            pass
+    return 6800.0, "fallback"
+
+
+def ncu_traffic():
+    """Per-launch DRAM bytes from the committed ncu summary, if present."""
+    path = ROOT / "profiles" / "dram_traffic.txt"
+    out = {}
+    if path.exists():
+        for line in path.read_text().splitlines():
+            parts = line.split()
+            if len(parts) >= 2 and not line.startswith("#"):
+                try:
+                    out[parts[0]] = float(parts[1])
+                except ValueError:
+                    pass
+    return out
+
+
+class ClockSampler:
+    """Samples nvidia-smi clocks and throttle reasons while the timed region runs."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index=0):
+        self.device_index = device_index
+        self.proc = None
+        self.lines = []
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device_index), f"--query-gpu={self.QUERY}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (OSError, ValueError):
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm, smax, power = [], [], []
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+                power.append(float(parts[3]))
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[5:9]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax),
+                "power_w_max": max(power) if power else None, "samples": len(sm),
+                "reasons": sorted(reasons)}
+
+
+# ---------------------------------------------------------------------------
+# distributed plumbing (torchrun): barrier and max over ranks
+# ---------------------------------------------------------------------------
+
+
+class Dist:
+    def __init__(self):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch
+            import torch.distributed as dist
+
+            backend = "nccl" if torch.cuda.is_available() else "gloo"
+            if backend == "nccl":
+                torch.cuda.set_device(self.local_rank)
+            dist.init_process_group(backend)
+            self.torch, self.dist = torch, dist
+
+    def barrier(self):
+        if self.world > 1:
+            self.dist.barrier()
+
+    def max(self, value: float) -> float:
+        if self.world == 1:
+            return value
+        dev = "cuda" if self.torch.cuda.is_available() else "cpu"
+        t = self.torch.tensor([value], dtype=self.torch.float64, device=dev)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.world > 1:
+            self.dist.destroy_process_group()
+
+
+# ---------------------------------------------------------------------------
+# workload
+# ---------------------------------------------------------------------------
+
+
+def make_inputs(seed=2024):
+    from stencil_benchmarks_gb300 import array as sbarray
+
+    rng = np.random.Generator(np.random.PCG64(seed))
+
+    def field(halo, lo, hi):
+        shape = (NI + 2 * halo[0], NJ + 2 * halo[1], NK + 2 * halo[2])
+        a = sbarray.alloc_array(shape, "float64", (2, 1, 0), 0, index_to_align=halo)
+        a[...] = rng.uniform(lo, hi, size=shape)
+        return a
+
+    hd = {n: field(HDIFF_HALO, 0.0, 1.0) for n in ("inp", "coeff", "out")}
+    va = {n: field(VADV_HALO, -1.0, 1.0) for n in ("ustage", "upos", "utens", "utensstage")}
+    va["wcon"] = field(VADV_HALO, -0.5, 0.5)
+    # the new utensstage goes to a separate field, so every step solves the same system
+    va["out"] = field(VADV_HALO, 0.0, 0.0)
+    return hd, va
+
+
+def run_gpu(args, dist):
+    from stencil_benchmarks_gb300 import _native, kernels
+    from stencil_benchmarks_gb300.device import DeviceBuffer, Event, Field, PinnedBuffer, Stream
+
+    _native.call("sb_set_device", dist.local_rank)
+    info = _native.device_info(dist.local_rank)
+    hd, va = make_inputs(seed=2024 + dist.rank)
+    dev_hd = {n: Field.like_host(h, "float64", HDIFF_HALO) for n, h in hd.items()}
+    dev_va = {n: Field.like_host(h, "float64", VADV_HALO) for n, h in va.items()}
+    for n, h in hd.items():
+        dev_hd[n].upload(h)
+    for n, h in va.items():
+        dev_va[n].upload(h)
+    stream = Stream()
+    launches = {"hdiff": 0, "vadv": 0}
+
+    def step(ev=None):
+        if ev is not None:
+            ev[0].record(stream)
+        kernels.hdiff(dev_hd["inp"], dev_hd["coeff"], dev_hd["out"], stream=stream)
+        if ev is not None:
+            ev[1].record(stream)
+        kernels.vadv(dev_va["ustage"], dev_va["upos"], dev_va["utens"], dev_va["utensstage"], dev_va["wcon"],
+                     out=dev_va["out"], stream=stream)
+        if ev is not None:
+            ev[2].record(stream)
+        launches["hdiff"] += 1
+        launches["vadv"] += 1
+
+    for _ in range(args.warmup):
+        step()
+    stream.synchronize()
+
+    events = [[Event(), Event(), Event()] for _ in range(args.steps)]
+    start, stop = Event(), Event()
+    clocks = ClockSampler(dist.local_rank)
+    clocks.start()
+    time.sleep(0.3)
+    dist.barrier()
+    _native.synchronize()
+    launches = {"hdiff": 0, "vadv": 0}
+    start.record(stream)
+    for s in range(args.steps):
+        step(events[s])
+    stop.record(stream)
+    stop.synchronize()
+    _native.synchronize()
+    elapsed = start.elapsed(stop)
+    dist.barrier()
+    clk = clocks.stop()
+    t_hdiff = [e[0].elapsed(e[1]) for e in events]
+    t_vadv = [e[1].elapsed(e[2]) for e in events]
+    elapsed_max = dist.max(elapsed)
+    gpu_launches = launches["hdiff"] + launches["vadv"]
+
+    # ---- end to end: pinned host buffers, H2D of the step's inputs, D2H of its outputs
+    in_fields = [(dev_hd[n], hd[n]) for n in ("inp", "coeff")] + \
+                [(dev_va[n], va[n]) for n in ("ustage", "upos", "utens", "utensstage", "wcon")]
+    out_fields = [(dev_hd["out"], hd["out"]), (dev_va["out"], va["out"])]
+    pinned_in = []
+    for f, h in in_fields:
+        pb = PinnedBuffer(f.span_bytes)
+        view = pb.array(np.uint8, (f.span_bytes,))
+        from stencil_benchmarks_gb300.device import _span_view
+
+        view[...] = _span_view(h)
+        pinned_in.append((f, pb))
+    pinned_out = [(f, PinnedBuffer(f.span_bytes)) for f, _ in out_fields]
+    h2d = sum(f.span_bytes for f, _ in pinned_in)
+    d2h = sum(f.span_bytes for f, _ in pinned_out)
+
+    def e2e_step():
+        for f, pb in pinned_in:
+            _native.call("sb_memcpy_async", f.base_ptr, pb.ptr, f.span_bytes, _native.H2D, stream.as_parameter)
+        step()
+        for f, pb in pinned_out:
+            _native.call("sb_memcpy_async", pb.ptr, f.base_ptr, f.span_bytes, _native.D2H, stream.as_parameter)
+
+    e2e_steps = max(1, min(args.steps, 10))
+    for _ in range(2):
+        e2e_step()
+    stream.synchronize()
+    dist.barrier()
+    e0, e1 = Event(), Event()
+    e0.record(stream)
+    for _ in range(e2e_steps):
+        e2e_step()
+    e1.record(stream)
+    e1.synchronize()
+    e2e_time = dist.max(e0.elapsed(e1))
+
+    # ---- STREAM triad calibration (outside the timed region)
+    triad = None
+    if not args.no_triad:
+        bufs = [DeviceBuffer(TRIAD_N * 8) for _ in range(3)]
+        a, b, c = (x.ptr for x in bufs)
+        kernels.stream_op(_native.STREAM_INIT, "float64", a, b, c, TRIAD_N)
+        times = []
+        for _ in range(6):
+            times.append(kernels.stream_op(_native.STREAM_TRIAD, "float64", a, b, c, TRIAD_N, 3.0, timed=True))
+        best = min(times[1:])
+        triad = {"n": TRIAD_N, "dtype": "f64", "best_s": best, "gbs": 3 * 8 * TRIAD_N / best / 1e9}
+        del bufs
+
+    return {
+        "info": info, "elapsed": elapsed_max, "t_hdiff": t_hdiff, "t_vadv": t_vadv, "clocks": clk,
+        "gpu_launches": gpu_launches, "e2e_time": e2e_time, "e2e_steps": e2e_steps, "h2d": h2d, "d2h": d2h,
+        "triad": triad,
+    }
+
+
+def cpu_baseline_sample(threads=None):
+    """Time the C restatement on the full 512x512x80 hdiff+vadv fp64 step."""
+    from oracle import cport
+
+    hd, va = make_inputs(seed=7)
+    if threads:
+        cport.set_threads(threads)
+    n_threads = cport.max_threads()
+    times = []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        cport.hdiff(hd["inp"], hd["coeff"], hd["out"], (NI, NJ, NK), HDIFF_HALO)
+        cport.vadv(va["ustage"], va["upos"], va["utens"], va["utensstage"], va["wcon"], (NI, NJ, NK), VADV_HALO,
+                   out=va["out"])
+        times.append(time.perf_counter() - t0)
+    t = statistics.median(times)
+    return {
+        "value": 2 * POINTS / t / 1e9, "unit": UNIT, "cores": n_threads, "kind": "port",
+        "sample": f"full 512x512x80 hdiff+vadv fp64 step, median of {len(times)} runs "
+                  f"(oracle/csrc/oracle.c, OpenMP, {n_threads} threads, {os.cpu_count()} host cores)",
+        "seconds_per_step": t,
+    }
+
+
+def run_reference(args, dist):
+    """--impl reference: the reference arithmetic on the host cores (C port)."""
+    if dist.rank != 0:
+        return 0
+    from oracle import cport
+
+    hd, va = make_inputs(seed=7)
+    n_threads = cport.max_threads()
+    for _ in range(args.warmup):
+        cport.hdiff(hd["inp"], hd["coeff"], hd["out"], (NI, NJ, NK), HDIFF_HALO)
+        cport.vadv(va["ustage"], va["upos"], va["utens"], va["utensstage"], va["wcon"], (NI, NJ, NK), VADV_HALO,
+                   out=va["out"])
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        cport.hdiff(hd["inp"], hd["coeff"], hd["out"], (NI, NJ, NK), HDIFF_HALO)
+        cport.vadv(va["ustage"], va["upos"], va["utens"], va["utensstage"], va["wcon"], (NI, NJ, NK), VADV_HALO,
+                   out=va["out"])
+    elapsed = time.perf_counter() - t0
+    value = 2 * POINTS * args.steps / elapsed / 1e9
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": elapsed / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded PCG64, workload distributions)",
+        "config": {"workload": "hdiff+vadv fp64 512x512x80 (halo 2,2,0 / 1,1,0)", "l2": "inputs > L2"},
+        "cpu_baseline": {
+            "value": value, "unit": UNIT, "cores": n_threads, "kind": "port",
+            "sample": "every step is the full 512x512x80 hdiff+vadv fp64 step on the host cores "
+                      "(C restatement of the reference arithmetic, OpenMP)",
+        },
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--no-cpu-baseline", action="store_true", help="skip the timed CPU baseline")
+    ap.add_argument("--no-triad", action="store_true", help="skip the STREAM triad calibration")
+    args = ap.parse_args(argv)
+    if args.warmup < 3:
+        print("warning: fewer than 3 warm-up steps", file=sys.stderr)
+
+    dist = Dist()
+    try:
+        if args.impl == "reference":
+            return run_reference(args, dist)
+        res = run_gpu(args, dist)
+        if dist.rank != 0:
+            return 0
+        peak, peak_kind = measured_peaks()
+        t_h = statistics.mean(res["t_hdiff"])
+        t_v = statistics.mean(res["t_vadv"])
+        dominant = "vadv" if t_v >= t_h else "hdiff"
+        t_dom = max(t_h, t_v)
+        achieved = compulsory_bytes(dominant) / t_dom / 1e9
+        traffic = ncu_traffic().get(dominant)
+        value = 2 * POINTS * args.steps * dist.world / res["elapsed"] / 1e9
+        e2e_value = 2 * POINTS * res["e2e_steps"] * dist.world / res["e2e_time"] / 1e9
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": res["elapsed"] / args.steps * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded PCG64, workload distributions)",
+            "config": {"workload": "hdiff+vadv fp64 512x512x80 (halo 2,2,0 / 1,1,0)",
+                       "l2": "inputs > L2 (1.35 GB of fields per step), no flush",
+                       "device": res["info"]["name"], "sm_count": res["info"]["sm_count"]},
+            "gpu_launches": res["gpu_launches"],
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": res["h2d"],
+                    "d2h_bytes_per_step": res["d2h"], "steps": res["e2e_steps"],
+                    "path": "C ABI: pinned host -> sb_memcpy_async -> sb_hdiff + sb_vadv -> pinned host"},
+            "roofline": {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peak,
+                         "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
+                         "traffic": traffic, "algorithmic_bytes": compulsory_bytes(dominant)},
+            "kernels": {
+                "hdiff": {"ms": t_h * 1e3, "gpoints_s": POINTS / t_h / 1e9,
+                          "hbm_gbs": compulsory_bytes("hdiff") / t_h / 1e9,
+                          "frac_of_" + peak_kind: compulsory_bytes("hdiff") / t_h / 1e9 / peak},
+                "vadv": {"ms": t_v * 1e3, "gpoints_s": POINTS / t_v / 1e9,
+                         "hbm_gbs": compulsory_bytes("vadv") / t_v / 1e9,
+                         "frac_of_" + peak_kind: compulsory_bytes("vadv") / t_v / 1e9 / peak},
+            },
+            "stream_triad": res["triad"],
+            "clocks": res["clocks"],
+        }
+        if res["triad"]:
+            line["stream_triad"]["frac_of_" + peak_kind] = res["triad"]["gbs"] / peak
+        if not args.no_cpu_baseline:
+            line["cpu_baseline"] = cpu_baseline_sample()
+        print(json.dumps(line), flush=True)
+        return 0
+    finally:
+        dist.close()
+
+
+if __name__ == "__main__":
+    sys.exit(main())

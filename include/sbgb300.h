@@ -1,0 +1,171 @@
+/*
+ * sbgb300 -- C ABI of the GB300 (sm_103a) structured-grid stencil backend.
+ *
+ * Every entry point takes plain pointers, sizes and integer codes; none takes
+ * or returns a C++ or PyTorch type.  All return an int status: SB_OK (0) on
+ * success, a non-zero SB_ERR_* code otherwise, with a description available
+ * from sb_last_error() on the calling thread.  This mirrors the reference's
+ * generated launcher, which returns 0 or 1 and prints the CUDA error
+ * (stencil_benchmarks/benchmarks_collection/stencils/cuda_hip/templates/base.j2:48-55),
+ * and which the reference's ctypes wrapper turns into ExecutionError
+ * (stencil_benchmarks/tools/compilation.py:176-193).
+ *
+ * Field convention (same as the reference): a field is a 3D array with a halo;
+ * the pointer passed is the address of the FIRST INTERIOR POINT (reference:
+ * compilation.data_ptr(array, halo), tools/compilation.py:273-282) and
+ * (si, sj, sk) are its strides in ELEMENTS.  All fields of one call share
+ * the same strides, because the reference allocates them identically
+ * (stencils/base.py:87-101).  Unlike the reference, which compiles domain and
+ * strides into each generated kernel (stencils/cuda_hip/mixin.py:113-123),
+ * every size here is a run-time argument: one prebuilt library serves all
+ * shapes.
+ *
+ * Timing convention: when `time_s` is non-NULL, the call records CUDA events
+ * on `stream` around the kernel launch, waits for the end event and stores
+ * the elapsed seconds (reference: base.j2:145-190, "gpu" timers).  When it is
+ * NULL the launch is asynchronous on `stream` (NULL = legacy default stream).
+ */
+#ifndef SBGB300_H
+#define SBGB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------- */
+#define SB_OK 0
+#define SB_ERR_INVALID 1     /* invalid argument: shape, stride, type, alignment */
+#define SB_ERR_CUDA 2        /* a CUDA runtime call failed                         */
+#define SB_ERR_UNSUPPORTED 3 /* valid request this build does not implement        */
+#define SB_ERR_NOMEM 4       /* device or host allocation failed                   */
+#define SB_ERR_TIMEOUT 5     /* a bounded device-side wait gave up                 */
+#define SB_ERR_BUDGET 6      /* request exceeds a configured memory budget         */
+
+/* ---- element types (storage and compute) -------------------------------- */
+#define SB_F64 0
+#define SB_F32 1
+#define SB_BF16 2 /* storage only; computed in f32 (or f64) */
+
+/* ---- memcpy kinds (same values as cudaMemcpyKind) ------------------------ */
+#define SB_H2H 0
+#define SB_H2D 1
+#define SB_D2H 2
+#define SB_D2D 3
+#define SB_DEFAULT 4
+
+/* ---- kernel variants ------------------------------------------------------ */
+#define SB_VARIANT_AUTO 0
+#define SB_HDIFF_TILE 1   /* smem-staged k-plane tiles, lap/flx/fly once per point */
+#define SB_HDIFF_JSCAN 2  /* register j-march, i-neighbours by warp shuffles       */
+#define SB_VADV_SMEM 1    /* one thread per column, ccol/dcol in shared memory     */
+#define SB_VADV_GLOBAL 2  /* one thread per column, ccol/dcol in caller scratch    */
+
+/*
+ * Launch tuning.  Zero in any field means "choose the default".  The
+ * reference exposes the same knobs as benchmark Parameters (block_size,
+ * unroll_factor; stencils/cuda_hip/horizontal_diffusion.py:41,
+ * vertical_advection.py:40-46) baked into generated code; here they are
+ * run-time values validated against the device limits (base.j2:92-135).
+ */
+typedef struct sb_tune {
+    int32_t variant;   /* SB_HDIFF_* / SB_VADV_* or SB_VARIANT_AUTO            */
+    int32_t block_x;   /* threads along i                                       */
+    int32_t block_y;   /* threads along j                                       */
+    int32_t tile_y;    /* hdiff: rows of j per CTA                              */
+    int32_t k_per_cta; /* hdiff: k-planes per CTA                               */
+    int32_t unroll;    /* STREAM: vectors per thread per iteration             */
+    int32_t flags;     /* STREAM: bit0 streaming (evict-first) stores          */
+    int32_t reserved;
+} sb_tune;
+
+/* ---- library / device ---------------------------------------------------- */
+const char* sb_last_error(void);
+int sb_version(void);
+int sb_device_count(int* count);
+int sb_set_device(int device);
+int sb_device_info(int device, char* name, int name_len, int* sm_count, int* cc_major,
+                   int* cc_minor, size_t* total_mem, int* l2_bytes, int* smem_optin);
+int sb_synchronize(void);
+
+/* ---- memory (reference: stencils/cuda_hip/api.py:54-94 via libcudart) ---- */
+int sb_malloc(void** ptr, size_t bytes);
+int sb_free(void* ptr);
+int sb_malloc_host(void** ptr, size_t bytes); /* page-locked host memory */
+int sb_free_host(void* ptr);
+int sb_memcpy(void* dst, const void* src, size_t bytes, int kind);
+int sb_memcpy_async(void* dst, const void* src, size_t bytes, int kind, void* stream);
+int sb_memset(void* dst, int value, size_t bytes);
+int sb_mem_info(size_t* free_bytes, size_t* total_bytes);
+
+/* ---- streams and events --------------------------------------------------- */
+int sb_stream_create(void** stream);
+int sb_stream_destroy(void* stream);
+int sb_stream_synchronize(void* stream);
+int sb_event_create(void** event);
+int sb_event_destroy(void* event);
+int sb_event_record(void* event, void* stream);
+int sb_event_elapsed(void* start, void* stop, double* seconds);
+int sb_event_synchronize(void* event);
+
+/* Overwrite an internal device buffer larger than L2 on `stream` so that the
+ * next kernel starts cold (the reference cycles `data_sets` for the same
+ * purpose, stencils/base.py:47-51,152). */
+int sb_l2_flush(void* stream);
+
+/* ---- STREAM (reference: stream/cuda_hip.j2:132-173, run() 179-288) --------
+ * op: 0 init (a=1, b=2, c=0), 1 copy (c=a), 2 scale (b=s*c), 3 add (c=a+b),
+ *     4 triad (a=b+s*c).  dtype SB_F64 or SB_F32; n elements per array.      */
+#define SB_STREAM_INIT 0
+#define SB_STREAM_COPY 1
+#define SB_STREAM_SCALE 2
+#define SB_STREAM_ADD 3
+#define SB_STREAM_TRIAD 4
+int sb_stream_op(int op, int dtype, void* a, void* b, void* c, double scalar, int64_t n,
+                 const sb_tune* tune, void* stream, double* time_s);
+
+/* ---- basic stencils (reference: stencils/cuda_hip/basic.py:115-132 bodies,
+ *      oracles stencils/base.py:180-254) -------------------------------------- */
+int sb_copy(int storage, const void* inp, void* out, int64_t ni, int64_t nj, int64_t nk,
+            int64_t si, int64_t sj, int64_t sk, const sb_tune* tune, void* stream,
+            double* time_s);
+/* along_mask: bit0 x, bit1 y, bit2 z (LaplacianStencil along_x/y/z) */
+int sb_laplacian(int storage, int compute, const void* inp, void* out, int64_t ni, int64_t nj,
+                 int64_t nk, int64_t si, int64_t sj, int64_t sk, int along_mask,
+                 const sb_tune* tune, void* stream, double* time_s);
+/* symmetric 0: (inp[+1] + inp) / 2; symmetric 1: (inp[+1] + inp[-1]) / 2 */
+int sb_average(int storage, int compute, const void* inp, void* out, int64_t ni, int64_t nj,
+               int64_t nk, int64_t si, int64_t sj, int64_t sk, int axis, int symmetric,
+               const sb_tune* tune, void* stream, double* time_s);
+
+/* ---- horizontal diffusion (reference: stencils/cuda_hip/horizontal_diffusion.py,
+ *      oracle stencils/base.py:276-311).  Needs a halo of >= 2 in i and j.    */
+int sb_hdiff(int storage, int compute, const void* inp, const void* coeff, void* out,
+             int64_t ni, int64_t nj, int64_t nk, int64_t si, int64_t sj, int64_t sk,
+             const sb_tune* tune, void* stream, double* time_s);
+
+/* ---- vertical advection, one velocity component (reference:
+ *      stencils/cuda_hip/vertical_advection.py, oracle stencils/base.py:410-473).
+ * The new tensstage is written to `out`; pass out == tensstage for the
+ * reference's in-place update (any other overlap is not allowed).  wcon is
+ * read at the column shifted by (wshift_i, wshift_j): (1,0) for u, (0,1)
+ * for v, (0,0) for w.  ccol/dcol may be NULL; they are only used as scratch
+ * by SB_VADV_GLOBAL (the reference's fields of the same names, compute
+ * type).  Needs nk >= 2.                                                    */
+int sb_vadv(int storage, int compute, const void* stage, const void* pos, const void* tens,
+            const void* tensstage, const void* wcon, void* out, void* ccol, void* dcol, int64_t ni,
+            int64_t nj, int64_t nk, int64_t si, int64_t sj, int64_t sk, int wshift_i, int wshift_j,
+            const sb_tune* tune, void* stream, double* time_s);
+
+/* ---- measurement helpers ---------------------------------------------------- */
+/* Throughput of dependent-free fp64 / fp32 arithmetic on this device, in
+ * operations per second (kind 0: f64 add, 1: f64 fma, 2: f32 fma). */
+int sb_probe_arith_rate(int kind, double* ops_per_s);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SBGB300_H */

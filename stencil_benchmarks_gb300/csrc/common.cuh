@@ -1,0 +1,239 @@
+// Shared helpers of the sbgb300 library: error reporting, element types,
+// correctly rounded arithmetic, device properties and the timed-launch
+// wrapper used by every entry point.
+#pragma once
+
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstdio>
+
+#include "../../include/sbgb300.h"
+
+namespace sb {
+
+// ---------------------------------------------------------------------------
+// errors: a per-thread message, read back with sb_last_error()
+// ---------------------------------------------------------------------------
+int fail(int code, const char* fmt, ...) __attribute__((format(printf, 2, 3)));
+void clear_error();
+
+#define SB_CUDA(call)                                                                  \
+    do {                                                                               \
+        cudaError_t sb_e_ = (call);                                                    \
+        if (sb_e_ != cudaSuccess) {                                                    \
+            return ::sb::fail(SB_ERR_CUDA, "%s failed: %s", #call,                     \
+                              cudaGetErrorString(sb_e_));                              \
+        }                                                                              \
+    } while (0)
+
+#define SB_CHECK(cond, code, ...)                                                      \
+    do {                                                                               \
+        if (!(cond)) return ::sb::fail((code), __VA_ARGS__);                           \
+    } while (0)
+
+// ---------------------------------------------------------------------------
+// device properties (cached per device)
+// ---------------------------------------------------------------------------
+struct DeviceProps {
+    int device;
+    int sm_count;
+    int max_threads_per_block;
+    int max_grid_y, max_grid_z;
+    int smem_optin;  // max dynamic shared memory per block after opt-in
+    int l2_bytes;
+};
+int device_props(const DeviceProps** out);
+
+// ---------------------------------------------------------------------------
+// element types
+// ---------------------------------------------------------------------------
+using bf16 = __nv_bfloat16;
+
+inline int storage_size(int t) { return t == SB_F64 ? 8 : t == SB_F32 ? 4 : t == SB_BF16 ? 2 : 0; }
+
+// load a storage element as compute type C (read-only path)
+template <class C, class S>
+__device__ __forceinline__ C ld(const S* p);
+template <>
+__device__ __forceinline__ double ld<double, double>(const double* p) { return __ldg(p); }
+template <>
+__device__ __forceinline__ float ld<float, float>(const float* p) { return __ldg(p); }
+template <>
+__device__ __forceinline__ double ld<double, float>(const float* p) { return (double)__ldg(p); }
+template <>
+__device__ __forceinline__ float ld<float, bf16>(const bf16* p) {
+    return __bfloat162float(__ldg(p));
+}
+template <>
+__device__ __forceinline__ double ld<double, bf16>(const bf16* p) {
+    return (double)__bfloat162float(__ldg(p));
+}
+
+// load through the coherent path (for fields the same kernel also writes)
+template <class C, class S>
+__device__ __forceinline__ C ldc(const S* p);
+template <>
+__device__ __forceinline__ double ldc<double, double>(const double* p) { return *p; }
+template <>
+__device__ __forceinline__ float ldc<float, float>(const float* p) { return *p; }
+template <>
+__device__ __forceinline__ double ldc<double, float>(const float* p) { return (double)*p; }
+template <>
+__device__ __forceinline__ float ldc<float, bf16>(const bf16* p) { return __bfloat162float(*p); }
+template <>
+__device__ __forceinline__ double ldc<double, bf16>(const bf16* p) {
+    return (double)__bfloat162float(*p);
+}
+
+// store a compute value into storage type S with one rounding
+template <class S, class C>
+__device__ __forceinline__ void st(S* p, C v);
+template <>
+__device__ __forceinline__ void st<double, double>(double* p, double v) { *p = v; }
+template <>
+__device__ __forceinline__ void st<float, float>(float* p, float v) { *p = v; }
+template <>
+__device__ __forceinline__ void st<float, double>(float* p, double v) { *p = __double2float_rn(v); }
+template <>
+__device__ __forceinline__ void st<bf16, float>(bf16* p, float v) { *p = __float2bfloat16_rn(v); }
+
+// ---------------------------------------------------------------------------
+// arithmetic with exactly one IEEE rounding per operation (never contracted
+// into FMA), matching numpy's evaluation of the reference's verification.
+// ---------------------------------------------------------------------------
+template <class C>
+struct Ar;
+template <>
+struct Ar<double> {
+    static __device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, b); }
+    static __device__ __forceinline__ double sub(double a, double b) { return __dsub_rn(a, b); }
+    static __device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
+    static __device__ __forceinline__ double div(double a, double b) { return __ddiv_rn(a, b); }
+    static __device__ __forceinline__ double rcp(double a) { return __drcp_rn(a); }
+
+    // Exact x * 2^e for small |e|: adjusts the exponent field with integer
+    // arithmetic when x and the result are normal numbers, otherwise falls
+    // back to a (correctly rounded) multiplication.  Saves an fp64 pipe slot.
+    template <int E>
+    static __device__ __forceinline__ double scale2(double x) {
+        const int hi = __double2hiint(x);
+        const int e = (hi >> 20) & 0x7ff;
+        const int en = e + E;
+        if (e >= 1 && e <= 2046 && en >= 1 && en <= 2046) {
+            return __hiloint2double(hi + E * (1 << 20), __double2loint(x));
+        }
+        return __dmul_rn(x, E >= 0 ? (double)(1 << (E >= 0 ? E : 0))
+                                   : 1.0 / (double)(1 << (E >= 0 ? 0 : -E)));
+    }
+
+    // Exact `(f * (a1 - a0) > 0) ? 0 : f` (the reference's flux limiter).
+    // Sign logic on the bit patterns replaces the fp64 subtract, multiply
+    // and compare whenever the product provably neither underflows nor
+    // involves zero/inf/nan; the rare remaining cases evaluate it literally.
+    static __device__ __forceinline__ double limit(double f, double a1, double a0) {
+        const int hf = __double2hiint(f);
+        const int h1 = __double2hiint(a1);
+        const int h0 = __double2hiint(a0);
+        const unsigned ef = ((unsigned)hf >> 20) & 0x7ffu;
+        const unsigned e1 = ((unsigned)h1 >> 20) & 0x7ffu;
+        const unsigned e0 = ((unsigned)h0 >> 20) & 0x7ffu;
+        const unsigned emin = e1 < e0 ? e1 : e0;
+        const long long b1 = __double_as_longlong(a1);
+        const long long b0 = __double_as_longlong(a0);
+        // f, a1, a0 finite normal; a1 != a0; |f| * |a1 - a0| >= 2^(ef-1023) * 2^(emin-1075)
+        // stays above the underflow threshold 2^-1075 when ef + emin >= 1024.
+        if (ef - 1u < 2046u && e1 - 1u < 2046u && e0 - 1u < 2046u && b1 != b0 && ef + emin >= 1024u) {
+            // sign(a1 - a0): compare as sign-magnitude integers
+            bool gt;
+            if ((b1 ^ b0) < 0) {
+                gt = b1 >= 0;  // different signs: the non-negative one is larger
+            } else {
+                gt = (b1 >= 0) ? (b1 > b0) : (b1 < b0);
+            }
+            const bool fpos = hf >= 0;
+            return (fpos == gt) ? 0.0 : f;  // same sign -> product > 0 -> limited
+        }
+        return (__dmul_rn(f, __dsub_rn(a1, a0)) > 0.0) ? 0.0 : f;
+    }
+
+    // -x, except that (a - b) and (b - a) both give +0 when a == b: returns
+    // the exact value of (b - a) given x = (a - b).
+    static __device__ __forceinline__ double neg_diff(double x, double a, double b) {
+        return ((__double_as_longlong(x) << 1) == 0) ? __dsub_rn(b, a) : -x;
+    }
+};
+
+template <>
+struct Ar<float> {
+    static __device__ __forceinline__ float add(float a, float b) { return __fadd_rn(a, b); }
+    static __device__ __forceinline__ float sub(float a, float b) { return __fsub_rn(a, b); }
+    static __device__ __forceinline__ float mul(float a, float b) { return __fmul_rn(a, b); }
+    static __device__ __forceinline__ float div(float a, float b) { return __fdiv_rn(a, b); }
+    static __device__ __forceinline__ float rcp(float a) { return __frcp_rn(a); }
+    template <int E>
+    static __device__ __forceinline__ float scale2(float x) {
+        return __fmul_rn(x, E >= 0 ? (float)(1 << (E >= 0 ? E : 0))
+                                   : 1.0f / (float)(1 << (E >= 0 ? 0 : -E)));
+    }
+    static __device__ __forceinline__ float limit(float f, float a1, float a0) {
+        return (__fmul_rn(f, __fsub_rn(a1, a0)) > 0.0f) ? 0.0f : f;
+    }
+    static __device__ __forceinline__ float neg_diff(float x, float a, float b) {
+        return (x == 0.0f) ? __fsub_rn(b, a) : -x;
+    }
+};
+
+// ---------------------------------------------------------------------------
+// launch helpers
+// ---------------------------------------------------------------------------
+
+// Run `launch()` on `stream`; with `time_s` non-NULL time it with CUDA events
+// (reference: stencils/cuda_hip/templates/base.j2:145-190).
+template <class F>
+int timed(cudaStream_t stream, double* time_s, F&& launch) {
+    cudaEvent_t start = nullptr, stop = nullptr;
+    if (time_s) {
+        SB_CUDA(cudaEventCreate(&start));
+        cudaError_t e = cudaEventCreate(&stop);
+        if (e != cudaSuccess) {
+            cudaEventDestroy(start);
+            return fail(SB_ERR_CUDA, "cudaEventCreate failed: %s", cudaGetErrorString(e));
+        }
+        e = cudaEventRecord(start, stream);
+        if (e != cudaSuccess) {
+            cudaEventDestroy(start);
+            cudaEventDestroy(stop);
+            return fail(SB_ERR_CUDA, "cudaEventRecord failed: %s", cudaGetErrorString(e));
+        }
+    }
+    int rc = launch();
+    if (rc == SB_OK) {
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) rc = fail(SB_ERR_CUDA, "kernel launch failed: %s", cudaGetErrorString(e));
+    }
+    if (time_s) {
+        if (rc == SB_OK) {
+            cudaError_t e = cudaEventRecord(stop, stream);
+            if (e == cudaSuccess) e = cudaEventSynchronize(stop);
+            float ms = 0.f;
+            if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, start, stop);
+            if (e != cudaSuccess) {
+                rc = fail(SB_ERR_CUDA, "timing the launch failed: %s", cudaGetErrorString(e));
+            } else {
+                *time_s = (double)ms / 1000.0;
+            }
+        }
+        cudaEventDestroy(start);
+        cudaEventDestroy(stop);
+    }
+    return rc;
+}
+
+inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
+
+// Shared validation of a 3D field description.
+int check_domain(int64_t ni, int64_t nj, int64_t nk, int64_t si, int64_t sj, int64_t sk);
+
+}  // namespace sb

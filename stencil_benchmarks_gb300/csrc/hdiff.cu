@@ -1,0 +1,184 @@
+// Horizontal diffusion (hdiff) on sm_103a.
+//
+// Oracle: stencil_benchmarks/benchmarks_collection/stencils/base.py:276-311
+//   lap = 4*inp - (((inp[i+1] + inp[i-1]) + inp[j+1]) + inp[j-1])
+//   flx = lap[i+1] - lap[i];  flx = 0 where flx * (inp[i+1] - inp[i]) > 0
+//   fly = lap[j+1] - lap[j];  fly = 0 where fly * (inp[j+1] - inp[j]) > 0
+//   out = inp - coeff * (((flx[i] - flx[i-1]) + fly[j]) - fly[j-1])
+// Every operation is rounded once, in this order, so fp64 results are
+// bit-identical to the reference's numpy verification.
+//
+// TILE variant: a CTA owns a TX x TY tile of (i, j) and walks KPER k-planes.
+// Per plane it stages inp with its 2-point halo in shared memory, then
+// computes lap on (TX+2) x (TY+2), flx on (TX+1) x TY and fly on TX x (TY+1)
+// -- each value once per tile, not five times per point -- and finally the
+// output, reading coeff and writing out straight from/to HBM with coalesced
+// accesses along i.  On GB300 the fp64 pipe (1/64 of the fp32 rate) is the
+// binding resource for the fp64 form, so the kernel minimises fp64
+// instructions: 4*inp is an exponent increment and the limiter's sign test
+// runs on integer bit patterns (Ar<double>::scale2 / ::limit).
+//
+// Caller contract: inp is readable on [-2, ni+1] x [-2, nj+1] x [0, nk)
+// relative to the interior pointer (a halo of at least 2 in i and j).
+#include "common.cuh"
+
+namespace sb {
+namespace {
+
+template <class C>
+struct HdiffSmem {
+    static size_t bytes(int tx, int ty) {
+        return sizeof(C) * (size_t)((ty + 4) * (tx + 4) + (ty + 2) * (tx + 2) + ty * (tx + 1) + (ty + 1) * tx);
+    }
+};
+
+template <class S, class C, int TX, int NTY>
+__global__ void __launch_bounds__(TX* NTY)
+    hdiff_tile_kernel(const S* __restrict__ inp, const S* __restrict__ coeff, S* __restrict__ out,
+                      int ni, int nj, int nk, int64_t si, int64_t sj, int64_t sk, int TY, int kper) {
+    using A = Ar<C>;
+    constexpr int WI = TX + 4, WL = TX + 2, WF = TX + 1, WY = TX;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    C* s_in = reinterpret_cast<C*>(smem_raw);  // (TY+4) x WI
+    C* s_lap = s_in + (TY + 4) * WI;            // (TY+2) x WL
+    C* s_flx = s_lap + (TY + 2) * WL;           // TY x WF
+    C* s_fly = s_flx + TY * WF;                 // (TY+1) x WY
+
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY;
+    const int k0 = blockIdx.z * kper;
+    const int k1 = min(nk, k0 + kper);
+    const int ilim = ni + 1 - (i0 - 2);  // staged column ii is inside the halo'd array iff ii <= ilim
+    const int jlim = nj + 1 - (j0 - 2);
+
+    for (int k = k0; k < k1; ++k) {
+        const S* in_k = inp + (int64_t)k * sk + (int64_t)(i0 - 2) * si + (int64_t)(j0 - 2) * sj;
+        for (int jj = ty; jj < TY + 4; jj += NTY) {
+            for (int ii = tx; ii < WI; ii += TX) {
+                C v = C(0);
+                if (ii <= ilim && jj <= jlim) v = ld<C, S>(in_k + (int64_t)ii * si + (int64_t)jj * sj);
+                s_in[jj * WI + ii] = v;
+            }
+        }
+        __syncthreads();
+
+        // lap at local (ii, jj) <-> global (i0-1+ii, j0-1+jj)
+        for (int jj = ty; jj < TY + 2; jj += NTY) {
+            for (int ii = tx; ii < WL; ii += TX) {
+                const C* c = s_in + (jj + 1) * WI + ii + 1;
+                const C sum = A::add(A::add(A::add(c[1], c[-1]), c[WI]), c[-WI]);
+                s_lap[jj * WL + ii] = A::sub(A::template scale2<2>(c[0]), sum);
+            }
+        }
+        __syncthreads();
+
+        // flx at local (ii, jj) <-> global (i0-1+ii, j0+jj)
+        for (int jj = ty; jj < TY; jj += NTY) {
+            for (int ii = tx; ii < WF; ii += TX) {
+                const C* l = s_lap + (jj + 1) * WL + ii;
+                const C* x = s_in + (jj + 2) * WI + ii + 1;
+                s_flx[jj * WF + ii] = A::limit(A::sub(l[1], l[0]), x[1], x[0]);
+            }
+        }
+        // fly at local (ii, jj) <-> global (i0+ii, j0-1+jj)
+        for (int jj = ty; jj < TY + 1; jj += NTY) {
+            for (int ii = tx; ii < WY; ii += TX) {
+                const C* l = s_lap + jj * WL + ii + 1;
+                const C* x = s_in + (jj + 1) * WI + ii + 2;
+                s_fly[jj * WY + ii] = A::limit(A::sub(l[WL], l[0]), x[WI], x[0]);
+            }
+        }
+        __syncthreads();
+
+        // out at local (tx, jj) <-> global (i0+tx, j0+jj)
+        const int gi = i0 + tx;
+        for (int jj = ty; jj < TY; jj += NTY) {
+            const int gj = j0 + jj;
+            if (gi < ni && gj < nj) {
+                const C fx1 = s_flx[jj * WF + tx + 1], fx0 = s_flx[jj * WF + tx];
+                const C fy1 = s_fly[(jj + 1) * WY + tx], fy0 = s_fly[jj * WY + tx];
+                const C x = s_in[(jj + 2) * WI + tx + 2];
+                const int64_t o = (int64_t)k * sk + (int64_t)gi * si + (int64_t)gj * sj;
+                const C cf = ld<C, S>(coeff + o);
+                st<S, C>(out + o, A::sub(x, A::mul(cf, A::sub(A::add(A::sub(fx1, fx0), fy1), fy0))));
+            }
+        }
+        __syncthreads();
+    }
+}
+
+template <class S, class C, int TX, int NTY>
+int launch_tile(const void* inp, const void* coeff, void* out, int64_t ni, int64_t nj, int64_t nk,
+                int64_t si, int64_t sj, int64_t sk, int ty, int kper, cudaStream_t stream,
+                const DeviceProps* p) {
+    const size_t smem = HdiffSmem<C>::bytes(TX, ty);
+    SB_CHECK((int64_t)smem <= p->smem_optin, SB_ERR_INVALID,
+             "hdiff tile %dx%d needs %zu bytes of shared memory (device limit %d)", TX, ty, smem,
+             p->smem_optin);
+    auto kernel = hdiff_tile_kernel<S, C, TX, NTY>;
+    if (smem > 48 * 1024) SB_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const int64_t gx = ceil_div(ni, TX), gy = ceil_div(nj, ty), gz = ceil_div(nk, kper);
+    SB_CHECK(gy <= p->max_grid_y && gz <= p->max_grid_z, SB_ERR_INVALID, "hdiff grid too large");
+    kernel<<<dim3((unsigned)gx, (unsigned)gy, (unsigned)gz), dim3(TX, NTY), smem, stream>>>(
+        (const S*)inp, (const S*)coeff, (S*)out, (int)ni, (int)nj, (int)nk, si, sj, sk, ty, kper);
+    return SB_OK;
+}
+
+template <class S, class C>
+int launch_typed(const void* inp, const void* coeff, void* out, int64_t ni, int64_t nj, int64_t nk,
+                 int64_t si, int64_t sj, int64_t sk, const sb_tune* tune, cudaStream_t stream) {
+    const DeviceProps* p;
+    int rc = device_props(&p);
+    if (rc) return rc;
+    const int variant = tune ? tune->variant : SB_VARIANT_AUTO;
+    SB_CHECK(variant == SB_VARIANT_AUTO || variant == SB_HDIFF_TILE, SB_ERR_UNSUPPORTED,
+             "hdiff variant %d is not available", variant);
+    const int bx = (tune && tune->block_x > 0) ? tune->block_x : 64;
+    const int by = (tune && tune->block_y > 0) ? tune->block_y : 4;
+    int ty = (tune && tune->tile_y > 0) ? tune->tile_y : 16;
+    int kper = (tune && tune->k_per_cta > 0) ? tune->k_per_cta : 4;
+    SB_CHECK(ty >= by && ty <= 256, SB_ERR_INVALID, "tile_y must be in [block_y, 256]");
+#define SB_HDIFF_CASE(TXV, NTYV)                                                            \
+    if (bx == TXV && by == NTYV)                                                            \
+        return launch_tile<S, C, TXV, NTYV>(inp, coeff, out, ni, nj, nk, si, sj, sk, ty, kper, stream, p);
+    SB_HDIFF_CASE(32, 4)
+    SB_HDIFF_CASE(32, 8)
+    SB_HDIFF_CASE(64, 2)
+    SB_HDIFF_CASE(64, 4)
+    SB_HDIFF_CASE(64, 8)
+    SB_HDIFF_CASE(128, 2)
+    SB_HDIFF_CASE(128, 4)
+#undef SB_HDIFF_CASE
+    return fail(SB_ERR_UNSUPPORTED,
+                "hdiff block (%d, %d) not instantiated; use 32x{4,8}, 64x{2,4,8} or 128x{2,4}", bx, by);
+}
+
+}  // namespace
+}  // namespace sb
+
+using namespace sb;
+
+extern "C" int sb_hdiff(int storage, int compute, const void* inp, const void* coeff, void* out,
+                        int64_t ni, int64_t nj, int64_t nk, int64_t si, int64_t sj, int64_t sk,
+                        const sb_tune* tune, void* stream, double* time_s) {
+    clear_error();
+    int rc = check_domain(ni, nj, nk, si, sj, sk);
+    if (rc) return rc;
+    SB_CHECK(inp && coeff && out, SB_ERR_INVALID, "NULL field pointer");
+    if (ni == 0 || nj == 0 || nk == 0) {
+        if (time_s) *time_s = 0.0;
+        return SB_OK;
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    return timed(s, time_s, [&]() {
+        if (storage == SB_F64 && compute == SB_F64)
+            return launch_typed<double, double>(inp, coeff, out, ni, nj, nk, si, sj, sk, tune, s);
+        if (storage == SB_F32 && compute == SB_F32)
+            return launch_typed<float, float>(inp, coeff, out, ni, nj, nk, si, sj, sk, tune, s);
+        if (storage == SB_F32 && compute == SB_F64)
+            return launch_typed<float, double>(inp, coeff, out, ni, nj, nk, si, sj, sk, tune, s);
+        if (storage == SB_BF16 && compute == SB_F32)
+            return launch_typed<bf16, float>(inp, coeff, out, ni, nj, nk, si, sj, sk, tune, s);
+        return fail(SB_ERR_UNSUPPORTED, "unsupported storage/compute combination (%d, %d)", storage, compute);
+    });
+}

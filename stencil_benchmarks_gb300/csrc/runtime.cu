@@ -1,0 +1,322 @@
+// Library plumbing behind the C ABI: error strings, device queries, memory,
+// streams/events, L2 flush and the arithmetic-rate probe.
+#include <cstdarg>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+
+namespace sb {
+
+namespace {
+thread_local std::string g_error;
+
+std::mutex g_props_mutex;
+std::vector<DeviceProps> g_props;  // indexed by device, device == -1 when unset
+}  // namespace
+
+int fail(int code, const char* fmt, ...) {
+    char buf[1024];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_error = buf;
+    return code;
+}
+
+void clear_error() { g_error.clear(); }
+
+int device_props(const DeviceProps** out) {
+    int dev = 0;
+    SB_CUDA(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lock(g_props_mutex);
+    if ((int)g_props.size() <= dev) g_props.resize(dev + 1, DeviceProps{-1, 0, 0, 0, 0, 0, 0});
+    DeviceProps& p = g_props[dev];
+    if (p.device != dev) {
+        cudaDeviceProp prop;
+        SB_CUDA(cudaGetDeviceProperties(&prop, dev));
+        p.sm_count = prop.multiProcessorCount;
+        p.max_threads_per_block = prop.maxThreadsPerBlock;
+        p.max_grid_y = prop.maxGridSize[1];
+        p.max_grid_z = prop.maxGridSize[2];
+        p.smem_optin = (int)prop.sharedMemPerBlockOptin;
+        p.l2_bytes = prop.l2CacheSize;
+        p.device = dev;
+    }
+    *out = &p;
+    return SB_OK;
+}
+
+int check_domain(int64_t ni, int64_t nj, int64_t nk, int64_t si, int64_t sj, int64_t sk) {
+    SB_CHECK(ni >= 0 && nj >= 0 && nk >= 0, SB_ERR_INVALID,
+             "negative domain size (%lld, %lld, %lld)", (long long)ni, (long long)nj, (long long)nk);
+    SB_CHECK(ni < (1LL << 31) && nj < (1LL << 31) && nk < (1LL << 31), SB_ERR_INVALID,
+             "domain size exceeds 2^31 along an axis");
+    SB_CHECK(si != 0 && sj != 0 && sk != 0, SB_ERR_INVALID, "zero stride");
+    return SB_OK;
+}
+
+// ---------------------------------------------------------------------------
+// L2 flush buffer (one per device, grown on demand)
+// ---------------------------------------------------------------------------
+namespace {
+std::mutex g_flush_mutex;
+std::vector<std::pair<void*, size_t>> g_flush;
+
+__global__ void flush_kernel(uint4* buf, size_t n, unsigned salt) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+         i += (size_t)gridDim.x * blockDim.x) {
+        buf[i] = make_uint4(salt, (unsigned)i, salt ^ 0x5bd1e995u, (unsigned)(i >> 32));
+    }
+}
+
+// Dependent-free arithmetic chains for the rate probe: each thread runs 8
+// independent accumulators so the pipe, not latency, is the limit.
+template <int KIND>
+__global__ void arith_probe_kernel(double* out, int iters, double x) {
+    if (KIND == 2) {
+        float a[8];
+        for (int u = 0; u < 8; ++u) a[u] = (float)x + (float)(threadIdx.x + u);
+        const float m = 0.999f, c = 1e-3f;
+        for (int it = 0; it < iters; ++it) {
+#pragma unroll
+            for (int u = 0; u < 8; ++u) a[u] = __fmaf_rn(a[u], m, c);
+        }
+        float s = 0.f;
+        for (int u = 0; u < 8; ++u) s += a[u];
+        if (s == 12345.678f) out[0] = s;
+    } else {
+        double a[8];
+        for (int u = 0; u < 8; ++u) a[u] = x + (double)(threadIdx.x + u);
+        const double m = 0.999, c = 1e-3;
+        for (int it = 0; it < iters; ++it) {
+#pragma unroll
+            for (int u = 0; u < 8; ++u) a[u] = KIND == 0 ? __dadd_rn(a[u], c) : __fma_rn(a[u], m, c);
+        }
+        double s = 0.0;
+        for (int u = 0; u < 8; ++u) s += a[u];
+        if (s == 12345.678) out[0] = s;
+    }
+}
+}  // namespace
+
+}  // namespace sb
+
+using namespace sb;
+
+extern "C" {
+
+const char* sb_last_error(void) { return g_error.c_str(); }
+
+int sb_version(void) { return 10000; }
+
+int sb_device_count(int* count) {
+    SB_CHECK(count, SB_ERR_INVALID, "count is NULL");
+    *count = 0;
+    cudaError_t e = cudaGetDeviceCount(count);
+    if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) {
+        cudaGetLastError();
+        *count = 0;
+        return SB_OK;
+    }
+    SB_CUDA(e);
+    return SB_OK;
+}
+
+int sb_set_device(int device) {
+    SB_CUDA(cudaSetDevice(device));
+    return SB_OK;
+}
+
+int sb_device_info(int device, char* name, int name_len, int* sm_count, int* cc_major,
+                   int* cc_minor, size_t* total_mem, int* l2_bytes, int* smem_optin) {
+    cudaDeviceProp prop;
+    SB_CUDA(cudaGetDeviceProperties(&prop, device));
+    if (name && name_len > 0) {
+        strncpy(name, prop.name, (size_t)name_len - 1);
+        name[name_len - 1] = '\0';
+    }
+    if (sm_count) *sm_count = prop.multiProcessorCount;
+    if (cc_major) *cc_major = prop.major;
+    if (cc_minor) *cc_minor = prop.minor;
+    if (total_mem) *total_mem = prop.totalGlobalMem;
+    if (l2_bytes) *l2_bytes = prop.l2CacheSize;
+    if (smem_optin) *smem_optin = (int)prop.sharedMemPerBlockOptin;
+    return SB_OK;
+}
+
+int sb_synchronize(void) {
+    SB_CUDA(cudaDeviceSynchronize());
+    return SB_OK;
+}
+
+int sb_malloc(void** ptr, size_t bytes) {
+    SB_CHECK(ptr, SB_ERR_INVALID, "ptr is NULL");
+    *ptr = nullptr;
+    if (bytes == 0) return SB_OK;
+    cudaError_t e = cudaMalloc(ptr, bytes);
+    if (e == cudaErrorMemoryAllocation) {
+        cudaGetLastError();
+        return fail(SB_ERR_NOMEM, "cudaMalloc of %zu bytes failed: out of device memory", bytes);
+    }
+    SB_CUDA(e);
+    return SB_OK;
+}
+
+int sb_free(void* ptr) {
+    if (ptr) SB_CUDA(cudaFree(ptr));
+    return SB_OK;
+}
+
+int sb_malloc_host(void** ptr, size_t bytes) {
+    SB_CHECK(ptr, SB_ERR_INVALID, "ptr is NULL");
+    *ptr = nullptr;
+    if (bytes == 0) return SB_OK;
+    cudaError_t e = cudaMallocHost(ptr, bytes);
+    if (e == cudaErrorMemoryAllocation) {
+        cudaGetLastError();
+        return fail(SB_ERR_NOMEM, "cudaMallocHost of %zu bytes failed", bytes);
+    }
+    SB_CUDA(e);
+    return SB_OK;
+}
+
+int sb_free_host(void* ptr) {
+    if (ptr) SB_CUDA(cudaFreeHost(ptr));
+    return SB_OK;
+}
+
+int sb_memcpy(void* dst, const void* src, size_t bytes, int kind) {
+    SB_CHECK(kind >= 0 && kind <= 4, SB_ERR_INVALID, "bad memcpy kind %d", kind);
+    if (bytes == 0) return SB_OK;
+    SB_CUDA(cudaMemcpy(dst, src, bytes, (cudaMemcpyKind)kind));
+    return SB_OK;
+}
+
+int sb_memcpy_async(void* dst, const void* src, size_t bytes, int kind, void* stream) {
+    SB_CHECK(kind >= 0 && kind <= 4, SB_ERR_INVALID, "bad memcpy kind %d", kind);
+    if (bytes == 0) return SB_OK;
+    SB_CUDA(cudaMemcpyAsync(dst, src, bytes, (cudaMemcpyKind)kind, (cudaStream_t)stream));
+    return SB_OK;
+}
+
+int sb_memset(void* dst, int value, size_t bytes) {
+    if (bytes == 0) return SB_OK;
+    SB_CUDA(cudaMemset(dst, value, bytes));
+    return SB_OK;
+}
+
+int sb_mem_info(size_t* free_bytes, size_t* total_bytes) {
+    size_t f = 0, t = 0;
+    SB_CUDA(cudaMemGetInfo(&f, &t));
+    if (free_bytes) *free_bytes = f;
+    if (total_bytes) *total_bytes = t;
+    return SB_OK;
+}
+
+int sb_stream_create(void** stream) {
+    SB_CHECK(stream, SB_ERR_INVALID, "stream is NULL");
+    cudaStream_t s;
+    SB_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    *stream = (void*)s;
+    return SB_OK;
+}
+
+int sb_stream_destroy(void* stream) {
+    if (stream) SB_CUDA(cudaStreamDestroy((cudaStream_t)stream));
+    return SB_OK;
+}
+
+int sb_stream_synchronize(void* stream) {
+    SB_CUDA(cudaStreamSynchronize((cudaStream_t)stream));
+    return SB_OK;
+}
+
+int sb_event_create(void** event) {
+    SB_CHECK(event, SB_ERR_INVALID, "event is NULL");
+    cudaEvent_t e;
+    SB_CUDA(cudaEventCreate(&e));
+    *event = (void*)e;
+    return SB_OK;
+}
+
+int sb_event_destroy(void* event) {
+    if (event) SB_CUDA(cudaEventDestroy((cudaEvent_t)event));
+    return SB_OK;
+}
+
+int sb_event_record(void* event, void* stream) {
+    SB_CUDA(cudaEventRecord((cudaEvent_t)event, (cudaStream_t)stream));
+    return SB_OK;
+}
+
+int sb_event_synchronize(void* event) {
+    SB_CUDA(cudaEventSynchronize((cudaEvent_t)event));
+    return SB_OK;
+}
+
+int sb_event_elapsed(void* start, void* stop, double* seconds) {
+    float ms = 0.f;
+    SB_CUDA(cudaEventElapsedTime(&ms, (cudaEvent_t)start, (cudaEvent_t)stop));
+    if (seconds) *seconds = ms / 1000.0;
+    return SB_OK;
+}
+
+int sb_l2_flush(void* stream) {
+    const DeviceProps* p;
+    int rc = device_props(&p);
+    if (rc) return rc;
+    const size_t bytes = (size_t)(p->l2_bytes > 0 ? p->l2_bytes : (128 << 20)) * 2;
+    void* buf = nullptr;
+    {
+        std::lock_guard<std::mutex> lock(g_flush_mutex);
+        if ((int)g_flush.size() <= p->device) g_flush.resize(p->device + 1, {nullptr, 0});
+        auto& slot = g_flush[p->device];
+        if (slot.second < bytes) {
+            if (slot.first) cudaFree(slot.first);
+            slot = {nullptr, 0};
+            void* ptr = nullptr;
+            cudaError_t e = cudaMalloc(&ptr, bytes);
+            if (e != cudaSuccess) {
+                cudaGetLastError();
+                return fail(SB_ERR_NOMEM, "L2 flush buffer allocation failed: %s",
+                            cudaGetErrorString(e));
+            }
+            slot = {ptr, bytes};
+        }
+        buf = slot.first;
+    }
+    static unsigned salt = 1;
+    const size_t n = bytes / sizeof(uint4);
+    flush_kernel<<<p->sm_count * 4, 512, 0, (cudaStream_t)stream>>>((uint4*)buf, n, salt++);
+    SB_CUDA(cudaGetLastError());
+    return SB_OK;
+}
+
+int sb_probe_arith_rate(int kind, double* ops_per_s) {
+    SB_CHECK(kind >= 0 && kind <= 2 && ops_per_s, SB_ERR_INVALID, "bad probe arguments");
+    const DeviceProps* p;
+    int rc = device_props(&p);
+    if (rc) return rc;
+    double* out = nullptr;
+    SB_CUDA(cudaMalloc(&out, sizeof(double)));
+    const int blocks = p->sm_count * 8, threads = 256, iters = kind == 2 ? 8192 : 512;
+    auto launch = [&]() {
+        if (kind == 0) arith_probe_kernel<0><<<blocks, threads>>>(out, iters, 0.5);
+        if (kind == 1) arith_probe_kernel<1><<<blocks, threads>>>(out, iters, 0.5);
+        if (kind == 2) arith_probe_kernel<2><<<blocks, threads>>>(out, iters, 0.5);
+        return SB_OK;
+    };
+    double t = 0.0;
+    rc = timed(nullptr, nullptr, launch);  // warm-up
+    if (rc == SB_OK) rc = timed(nullptr, &t, launch);
+    cudaFree(out);
+    if (rc) return rc;
+    *ops_per_s = (double)blocks * threads * iters * 8.0 / t;
+    return SB_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,350 @@
+"""GPU parity: every kernel against the reference's golden vectors and the
+CPU oracle, through the C ABI.
+
+fp64 forms must be bit-identical to the reference's numpy verification.  The
+reduced-precision forms must be bit-identical to the oracle evaluated on the
+same quantised inputs in the same compute type, then rounded once to the
+storage type.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from oracle import stencils as ora
+from stencil_benchmarks_gb300 import _native, kernels
+from tests.conftest import golden_cases, load_golden
+from tests.gpu_helpers import (
+    VADV_ARGS,
+    VADV_DISTS,
+    bits_equal,
+    compute_view,
+    download_like,
+    host_field,
+    interior,
+    mismatch_report,
+    rng_fields,
+    round_to_storage,
+    to_device,
+)
+
+pytestmark = pytest.mark.gpu
+
+CASES = {k: v for k, v in golden_cases().items() if not k.startswith("_")}
+
+
+def _assert_bits(got, want, what):
+    assert bits_equal(got, want), f"{what}: " + mismatch_report(got, want)
+
+
+# ---------------------------------------------------------------------------
+# golden vectors captured from the reference
+# ---------------------------------------------------------------------------
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_golden(name, lib):
+    meta = CASES[name]
+    data = load_golden(name)
+    storage = meta["dtype"]
+    domain, halo = tuple(meta["domain"]), tuple(meta["halo"])
+    hosts = {n: host_field(data[f"in_{n}"], storage, halo=halo) for n in meta["args"]}
+    dev = {n: to_device(h, storage, halo) for n, h in hosts.items()}
+    kind, params = meta["kind"], meta["params"]
+    if kind == "hdiff":
+        kernels.hdiff(dev["inp"], dev["coeff"], dev["out"])
+        outs = {"out": "out"}
+    elif kind == "vadv":
+        kernels.vadv(dev["ustage"], dev["upos"], dev["utens"], dev["utensstage"], dev["wcon"], (1, 0))
+        outs = {"utensstage": "utensstage"}
+        if params.get("all_components"):
+            kernels.vadv(dev["vstage"], dev["vpos"], dev["vtens"], dev["vtensstage"], dev["wcon"], (0, 1))
+            kernels.vadv(dev["wstage"], dev["wpos"], dev["wtens"], dev["wtensstage"], dev["wcon"], (0, 0))
+            outs.update(vtensstage="vtensstage", wtensstage="wtensstage")
+    elif kind == "copy":
+        kernels.copy(dev["inp"], dev["out"])
+        outs = {"out": "out"}
+    elif kind == "laplacian":
+        along = (params.get("along_x", True), params.get("along_y", True), params.get("along_z", False))
+        kernels.laplacian(dev["inp"], dev["out"], along)
+        outs = {"out": "out"}
+    elif kind in ("onesided_average", "symmetric_average"):
+        kernels.average(dev["inp"], dev["out"], params["axis"], kind == "symmetric_average")
+        outs = {"out": "out"}
+    else:
+        raise AssertionError(kind)
+    _native.synchronize()
+    for expected_name, field_name in outs.items():
+        got = interior(download_like(dev[field_name], hosts[field_name]), domain, halo)
+        _assert_bits(got, data[f"expected_{expected_name}"], f"{name}:{expected_name}")
+
+
+# ---------------------------------------------------------------------------
+# horizontal diffusion: shapes, layouts, tunings, precisions
+# ---------------------------------------------------------------------------
+
+FORMS = [("float64", "float64"), ("float32", "float32"), ("bfloat16", "float32"), ("float32", "float64")]
+
+
+def _run_hdiff(domain, halo, storage="float64", compute="float64", layout=(2, 1, 0), alignment=0,
+               tune=None, seed=0):
+    shape = tuple(d + 2 * h for d, h in zip(domain, halo))
+    vals = rng_fields(seed, shape, ("inp", "coeff", "out"), {})
+    hosts = {n: host_field(v, storage, layout, alignment, halo) for n, v in vals.items()}
+    dev = {n: to_device(h, storage, halo) for n, h in hosts.items()}
+    kernels.hdiff(dev["inp"], dev["coeff"], dev["out"], compute=compute, tune=tune)
+    got = interior(download_like(dev["out"], hosts["out"]), domain, halo)
+    want = ora.hdiff(compute_view(hosts["inp"], storage, compute),
+                     compute_view(hosts["coeff"], storage, compute), domain, halo)
+    return got, round_to_storage(want, storage), hosts
+
+
+@pytest.mark.parametrize("storage,compute", FORMS)
+def test_hdiff_forms(storage, compute, lib):
+    got, want, _ = _run_hdiff((150, 97, 6), (2, 2, 0), storage, compute, seed=5)
+    _assert_bits(got, want, f"hdiff {storage}/{compute}")
+
+
+@pytest.mark.parametrize(
+    "domain,halo,layout,alignment",
+    [
+        ((77, 45, 3), (3, 3, 1), (2, 1, 0), 64),
+        ((64, 16, 5), (2, 2, 0), (2, 1, 0), 0),
+        ((1, 1, 1), (2, 2, 0), (2, 1, 0), 0),
+        ((33, 130, 2), (2, 4, 2), (0, 1, 2), 0),
+        ((40, 21, 9), (2, 2, 1), (1, 2, 0), 32),
+    ],
+)
+def test_hdiff_shapes_layouts(domain, halo, layout, alignment, lib):
+    got, want, _ = _run_hdiff(domain, halo, layout=layout, alignment=alignment, seed=7)
+    _assert_bits(got, want, f"hdiff {domain} {halo} {layout}")
+
+
+@pytest.mark.parametrize("bx,by,ty,kper", [(32, 4, 8, 1), (32, 8, 24, 3), (64, 2, 2, 7), (64, 8, 32, 2),
+                                           (128, 2, 4, 1), (128, 4, 16, 5)])
+def test_hdiff_tunings(bx, by, ty, kper, lib):
+    t = _native.tune(variant=_native.HDIFF_TILE, block_x=bx, block_y=by, tile_y=ty, k_per_cta=kper)
+    got, want, _ = _run_hdiff((131, 70, 11), (2, 2, 0), tune=t, seed=9)
+    _assert_bits(got, want, f"hdiff tune {bx}x{by} ty{ty} k{kper}")
+
+
+def test_hdiff_special_values(lib):
+    """Ties, zeros, signed zeros, tiny and huge values, inf and nan."""
+    domain, halo = (40, 12, 3), (2, 2, 0)
+    shape = tuple(d + 2 * h for d, h in zip(domain, halo))
+    rng = np.random.Generator(np.random.PCG64(3))
+    specials = np.array([0.0, -0.0, 1.0, 1.0, 0.5, 1e-300, -1e-300, 5e-324, 1e300, -1e300, np.inf,
+                         -np.inf, np.nan, 2.0, 0.125], dtype=np.float64)
+    # a third special values, a third coarse values (exact ties), a third random
+    pick = rng.integers(0, 3, size=shape)
+    inp = np.where(pick == 0, rng.choice(specials, size=shape),
+                   np.where(pick == 1, rng.integers(0, 4, size=shape) / 4.0, rng.random(shape)))
+    coeff = np.where(rng.random(shape) < 0.2, rng.choice(specials, size=shape), rng.random(shape))
+    hosts = {"inp": host_field(inp, halo=halo), "coeff": host_field(coeff, halo=halo),
+             "out": host_field(np.zeros(shape), halo=halo)}
+    dev = {n: to_device(h, "float64", halo) for n, h in hosts.items()}
+    kernels.hdiff(dev["inp"], dev["coeff"], dev["out"])
+    got = interior(download_like(dev["out"], hosts["out"]), domain, halo)
+    with np.errstate(all="ignore"):
+        want = ora.hdiff(np.array(hosts["inp"]), np.array(hosts["coeff"]), domain, halo)
+    _assert_bits(got, want, "hdiff special values")
+
+
+def test_hdiff_empty_domain_is_noop(lib):
+    got, want, _ = _run_hdiff((0, 5, 3), (2, 2, 0))
+    assert got.size == 0 and want.size == 0
+
+
+# ---------------------------------------------------------------------------
+# vertical advection
+# ---------------------------------------------------------------------------
+
+
+def _run_vadv(domain, halo, storage="float64", compute="float64", layout=(2, 1, 0), alignment=0,
+              tune=None, seed=0, shift=(1, 0), use_scratch=False):
+    shape = tuple(d + 2 * h for d, h in zip(domain, halo))
+    vals = rng_fields(seed, shape, VADV_ARGS, VADV_DISTS)
+    hosts = {n: host_field(v, storage, layout, alignment, halo) for n, v in vals.items()}
+    dev = {n: to_device(h, storage, halo) for n, h in hosts.items()}
+    scratch = {}
+    if use_scratch:
+        for n in ("ccol", "dcol"):
+            h = host_field(np.zeros(shape), compute, layout, alignment, halo)
+            scratch[n] = to_device(h, compute, halo)
+    kernels.vadv(dev["ustage"], dev["upos"], dev["utens"], dev["utensstage"], dev["wcon"], shift,
+                 ccol=scratch.get("ccol"), dcol=scratch.get("dcol"), compute=compute, tune=tune)
+    got = interior(download_like(dev["utensstage"], hosts["utensstage"]), domain, halo)
+    fields = {n: compute_view(h, storage, compute) for n, h in hosts.items()}
+    comp = ora._vadv_component(fields["ustage"], fields["upos"], fields["utens"], fields["utensstage"],
+                               fields["wcon"], domain, halo, shift[0], shift[1])
+    return got, round_to_storage(comp, storage)
+
+
+@pytest.mark.parametrize("storage,compute", FORMS)
+def test_vadv_forms(storage, compute, lib):
+    got, want = _run_vadv((70, 33, 40), (1, 1, 0), storage, compute, seed=11)
+    _assert_bits(got, want, f"vadv {storage}/{compute}")
+
+
+@pytest.mark.parametrize("shift", [(1, 0), (0, 1), (0, 0)])
+def test_vadv_shifts(shift, lib):
+    got, want = _run_vadv((45, 20, 17), (1, 1, 1), seed=12, shift=shift)
+    _assert_bits(got, want, f"vadv shift {shift}")
+
+
+@pytest.mark.parametrize("variant,bx,by", [(1, 32, 1), (1, 64, 2), (1, 16, 4), (2, 32, 1), (2, 128, 2)])
+def test_vadv_variants(variant, bx, by, lib):
+    t = _native.tune(variant=variant, block_x=bx, block_y=by)
+    got, want = _run_vadv((97, 19, 23), (1, 1, 0), tune=t, seed=13, use_scratch=(variant == 2))
+    _assert_bits(got, want, f"vadv variant {variant} {bx}x{by}")
+
+
+@pytest.mark.parametrize(
+    "domain,halo,layout,alignment",
+    [((5, 4, 2), (1, 1, 0), (2, 1, 0), 0), ((64, 8, 137), (1, 1, 0), (2, 1, 0), 64),
+     ((31, 9, 12), (2, 3, 1), (0, 1, 2), 0), ((1, 1, 3), (1, 0, 0), (2, 1, 0), 0)],
+)
+def test_vadv_shapes_layouts(domain, halo, layout, alignment, lib):
+    got, want = _run_vadv(domain, halo, layout=layout, alignment=alignment, seed=14)
+    _assert_bits(got, want, f"vadv {domain} {layout}")
+
+
+def test_vadv_rejects_single_level(lib):
+    with pytest.raises(_native.SbError) as err:
+        _run_vadv((8, 4, 1), (1, 1, 0))
+    assert err.value.code == _native.SB_ERR_INVALID
+    assert "at least 2 levels" in err.value.message
+
+
+def test_vadv_global_variant_requires_scratch(lib):
+    t = _native.tune(variant=_native.VADV_GLOBAL)
+    with pytest.raises(_native.SbError) as err:
+        _run_vadv((8, 4, 3), (1, 1, 0), tune=t)
+    assert err.value.code == _native.SB_ERR_INVALID
+
+
+# ---------------------------------------------------------------------------
+# basic stencils beyond the golden cases
+# ---------------------------------------------------------------------------
+
+
+@pytest.mark.parametrize("storage,compute", FORMS)
+@pytest.mark.parametrize("along", [(True, True, False), (True, True, True), (False, False, True), (False,) * 3])
+def test_laplacian_forms(storage, compute, along, lib):
+    domain, halo = (37, 19, 6), (1, 1, 1)
+    shape = tuple(d + 2 * h for d, h in zip(domain, halo))
+    vals = rng_fields(21, shape, ("inp", "out"), {})
+    hosts = {n: host_field(v, storage, halo=halo) for n, v in vals.items()}
+    dev = {n: to_device(h, storage, halo) for n, h in hosts.items()}
+    kernels.laplacian(dev["inp"], dev["out"], along, compute=compute)
+    got = interior(download_like(dev["out"], hosts["out"]), domain, halo)
+    want = round_to_storage(ora.laplacian(compute_view(hosts["inp"], storage, compute), domain, halo, along), storage)
+    _assert_bits(got, want, f"laplacian {along} {storage}/{compute}")
+
+
+@pytest.mark.parametrize("storage", ["float64", "float32", "bfloat16"])
+def test_copy_storage(storage, lib):
+    domain, halo = (50, 7, 9), (3, 3, 3)
+    shape = tuple(d + 2 * h for d, h in zip(domain, halo))
+    vals = rng_fields(22, shape, ("inp", "out"), {})
+    hosts = {n: host_field(v, storage, alignment=32, halo=halo) for n, v in vals.items()}
+    dev = {n: to_device(h, storage, halo) for n, h in hosts.items()}
+    kernels.copy(dev["inp"], dev["out"])
+    got = interior(download_like(dev["out"], hosts["out"]), domain, halo)
+    _assert_bits(got, interior(hosts["inp"], domain, halo), f"copy {storage}")
+
+
+# ---------------------------------------------------------------------------
+# STREAM
+# ---------------------------------------------------------------------------
+
+
+def _fma_exact(b, s, c):
+    """Correctly rounded b + s*c for float64 arrays, via exact rationals."""
+    from fractions import Fraction
+
+    out = np.empty_like(b)
+    for idx in range(b.size):
+        exact = Fraction(float(b.flat[idx])) + Fraction(float(s)) * Fraction(float(c.flat[idx]))
+        out.flat[idx] = float(exact)
+    return out
+
+
+@pytest.mark.parametrize("n,offset", [(1 << 16, 0), ((1 << 16) + 3, 0), (1000, 1), (5, 0)])
+def test_stream_ops(n, offset, lib):
+    from stencil_benchmarks_gb300.device import DeviceBuffer, copy_to_device, copy_to_host
+
+    rng = np.random.Generator(np.random.PCG64(31))
+    bufs = [DeviceBuffer((n + offset) * 8) for _ in range(3)]
+    ptrs = [b.ptr + offset * 8 for b in bufs]
+    a0, b0, c0 = (rng.random(n) for _ in range(3))
+
+    def put(p, x):
+        copy_to_device(p, np.ascontiguousarray(x))
+
+    def get(p):
+        x = np.empty(n)
+        copy_to_host(x, p)
+        return x
+
+    for p, x in zip(ptrs, (a0, b0, c0)):
+        put(p, x)
+    kernels.stream_op(_native.STREAM_COPY, "float64", *ptrs, n)
+    assert np.array_equal(get(ptrs[2]), a0)
+    put(ptrs[2], c0)
+    kernels.stream_op(_native.STREAM_SCALE, "float64", *ptrs, n, 3.0)
+    assert bits_equal(get(ptrs[1]), 3.0 * c0)
+    put(ptrs[1], b0)
+    kernels.stream_op(_native.STREAM_ADD, "float64", *ptrs, n)
+    assert bits_equal(get(ptrs[2]), a0 + b0)
+    put(ptrs[2], c0)
+    kernels.stream_op(_native.STREAM_TRIAD, "float64", *ptrs, n, 3.0)
+    got = get(ptrs[0])
+    sample = slice(0, min(n, 2000))
+    assert bits_equal(got[sample], _fma_exact(b0[sample], 3.0, c0[sample]))
+    assert np.all(np.abs(got - (b0 + 3.0 * c0)) <= np.spacing(b0 + 3.0 * c0))
+
+
+@pytest.mark.parametrize("dtype", ["float64", "float32"])
+def test_stream_reference_sequence(dtype, lib, golden):
+    """init + 10 rounds of copy/scale/add/triad give the reference's scalars."""
+    from stencil_benchmarks_gb300.device import DeviceBuffer, copy_to_host
+
+    n = (1 << 18) + 5
+    item = 8 if dtype == "float64" else 4
+    bufs = [DeviceBuffer(n * item) for _ in range(3)]
+    a, b, c = (x.ptr for x in bufs)
+    kernels.stream_op(_native.STREAM_INIT, dtype, a, b, c, n)
+    for _ in range(10):
+        for op in (_native.STREAM_COPY, _native.STREAM_SCALE, _native.STREAM_ADD, _native.STREAM_TRIAD):
+            kernels.stream_op(op, dtype, a, b, c, n, 3.0)
+    want = golden["_stream_scalars"][f"{dtype}_10"]
+    for ptr, w in zip((a, b, c), want):
+        host = np.empty(n, dtype=dtype)
+        copy_to_host(host, ptr)
+        assert np.all(host == np.asarray(w, dtype=dtype))
+
+
+# ---------------------------------------------------------------------------
+# full-size BASELINE configurations (512 x 512 x 80, fp64)
+# ---------------------------------------------------------------------------
+
+
+def test_hdiff_full_size_fp64(lib):
+    got, want, _ = _run_hdiff((512, 512, 80), (2, 2, 0), seed=101)
+    _assert_bits(got, want, "hdiff 512x512x80")
+
+
+def test_vadv_full_size_fp64_against_c_oracle(lib):
+    from oracle import cport
+
+    domain, halo = (512, 512, 80), (1, 1, 0)
+    shape = tuple(d + 2 * h for d, h in zip(domain, halo))
+    vals = rng_fields(102, shape, VADV_ARGS, VADV_DISTS)
+    hosts = {n: host_field(v, halo=halo) for n, v in vals.items()}
+    dev = {n: to_device(h, "float64", halo) for n, h in hosts.items()}
+    kernels.vadv(dev["ustage"], dev["upos"], dev["utens"], dev["utensstage"], dev["wcon"])
+    got = interior(download_like(dev["utensstage"], hosts["utensstage"]), domain, halo)
+    cport.vadv(hosts["ustage"], hosts["upos"], hosts["utens"], hosts["utensstage"], hosts["wcon"], domain, halo)
+    _assert_bits(got, interior(hosts["utensstage"], domain, halo), "vadv 512x512x80")
