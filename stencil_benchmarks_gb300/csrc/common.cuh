@@ -186,6 +186,41 @@ struct Ar<float> {
 };
 
 // ---------------------------------------------------------------------------
+// asynchronous global -> shared copies (cp.async, per thread, 4/8/16 bytes).
+// Completion is tracked per thread in commit groups, so a thread can keep
+// several levels of loads in flight without tying up registers.
+// ---------------------------------------------------------------------------
+template <int BYTES>
+__device__ __forceinline__ void cp_async(void* smem_dst, const void* gsrc) {
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem_dst);
+    if (BYTES == 4) {
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(sa), "l"(gsrc) : "memory");
+    } else if (BYTES == 8) {
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(gsrc) : "memory");
+    } else {
+        static_assert(BYTES == 4 || BYTES == 8 || BYTES == 16, "cp.async copies 4, 8 or 16 bytes");
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gsrc) : "memory");
+    }
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
+// storage -> compute conversion of a value already in registers/shared memory
+template <class C, class S>
+__device__ __forceinline__ C cvt(S v);
+template <>
+__device__ __forceinline__ double cvt<double, double>(double v) { return v; }
+template <>
+__device__ __forceinline__ float cvt<float, float>(float v) { return v; }
+template <>
+__device__ __forceinline__ double cvt<double, float>(float v) { return (double)v; }
+template <>
+__device__ __forceinline__ float cvt<float, bf16>(bf16 v) { return __bfloat162float(v); }
+
+// ---------------------------------------------------------------------------
 // launch helpers
 // ---------------------------------------------------------------------------
 

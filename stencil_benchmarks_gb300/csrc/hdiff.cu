@@ -20,6 +20,8 @@
 //
 // Caller contract: inp is readable on [-2, ni+1] x [-2, nj+1] x [0, nk)
 // relative to the interior pointer (a halo of at least 2 in i and j).
+#include <cstdlib>
+
 #include "common.cuh"
 
 namespace sb {
@@ -107,6 +109,124 @@ __global__ void __launch_bounds__(TX* NTY)
     }
 }
 
+// JSCAN variant: one warp owns 32 consecutive i-columns (lanes) and marches
+// along j; lanes 2..29 produce outputs (28 per warp), lanes 0-1 and 30-31
+// only supply the i-halo.  Per row step a lane loads one inp value and one
+// coeff value; inp(i+-1), lap(i+1) and flx(i-1) come from warp shuffles and
+// inp/lap/fly of the previous rows stay in registers, so every lap, flx and
+// fly of the strip is computed exactly once.  Rows are loaded U at a time
+// (all loads of a chunk issued before its arithmetic) to keep U row
+// requests per warp in flight.  Block = (32, NW) warps side by side in i;
+// grid = (strips of 28*NW columns, j-segments of TY rows, k-chunks of KPER).
+constexpr int kJscanOut = 28;
+
+template <class S, class C, int U, class IDX>
+__global__ void __launch_bounds__(256)
+    hdiff_jscan_kernel(const S* __restrict__ inp, const S* __restrict__ coeff, S* __restrict__ out,
+                       int ni, int nj, int nk, IDX si, IDX sj, IDX sk, int TY, int kper) {
+    using A = Ar<C>;
+    const int lane = threadIdx.x;
+    const int i = (blockIdx.x * blockDim.y + threadIdx.y) * kJscanOut - 2 + lane;  // column of this lane
+    const int j0 = blockIdx.y * TY;
+    const int j1 = min(nj, j0 + TY);  // output rows [j0, j1)
+    const int k0 = blockIdx.z * kper;
+    const int k1 = min(nk, k0 + kper);
+    const bool col_in = i <= ni + 1;  // inside the halo'd array (i >= -2 always)
+    const bool writer = lane >= 2 && lane < 2 + kJscanOut && i < ni;
+    const int rmax = nj + 1;  // last row inside the halo'd array
+
+    for (int k = k0; k < k1; ++k) {
+        const IDX obase = (IDX)k * sk + (IDX)i * si;
+        auto load_row = [&](int r) -> C {
+            return (col_in && r <= rmax) ? ld<C, S>(inp + (obase + (IDX)r * sj)) : C(0);
+        };
+        auto lap_of = [&](C below, C center, C above) -> C {
+            const C left = __shfl_up_sync(0xffffffffu, center, 1);
+            const C right = __shfl_down_sync(0xffffffffu, center, 1);
+            return A::sub(A::template scale2<2>(center), A::add(A::add(A::add(right, left), above), below));
+        };
+        // preamble: rows j0-2 .. j0+1
+        const C am2 = load_row(j0 - 2);
+        C a0 = load_row(j0 - 1);  // inp(j-1) until rotated
+        C a1 = load_row(j0);
+        C a2 = load_row(j0 + 1);
+        const C lap_m1 = lap_of(am2, a0, a1);  // lap(j0-1)
+        C lap0 = lap_of(a0, a1, a2);           // lap(j0)
+        C fly_m1 = A::limit(A::sub(lap0, lap_m1), a1, a0);  // fly(j0-1)
+        C right0 = __shfl_down_sync(0xffffffffu, a1, 1);    // inp(i+1, j0)
+        // state for output row j: a0 = inp(j), a1 = inp(j+1), lap0 = lap(j)
+        a0 = a1;
+        a1 = a2;
+
+        for (int jb = j0; jb < j1; jb += U) {
+            C nxt[U], cf[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const int j = jb + u;
+                nxt[u] = load_row(j + 2);
+                cf[u] = (writer && j < j1) ? ld<C, S>(coeff + (obase + (IDX)j * sj)) : C(0);
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const int j = jb + u;
+                if (jb + u >= j1) break;  // warp-uniform
+                const C a2n = nxt[u];
+                const C left1 = __shfl_up_sync(0xffffffffu, a1, 1);
+                const C right1 = __shfl_down_sync(0xffffffffu, a1, 1);
+                const C lap1 = A::sub(A::template scale2<2>(a1), A::add(A::add(A::add(right1, left1), a2n), a0));
+                const C fly0 = A::limit(A::sub(lap1, lap0), a1, a0);              // fly(i, j)
+                const C lapR = __shfl_down_sync(0xffffffffu, lap0, 1);            // lap(i+1, j)
+                const C flx0 = A::limit(A::sub(lapR, lap0), right0, a0);          // flx(i, j)
+                const C flxL = __shfl_up_sync(0xffffffffu, flx0, 1);              // flx(i-1, j)
+                if (writer) {
+                    const C d = A::sub(A::add(A::sub(flx0, flxL), fly0), fly_m1);
+                    st<S, C>(out + (obase + (IDX)j * sj), A::sub(a0, A::mul(cf[u], d)));
+                }
+                a0 = a1;
+                a1 = a2n;
+                lap0 = lap1;
+                fly_m1 = fly0;
+                right0 = right1;
+            }
+        }
+    }
+}
+
+template <class S, class C, class IDX>
+int launch_jscan_idx(dim3 grid, dim3 block, cudaStream_t stream, const void* inp, const void* coeff, void* out,
+                     int64_t ni, int64_t nj, int64_t nk, int64_t si, int64_t sj, int64_t sk, int ty, int kper,
+                     int unroll) {
+#define SB_JSCAN(UV)                                                                                        \
+    hdiff_jscan_kernel<S, C, UV, IDX><<<grid, block, 0, stream>>>((const S*)inp, (const S*)coeff, (S*)out,    \
+                                                                  (int)ni, (int)nj, (int)nk, (IDX)si,       \
+                                                                  (IDX)sj, (IDX)sk, ty, kper)
+    switch (unroll) {
+        case 1: SB_JSCAN(1); break;
+        case 2: SB_JSCAN(2); break;
+        case 4: SB_JSCAN(4); break;
+        case 8: SB_JSCAN(8); break;
+        default: return fail(SB_ERR_INVALID, "jscan unroll must be 1, 2, 4 or 8 (got %d)", unroll);
+    }
+#undef SB_JSCAN
+    return SB_OK;
+}
+
+template <class S, class C>
+int launch_jscan(const void* inp, const void* coeff, void* out, int64_t ni, int64_t nj, int64_t nk,
+                 int64_t si, int64_t sj, int64_t sk, int nw, int ty, int kper, int unroll,
+                 cudaStream_t stream, const DeviceProps* p) {
+    SB_CHECK(nw >= 1 && nw <= 8, SB_ERR_INVALID, "jscan: 1..8 warps per block");
+    const int64_t gx = ceil_div(ni, (int64_t)kJscanOut * nw), gy = ceil_div(nj, ty), gz = ceil_div(nk, kper);
+    SB_CHECK(gy <= p->max_grid_y && gz <= p->max_grid_z, SB_ERR_INVALID, "hdiff grid too large");
+    const dim3 grid((unsigned)gx, (unsigned)gy, (unsigned)gz), block(32, nw);
+    // 32-bit offsets when every address of the halo'd fields fits (the common case)
+    const int64_t lo = -2 * (std::abs(si) + std::abs(sj));
+    const int64_t hi = (ni + 2 + 32) * std::abs(si) + (nj + 2) * std::abs(sj) + nk * std::abs(sk);
+    if (lo > -(1LL << 31) && hi < (1LL << 31))
+        return launch_jscan_idx<S, C, int>(grid, block, stream, inp, coeff, out, ni, nj, nk, si, sj, sk, ty, kper, unroll);
+    return launch_jscan_idx<S, C, int64_t>(grid, block, stream, inp, coeff, out, ni, nj, nk, si, sj, sk, ty, kper, unroll);
+}
+
 template <class S, class C, int TX, int NTY>
 int launch_tile(const void* inp, const void* coeff, void* out, int64_t ni, int64_t nj, int64_t nk,
                 int64_t si, int64_t sj, int64_t sk, int ty, int kper, cudaStream_t stream,
@@ -130,9 +250,19 @@ int launch_typed(const void* inp, const void* coeff, void* out, int64_t ni, int6
     const DeviceProps* p;
     int rc = device_props(&p);
     if (rc) return rc;
-    const int variant = tune ? tune->variant : SB_VARIANT_AUTO;
-    SB_CHECK(variant == SB_VARIANT_AUTO || variant == SB_HDIFF_TILE, SB_ERR_UNSUPPORTED,
+    int variant = tune ? tune->variant : SB_VARIANT_AUTO;
+    if (variant == SB_VARIANT_AUTO) variant = SB_HDIFF_JSCAN;
+    SB_CHECK(variant == SB_HDIFF_TILE || variant == SB_HDIFF_JSCAN, SB_ERR_UNSUPPORTED,
              "hdiff variant %d is not available", variant);
+    if (variant == SB_HDIFF_JSCAN) {
+        const int nw = (tune && tune->block_y > 0) ? tune->block_y : 4;
+        const int ty = (tune && tune->tile_y > 0) ? tune->tile_y : 32;
+        const int kper = (tune && tune->k_per_cta > 0) ? tune->k_per_cta : 1;
+        const int unroll = (tune && tune->unroll > 0) ? tune->unroll : 4;
+        SB_CHECK(!tune || tune->block_x == 0 || tune->block_x == 32, SB_ERR_INVALID,
+                 "hdiff jscan uses one warp (block_x = 32) per strip");
+        return launch_jscan<S, C>(inp, coeff, out, ni, nj, nk, si, sj, sk, nw, ty, kper, unroll, stream, p);
+    }
     const int bx = (tune && tune->block_x > 0) ? tune->block_x : 64;
     const int by = (tune && tune->block_y > 0) ? tune->block_y : 4;
     int ty = (tune && tune->tile_y > 0) ? tune->tile_y : 16;

@@ -33,7 +33,7 @@
 namespace sb {
 namespace {
 
-template <class S, class C, bool GLOBAL>
+template <class S, class C, bool GLOBAL, int D>
 __global__ void __launch_bounds__(256)
     vadv_kernel(const S* __restrict__ stage, const S* __restrict__ pos, const S* __restrict__ tens,
                 const S* tensstage, const S* __restrict__ wcon, S* out, C* __restrict__ gccol,
@@ -62,8 +62,6 @@ __global__ void __launch_bounds__(256)
             sd[(size_t)k * nthr + t] = dv;
         }
     };
-    auto get_c = [&](int k) -> C { return GLOBAL ? gccol[col + (int64_t)k * sk] : sc[(size_t)k * nthr + t]; };
-    auto get_d = [&](int k) -> C { return GLOBAL ? gdcol[col + (int64_t)k * sk] : sd[(size_t)k * nthr + t]; };
 
     // ---- forward sweep, k = 0
     int64_t o = col;
@@ -79,25 +77,48 @@ __global__ void __launch_bounds__(256)
     C dp = A::div(dv, bcol);
     put(0, cp, dp);
 
-    // ---- forward sweep, 0 < k < nk-1
-#pragma unroll 2
-    for (int k = 1; k < nk - 1; ++k) {
-        o = col + (int64_t)k * sk;
-        const C as_ = A::template scale2<-1>(-gcv);  // gav * bet_m == acol, gav = -gcv(k-1)
-        gcv = A::template scale2<-2>(A::add(ld<C, S>(wcon + o + sk + wsh), ld<C, S>(wcon + o + sk)));
-        cs = A::template scale2<-1>(gcv);
-        const C snext = ld<C, S>(stage + o + sk);
-        const C ddown = A::neg_diff(dup, scur, sprev);  // stage[k-1] - stage[k]
-        dup = A::sub(snext, scur);                     // stage[k+1] - stage[k]
-        bcol = A::sub(A::sub(dtr, as_), cs);
-        corr = A::sub(A::mul(-as_, ddown), A::mul(cs, dup));
-        dv = A::add(A::add(A::add(A::mul(dtr, ld<C, S>(pos + o)), ld<C, S>(tens + o)), ldc<C, S>(tensstage + o)), corr);
-        const C divided = A::rcp(A::sub(bcol, A::mul(cp, as_)));
-        cp = A::mul(cs, divided);
-        dp = A::mul(A::sub(dv, A::mul(dp, as_)), divided);
-        put(k, cp, dp);
-        sprev = scur;
-        scur = snext;
+    // ---- forward sweep, 0 < k < nk-1, with a D-deep register prefetch ring:
+    // slot u holds the inputs of level k (wcon at k+1 in both columns,
+    // stage at k+1, pos/tens/tensstage at k); after level k is consumed the
+    // slot is refilled with level k+D, so D levels of loads stay in flight
+    // while the serial recurrence runs.
+    C rw1[D], rw0[D], rst[D], rpo[D], rte[D], rts[D];
+    auto fetch = [&](C& w1, C& w0, C& s1, C& p0, C& t0, C& ts0, int k) {
+        if (k < nk - 1) {
+            const int64_t q = col + (int64_t)k * sk;
+            w1 = ld<C, S>(wcon + q + sk + wsh);
+            w0 = ld<C, S>(wcon + q + sk);
+            s1 = ld<C, S>(stage + q + sk);
+            p0 = ld<C, S>(pos + q);
+            t0 = ld<C, S>(tens + q);
+            ts0 = ldc<C, S>(tensstage + q);
+        }
+    };
+#pragma unroll
+    for (int u = 0; u < D; ++u) fetch(rw1[u], rw0[u], rst[u], rpo[u], rte[u], rts[u], 1 + u);
+
+    for (int kb = 1; kb < nk - 1; kb += D) {
+#pragma unroll
+        for (int u = 0; u < D; ++u) {
+            const int k = kb + u;
+            if (k >= nk - 1) break;  // uniform: every thread has the same nk
+            const C as_ = A::template scale2<-1>(-gcv);  // gav * bet_m == acol, gav = -gcv(k-1)
+            gcv = A::template scale2<-2>(A::add(rw1[u], rw0[u]));
+            cs = A::template scale2<-1>(gcv);
+            const C snext = rst[u];
+            const C ddown = A::neg_diff(dup, scur, sprev);  // stage[k-1] - stage[k]
+            dup = A::sub(snext, scur);                     // stage[k+1] - stage[k]
+            bcol = A::sub(A::sub(dtr, as_), cs);
+            corr = A::sub(A::mul(-as_, ddown), A::mul(cs, dup));
+            dv = A::add(A::add(A::add(A::mul(dtr, rpo[u]), rte[u]), rts[u]), corr);
+            fetch(rw1[u], rw0[u], rst[u], rpo[u], rte[u], rts[u], k + D);
+            const C divided = A::rcp(A::sub(bcol, A::mul(cp, as_)));
+            cp = A::mul(cs, divided);
+            dp = A::mul(A::sub(dv, A::mul(dp, as_)), divided);
+            put(k, cp, dp);
+            sprev = scur;
+            scur = snext;
+        }
     }
 
     // ---- forward sweep, k = nk-1
@@ -112,15 +133,239 @@ __global__ void __launch_bounds__(256)
         dp = A::div(A::sub(dv, A::mul(dp, as_)), A::sub(bcol, A::mul(cp, as_)));
     }
 
-    // ---- backward sweep
+    // ---- backward sweep; pos (and, for GLOBAL, ccol/dcol) prefetched D levels ahead
     C data = dp;
     o = col + (int64_t)(nk - 1) * sk;
     st<S, C>(out + o, A::mul(dtr, A::sub(data, ld<C, S>(pos + o))));
-#pragma unroll 2
-    for (int k = nk - 2; k >= 0; --k) {
-        o = col + (int64_t)k * sk;
-        data = A::sub(get_d(k), A::mul(get_c(k), data));
+    C bpo[D], bcc[D], bdd[D];
+    auto fetch_back = [&](C& p0, C& c0, C& d0, int k) {
+        if (k >= 0) {
+            const int64_t q = col + (int64_t)k * sk;
+            p0 = ld<C, S>(pos + q);
+            if (GLOBAL) {
+                c0 = gccol[q];
+                d0 = gdcol[q];
+            }
+        }
+    };
+#pragma unroll
+    for (int u = 0; u < D; ++u) fetch_back(bpo[u], bcc[u], bdd[u], nk - 2 - u);
+    for (int kb = nk - 2; kb >= 0; kb -= D) {
+#pragma unroll
+        for (int u = 0; u < D; ++u) {
+            const int k = kb - u;
+            if (k < 0) break;
+            const C cv = GLOBAL ? bcc[u] : sc[(size_t)k * nthr + t];
+            const C dvv = GLOBAL ? bdd[u] : sd[(size_t)k * nthr + t];
+            const C p0 = bpo[u];
+            fetch_back(bpo[u], bcc[u], bdd[u], k - D);
+            data = A::sub(dvv, A::mul(cv, data));
+            st<S, C>(out + col + (int64_t)k * sk, A::mul(dtr, A::sub(data, p0)));
+        }
+    }
+}
+
+// SMEM variant with asynchronous staging (storage of 4 or 8 bytes): the six
+// per-level inputs of the forward sweep (wcon at k+1 in both columns, stage
+// at k+1, pos/tens/tensstage at k) are copied global -> shared with cp.async
+// into a ring of R = D+1 slots, D levels ahead of the recurrence; the
+// backward sweep streams pos the same way.  Slots are compile-time indices
+// (the level loops are unrolled by R) and BT threads per block is a template
+// parameter, so every shared-memory address is a register + immediate.
+// Layout of dynamic shared memory: ccol[nk][BT], dcol[nk][BT] (compute type),
+// then ring[R][6][BT] (storage type), 16-byte aligned.
+template <class S, class C, int BT, int D>
+__global__ void __launch_bounds__(BT)
+    vadv_async_kernel(const S* __restrict__ stage, const S* __restrict__ pos, const S* __restrict__ tens,
+                      const S* tensstage, const S* __restrict__ wcon, S* out, int ni, int nj, int nk,
+                      int si, int sj, int sk, int wsh, int ring_offset) {
+    using A = Ar<C>;
+    constexpr int R = D + 1;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int t = threadIdx.x;
+    C* sc = reinterpret_cast<C*>(smem_raw) + t;
+    C* sd = sc + nk * BT;
+    S* ring = reinterpret_cast<S*>(smem_raw + ring_offset) + t;
+
+    const int i = blockIdx.x * BT + t;
+    const int j = blockIdx.y;
+    if (i >= ni) return;  // no block-wide barrier below
+    const C dtr = (C)(3.0 / 20.0);
+    const int col = i * si + j * sj;
+
+    auto issue = [&](int slot, int k) {
+        if (k < nk - 1) {
+            const int q = col + k * sk;
+            S* d = ring + slot * 6 * BT;
+            cp_async<sizeof(S)>(d, wcon + q + sk + wsh);
+            cp_async<sizeof(S)>(d + BT, wcon + q + sk);
+            cp_async<sizeof(S)>(d + 2 * BT, stage + q + sk);
+            cp_async<sizeof(S)>(d + 3 * BT, pos + q);
+            cp_async<sizeof(S)>(d + 4 * BT, tens + q);
+            cp_async<sizeof(S)>(d + 5 * BT, tensstage + q);
+        }
+        cp_async_commit();
+    };
+    // level L is staged in slot (L-1) % R
+#pragma unroll
+    for (int u = 0; u < D; ++u) issue(u, 1 + u);
+
+    // ---- forward sweep, k = 0 (direct loads)
+    C gcv = A::template scale2<-2>(A::add(ld<C, S>(wcon + col + sk + wsh), ld<C, S>(wcon + col + sk)));
+    C cs = A::template scale2<-1>(gcv);
+    C sprev = ld<C, S>(stage + col);
+    C scur = ld<C, S>(stage + col + sk);
+    C dup = A::sub(scur, sprev);
+    C bcol = A::sub(dtr, cs);
+    C corr = A::mul(-cs, dup);
+    C dv = A::add(A::add(A::add(A::mul(dtr, ld<C, S>(pos + col)), ld<C, S>(tens + col)), ldc<C, S>(tensstage + col)), corr);
+    C cp = A::div(cs, bcol);
+    C dp = A::div(dv, bcol);
+    sc[0] = cp;
+    sd[0] = dp;
+
+    // ---- forward sweep, 0 < k < nk-1
+    for (int kb = 1; kb < nk - 1; kb += R) {
+#pragma unroll
+        for (int u = 0; u < R; ++u) {
+            const int k = kb + u;
+            if (k >= nk - 1) break;  // uniform
+            cp_async_wait<D - 1>();
+            const S* sl = ring + u * 6 * BT;
+            const C w1 = cvt<C, S>(sl[0]), w0 = cvt<C, S>(sl[BT]), snext = cvt<C, S>(sl[2 * BT]);
+            const C p0 = cvt<C, S>(sl[3 * BT]), t0 = cvt<C, S>(sl[4 * BT]), ts0 = cvt<C, S>(sl[5 * BT]);
+            issue((u + D) % R, k + D);  // the slot of level k-1, already consumed
+            const C as_ = A::template scale2<-1>(-gcv);
+            gcv = A::template scale2<-2>(A::add(w1, w0));
+            cs = A::template scale2<-1>(gcv);
+            const C ddown = A::neg_diff(dup, scur, sprev);
+            dup = A::sub(snext, scur);
+            bcol = A::sub(A::sub(dtr, as_), cs);
+            corr = A::sub(A::mul(-as_, ddown), A::mul(cs, dup));
+            dv = A::add(A::add(A::add(A::mul(dtr, p0), t0), ts0), corr);
+            const C divided = A::rcp(A::sub(bcol, A::mul(cp, as_)));
+            cp = A::mul(cs, divided);
+            dp = A::mul(A::sub(dv, A::mul(dp, as_)), divided);
+            sc[k * BT] = cp;
+            sd[k * BT] = dp;
+            sprev = scur;
+            scur = snext;
+        }
+    }
+    cp_async_wait<0>();
+
+    // ---- forward sweep, k = nk-1
+    {
+        const int o = col + (nk - 1) * sk;
+        const C as_ = A::template scale2<-1>(-gcv);
+        bcol = A::sub(dtr, as_);
+        const C ddown = A::neg_diff(dup, scur, sprev);
+        corr = A::mul(-as_, ddown);
+        dv = A::add(A::add(A::add(A::mul(dtr, ld<C, S>(pos + o)), ld<C, S>(tens + o)), ldc<C, S>(tensstage + o)), corr);
+        dp = A::div(A::sub(dv, A::mul(dp, as_)), A::sub(bcol, A::mul(cp, as_)));
+    }
+
+    // ---- backward sweep; pos of level L staged in slot (nk-2-L) % R, field 3
+    auto issue_b = [&](int slot, int k) {
+        if (k >= 0) cp_async<sizeof(S)>(ring + slot * 6 * BT + 3 * BT, pos + col + k * sk);
+        cp_async_commit();
+    };
+#pragma unroll
+    for (int u = 0; u < D; ++u) issue_b(u, nk - 2 - u);
+    C data = dp;
+    {
+        const int o = col + (nk - 1) * sk;
         st<S, C>(out + o, A::mul(dtr, A::sub(data, ld<C, S>(pos + o))));
+    }
+    for (int kb = nk - 2; kb >= 0; kb -= R) {
+#pragma unroll
+        for (int u = 0; u < R; ++u) {
+            const int k = kb - u;
+            if (k < 0) break;
+            cp_async_wait<D - 1>();
+            const C p0 = cvt<C, S>(ring[u * 6 * BT + 3 * BT]);
+            issue_b((u + D) % R, k - D);
+            data = A::sub(sd[k * BT], A::mul(sc[k * BT], data));
+            st<S, C>(out + col + k * sk, A::mul(dtr, A::sub(data, p0)));
+        }
+    }
+    cp_async_wait<0>();
+}
+
+template <class S, class C, bool GLOBAL, int D>
+int launch_one(dim3 grid, dim3 block, size_t smem, cudaStream_t stream, const void* stage, const void* pos,
+               const void* tens, const void* tensstage, const void* wcon, void* out, void* ccol, void* dcol,
+               int64_t ni, int64_t nj, int64_t nk, int64_t si, int64_t sj, int64_t sk, int64_t wsh) {
+    auto kernel = vadv_kernel<S, C, GLOBAL, D>;
+    if (smem > 48 * 1024) SB_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    kernel<<<grid, block, smem, stream>>>((const S*)stage, (const S*)pos, (const S*)tens, (const S*)tensstage,
+                                          (const S*)wcon, (S*)out, (C*)ccol, (C*)dcol, (int)ni, (int)nj, (int)nk,
+                                          si, sj, sk, wsh);
+    return SB_OK;
+}
+
+template <class S, class C, bool GLOBAL>
+int launch_depth(int depth, dim3 grid, dim3 block, size_t smem, cudaStream_t stream, const void* stage,
+                 const void* pos, const void* tens, const void* tensstage, const void* wcon, void* out,
+                 void* ccol, void* dcol, int64_t ni, int64_t nj, int64_t nk, int64_t si, int64_t sj,
+                 int64_t sk, int64_t wsh) {
+    switch (depth) {
+        case 1: return launch_one<S, C, GLOBAL, 1>(grid, block, smem, stream, stage, pos, tens, tensstage, wcon, out, ccol, dcol, ni, nj, nk, si, sj, sk, wsh);
+        case 2: return launch_one<S, C, GLOBAL, 2>(grid, block, smem, stream, stage, pos, tens, tensstage, wcon, out, ccol, dcol, ni, nj, nk, si, sj, sk, wsh);
+        case 4: return launch_one<S, C, GLOBAL, 4>(grid, block, smem, stream, stage, pos, tens, tensstage, wcon, out, ccol, dcol, ni, nj, nk, si, sj, sk, wsh);
+        case 8: return launch_one<S, C, GLOBAL, 8>(grid, block, smem, stream, stage, pos, tens, tensstage, wcon, out, ccol, dcol, ni, nj, nk, si, sj, sk, wsh);
+    }
+    return fail(SB_ERR_INVALID, "vadv prefetch depth (unroll) must be 1, 2, 4 or 8 (got %d)", depth);
+}
+
+// Shared memory of the asynchronous SMEM kernel for BT threads and depth D.
+template <class S, class C>
+size_t async_smem(int64_t nk, int bt, int depth, int* ring_offset) {
+    const size_t scratch = ((2 * sizeof(C) * (size_t)nk * (size_t)bt) + 15) / 16 * 16;
+    if (ring_offset) *ring_offset = (int)scratch;
+    return scratch + (size_t)(depth + 1) * 6 * (size_t)bt * sizeof(S);
+}
+
+template <class S, class C, int BT, int D>
+int launch_async_one(dim3 grid, size_t smem, int ring_offset, cudaStream_t stream, const void* stage,
+                     const void* pos, const void* tens, const void* tensstage, const void* wcon, void* out,
+                     int64_t ni, int64_t nj, int64_t nk, int64_t si, int64_t sj, int64_t sk, int64_t wsh) {
+    auto kernel = vadv_async_kernel<S, C, BT, D>;
+    if (smem > 48 * 1024) SB_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    kernel<<<grid, BT, smem, stream>>>((const S*)stage, (const S*)pos, (const S*)tens, (const S*)tensstage,
+                                       (const S*)wcon, (S*)out, (int)ni, (int)nj, (int)nk, (int)si, (int)sj,
+                                       (int)sk, (int)wsh, ring_offset);
+    return SB_OK;
+}
+
+// Asynchronous SMEM kernel if this launch qualifies (4/8-byte storage, one
+// row of 32 or 64 columns per block, all offsets within 32 bits); returns
+// SB_ERR_UNSUPPORTED (without error text) when it does not.
+template <class S, class C>
+int launch_async(int bx, int by, int depth, const DeviceProps* p, cudaStream_t stream, const void* stage,
+                 const void* pos, const void* tens, const void* tensstage, const void* wcon, void* out,
+                 int64_t ni, int64_t nj, int64_t nk, int64_t si, int64_t sj, int64_t sk, int64_t wsh) {
+    if constexpr (sizeof(S) != 4 && sizeof(S) != 8) {
+        return SB_ERR_UNSUPPORTED;
+    } else {
+    if (by != 1 || (bx != 32 && bx != 64) || (depth != 4 && depth != 8)) return SB_ERR_UNSUPPORTED;
+    if (si <= 0 || sj <= 0 || sk <= 0 || nj > p->max_grid_y) return SB_ERR_UNSUPPORTED;
+    const int64_t span = (ni + 1) * si + nj * sj + (nk + 1) * sk;
+    if (span >= (1LL << 31)) return SB_ERR_UNSUPPORTED;
+    int ring_offset = 0;
+    const size_t smem = async_smem<S, C>(nk, bx, depth, &ring_offset);
+    if ((int64_t)smem > p->smem_optin) return SB_ERR_UNSUPPORTED;
+    const dim3 grid((unsigned)ceil_div(ni, bx), (unsigned)nj);
+#define SB_VADV_ASYNC(BTV, DV)                                                                              \
+    if (bx == BTV && depth == DV)                                                                           \
+        return launch_async_one<S, C, BTV, DV>(grid, smem, ring_offset, stream, stage, pos, tens, tensstage, \
+                                               wcon, out, ni, nj, nk, si, sj, sk, wsh);
+    SB_VADV_ASYNC(32, 4)
+    SB_VADV_ASYNC(32, 8)
+    SB_VADV_ASYNC(64, 4)
+    SB_VADV_ASYNC(64, 8)
+#undef SB_VADV_ASYNC
+    return SB_ERR_UNSUPPORTED;
     }
 }
 
@@ -143,25 +388,21 @@ int launch_typed(const void* stage, const void* pos, const void* tens, const voi
     const int64_t gx = ceil_div(ni, bx), gy = ceil_div(nj, by);
     SB_CHECK(gy <= p->max_grid_y, SB_ERR_INVALID, "vadv grid too large");
     const dim3 grid((unsigned)gx, (unsigned)gy), block(bx, by);
+    const int depth = (tune && tune->unroll > 0) ? tune->unroll : (sizeof(C) == 8 ? 4 : 8);
     if (variant == SB_VADV_SMEM) {
+        const int arc = launch_async<S, C>(bx, by, depth, p, stream, stage, pos, tens, tensstage, wcon, out, ni, nj,
+                                           nk, si, sj, sk, wsh);
+        if (arc != SB_ERR_UNSUPPORTED) return arc;
         SB_CHECK((int64_t)smem <= p->smem_optin, SB_ERR_INVALID,
                  "vadv: %lld levels x %d columns need %zu bytes of shared memory (limit %d); "
                  "use fewer threads per block or the GLOBAL variant with ccol/dcol scratch",
                  (long long)nk, bx * by, smem, p->smem_optin);
-        auto kernel = vadv_kernel<S, C, false>;
-        if (smem > 48 * 1024) SB_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        kernel<<<grid, block, smem, stream>>>((const S*)stage, (const S*)pos, (const S*)tens, (const S*)tensstage,
-                                              (const S*)wcon, (S*)out, nullptr, nullptr, (int)ni, (int)nj, (int)nk,
-                                              si, sj, sk, wsh);
-    } else {
-        SB_CHECK(can_global, SB_ERR_INVALID,
-                 "vadv GLOBAL variant needs ccol/dcol scratch fields of the compute type");
-        vadv_kernel<S, C, true><<<grid, block, 0, stream>>>((const S*)stage, (const S*)pos, (const S*)tens,
-                                                          (const S*)tensstage, (const S*)wcon, (S*)out,
-                                                          (C*)ccol, (C*)dcol,
-                                                          (int)ni, (int)nj, (int)nk, si, sj, sk, wsh);
+        return launch_depth<S, C, false>(depth, grid, block, smem, stream, stage, pos, tens, tensstage, wcon, out,
+                                         nullptr, nullptr, ni, nj, nk, si, sj, sk, wsh);
     }
-    return SB_OK;
+    SB_CHECK(can_global, SB_ERR_INVALID, "vadv GLOBAL variant needs ccol/dcol scratch fields of the compute type");
+    return launch_depth<S, C, true>(depth, grid, block, 0, stream, stage, pos, tens, tensstage, wcon, out,
+                                    ccol, dcol, ni, nj, nk, si, sj, sk, wsh);
 }
 
 }  // namespace

@@ -62,13 +62,15 @@ def _import_reference():
 
 
 def _capture(base):
-    """Wrap base.validation.check_equality to record (name, expected)."""
+    """Replace base.validation.check_equality by a recorder of (name, expected).
+
+    The recorder never raises, so every field the reference would compare is
+    captured (a raising check would stop at the first output)."""
     records = {}
     original = base.validation.check_equality
 
     def check_equality(name, result, expected):
         records[name] = np.array(expected, copy=True)
-        original(name, result, expected)
 
     base.validation.check_equality = check_equality
     return records, original

@@ -66,19 +66,28 @@ def compute_view(host, storage, compute):
 
 
 def bits_equal(a, b):
+    """Bitwise equality, except that any NaN matches any NaN: IEEE 754 leaves
+    the sign and payload of a NaN result unspecified, and CPUs and GPUs
+    propagate them differently."""
     a = np.ascontiguousarray(a)
     b = np.ascontiguousarray(b)
     if a.shape != b.shape or a.dtype.itemsize != b.dtype.itemsize:
         return False
     view = {8: np.uint64, 4: np.uint32, 2: np.uint16}[a.dtype.itemsize]
-    return np.array_equal(a.view(view), b.view(view))
+    same = a.view(view) == b.view(view)
+    if a.dtype.kind == "f":
+        same |= np.isnan(a) & np.isnan(b)
+    return bool(np.all(same))
 
 
 def mismatch_report(got, want, limit=5):
     g = np.ascontiguousarray(got)
     w = np.ascontiguousarray(want)
     view = {8: np.uint64, 4: np.uint32, 2: np.uint16}[g.dtype.itemsize]
-    bad = np.argwhere(g.view(view) != w.view(view))
+    differ = g.view(view) != w.view(view)
+    if g.dtype.kind == "f":
+        differ &= ~(np.isnan(g) & np.isnan(w))
+    bad = np.argwhere(differ)
     lines = [f"{len(bad)} of {g.size} differ"]
     for idx in bad[:limit]:
         idx = tuple(idx)
