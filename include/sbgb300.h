@@ -159,6 +159,31 @@ int sb_vadv(int storage, int compute, const void* stage, const void* pos, const 
             int64_t nj, int64_t nk, int64_t si, int64_t sj, int64_t sk, int wshift_i, int wshift_j,
             const sb_tune* tune, void* stream, double* time_s);
 
+/* ---- vertical advection without device allocation -------------------------
+ * No counterpart in the reference.  For callers that cannot call cudaMalloc:
+ * code embedded in a host framework that owns every device allocation (fixed
+ * memory pools), or paths that must not trigger the device-wide
+ * synchronisation that cudaMalloc/cudaFree can cause.  Computes exactly what
+ * sb_vadv computes (bit-identical results) with the factors of the
+ * elimination kept in global memory, but that scratch is one fixed array of
+ * SB_VADV_NOALLOC_SCRATCH_BYTES compiled into the library (held by every
+ * device that loads the library until the process exits) instead of
+ * caller-provided ccol/dcol fields; the call allocates nothing.  The caller
+ * still passes all input and output fields.  Columns are processed in a
+ * grid-stride loop over as many thread slots as the array holds (2 * nk
+ * factors per slot); a call whose nk leaves room for fewer than one block of
+ * 64 slots fails with SB_ERR_BUDGET before launching.  The first call on a
+ * device looks up the array's device address (cudaGetSymbolAddress) and
+ * caches it: make that first call before any stream capture on the device.
+ * Every call shares the array, so calls that overlap on the GPU race and
+ * must be serialised by the caller; every factor is written before it is
+ * read, so no state carries over between calls.                             */
+#define SB_VADV_NOALLOC_SCRATCH_BYTES (32u * 1024u * 1024u)
+int sb_vadv_noalloc(int storage, int compute, const void* stage, const void* pos, const void* tens,
+                    const void* tensstage, const void* wcon, void* out, int64_t ni, int64_t nj, int64_t nk,
+                    int64_t si, int64_t sj, int64_t sk, int wshift_i, int wshift_j, void* stream,
+                    double* time_s);
+
 /* ---- measurement helpers ---------------------------------------------------- */
 /* Throughput of dependent-free fp64 / fp32 arithmetic on this device, in
  * operations per second (kind 0: f64 add, 1: f64 fma, 2: f32 fma). */

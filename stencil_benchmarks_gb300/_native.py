@@ -114,6 +114,7 @@ SIGNATURES = {
     "sb_average": [_int, _int, _vp, _vp] + [_i64] * 6 + [_int, _int, _tp, _vp, _dp],
     "sb_hdiff": [_int, _int, _vp, _vp, _vp] + [_i64] * 6 + [_tp, _vp, _dp],
     "sb_vadv": [_int, _int] + [_vp] * 8 + [_i64] * 6 + [_int, _int, _tp, _vp, _dp],
+    "sb_vadv_noalloc": [_int, _int] + [_vp] * 6 + [_i64] * 6 + [_int, _int, _vp, _dp],
     "sb_probe_arith_rate": [_int, _dp],
 }
 _RESTYPES = {"sb_last_error": ctypes.c_char_p}
