@@ -1,0 +1,92 @@
+"""Vertical advection on GB300: ``sbench stencils gb300 vertical-advection <impl>``.
+
+Counterpart of stencil_benchmarks/benchmarks_collection/stencils/cuda_hip/
+vertical_advection.py:39-73.  The fields and the in-place update of
+``utensstage`` (and, with ``all_components``, ``vtensstage``/``wtensstage``)
+are the reference's; each component is one ``sb_vadv`` launch, with wcon read
+at the column shifted by (1, 0), (0, 1) and (0, 0) for u, v and w
+(stencils/base.py:475-483).
+
+* ``SharedMem``     -- factors in shared memory, inputs staged with cp.async;
+* ``GlobalScratch`` -- factors in the ``ccol``/``dcol`` fields (fastest fp64 form);
+* ``NoAlloc``       -- factors in the library's static scratch array
+  (``sb_vadv_noalloc``), for callers that cannot allocate device memory.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import warnings
+
+from .... import _native, kernels
+from ....benchmark import Parameter, ParameterError
+from ....device import _stream_arg
+from .. import base
+from .mixin import StencilMixin
+
+_SHIFTS = {"u": (1, 0), "v": (0, 1), "w": (0, 0)}
+
+
+class VerticalAdvectionMixin(StencilMixin):
+    block_size = Parameter("threads per block along i and j", (32, 1))
+    unroll_factor = Parameter("levels of inputs kept in flight (1, 2, 4 or 8)", 4, choices=[1, 2, 4, 8])
+
+    def setup(self):
+        super().setup()
+        if self.verify and self.dry_runs:
+            warnings.warn(
+                "using --dry-runs together with verification might lead to false negatives for "
+                "stencils with read-write fields"
+            )
+
+    def components(self, fields):
+        named = dict(zip(self.args, fields))
+        comps = ["u", "v", "w"] if self.all_components else ["u"]
+        for c in comps:
+            yield c, [named[f"{c}{n}"] for n in ("stage", "pos", "tens", "tensstage")], named
+
+    def launch_component(self, f, named, shift, timed):
+        raise NotImplementedError
+
+    def launch(self, fields, timed):
+        total = 0.0
+        for c, f, named in self.components(fields):
+            t = self.launch_component(f, named, _SHIFTS[c], timed)
+            total += t or 0.0
+        return total if timed else None
+
+
+class SharedMem(VerticalAdvectionMixin, base.VerticalAdvectionStencil):
+    def launch_component(self, f, named, shift, timed):
+        tune = _native.tune(variant=_native.VADV_SMEM, block_x=self.block_size[0], block_y=self.block_size[1],
+                            unroll=self.unroll_factor)
+        return kernels.vadv(*f, named["wcon"], shift, compute=self.compute, tune=tune, timed=timed)
+
+
+class GlobalScratch(VerticalAdvectionMixin, base.VerticalAdvectionStencil):
+    block_size = Parameter("threads per block along i and j", (64, 1))
+    unroll_factor = Parameter("levels of inputs kept in flight (1, 2, 4 or 8)", 2, choices=[1, 2, 4, 8])
+
+    def setup(self):
+        super().setup()
+        if self.dtype_size != {"float64": 8, "float32": 4}[self.compute]:
+            raise ParameterError("GlobalScratch keeps the factors in ccol/dcol: storage and compute types must match")
+
+    def launch_component(self, f, named, shift, timed):
+        tune = _native.tune(variant=_native.VADV_GLOBAL, block_x=self.block_size[0], block_y=self.block_size[1],
+                            unroll=self.unroll_factor)
+        return kernels.vadv(*f, named["wcon"], shift, ccol=named["ccol"], dcol=named["dcol"], compute=self.compute,
+                            tune=tune, timed=timed)
+
+
+class NoAlloc(VerticalAdvectionMixin, base.VerticalAdvectionStencil):
+    def launch_component(self, f, named, shift, timed):
+        stage, pos, tens, tensstage = f
+        ni, nj, nk = self.domain
+        t = ctypes.c_double(0.0)
+        _native.call(
+            "sb_vadv_noalloc", _native.storage_code(self.dtype), _native.storage_code(self.compute),
+            *(ctypes.c_void_p(x.interior_ptr) for x in (stage, pos, tens, tensstage, named["wcon"], tensstage)),
+            ni, nj, nk, *stage.strides, shift[0], shift[1], _stream_arg(None), ctypes.byref(t) if timed else None,
+        )
+        return t.value if timed else None

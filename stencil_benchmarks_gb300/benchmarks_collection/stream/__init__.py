@@ -1,0 +1,3 @@
+from . import gb300
+
+__all__ = ["gb300"]
