@@ -251,7 +251,11 @@ int launch_typed(const void* inp, const void* coeff, void* out, int64_t ni, int6
     int rc = device_props(&p);
     if (rc) return rc;
     int variant = tune ? tune->variant : SB_VARIANT_AUTO;
-    if (variant == SB_VARIANT_AUTO) variant = SB_HDIFF_JSCAN;
+    // fp64 compute is bound by the fp64 pipe: TILE computes every lap/flx/fly
+    // once per tile (fewest fp64 operations); fp32 compute is bound by memory
+    // and instruction issue: JSCAN (shuffles, no block barriers) is faster.
+    const bool auto_tile = variant == SB_VARIANT_AUTO && sizeof(C) == 8;
+    if (variant == SB_VARIANT_AUTO) variant = auto_tile ? SB_HDIFF_TILE : SB_HDIFF_JSCAN;
     SB_CHECK(variant == SB_HDIFF_TILE || variant == SB_HDIFF_JSCAN, SB_ERR_UNSUPPORTED,
              "hdiff variant %d is not available", variant);
     if (variant == SB_HDIFF_JSCAN) {
@@ -263,7 +267,7 @@ int launch_typed(const void* inp, const void* coeff, void* out, int64_t ni, int6
                  "hdiff jscan uses one warp (block_x = 32) per strip");
         return launch_jscan<S, C>(inp, coeff, out, ni, nj, nk, si, sj, sk, nw, ty, kper, unroll, stream, p);
     }
-    const int bx = (tune && tune->block_x > 0) ? tune->block_x : 64;
+    const int bx = (tune && tune->block_x > 0) ? tune->block_x : (auto_tile ? 128 : 64);
     const int by = (tune && tune->block_y > 0) ? tune->block_y : 4;
     int ty = (tune && tune->tile_y > 0) ? tune->tile_y : 16;
     int kper = (tune && tune->k_per_cta > 0) ? tune->k_per_cta : 4;

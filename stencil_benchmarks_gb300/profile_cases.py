@@ -1,0 +1,111 @@
+"""Launch named kernel cases a fixed number of times (for ncu captures).
+
+    python -m stencil_benchmarks_gb300.profile_cases [--warmup W] [--launches L] CASE...
+
+CASE is ``<stencil>-<form>`` with stencil in hdiff, vadv, triad, copy, lap and
+form in f64, f32, bf16 (bf16 = bfloat16 storage, f32 compute); ``all`` runs
+every hdiff/vadv form plus triad-f64.  Stencil cases use the 512 x 512 x 80
+interior with the reference's halos (2 for hdiff, 1 for vadv); triad uses
+2^27 elements.  Each case allocates its fields, runs W warm-up launches and L
+measured launches (CUDA events), prints one line per case, and frees its
+fields before the next case.  The kernel variants are the defaults of the
+library, except vadv-f64 which uses the caller-scratch (GLOBAL) variant as
+``bench.py`` does.
+"""
+
+from __future__ import annotations
+
+import argparse
+import statistics
+import sys
+
+import numpy as np
+
+from . import _native, kernels
+from . import array as sbarray
+from .device import DeviceBuffer, Field
+
+NI, NJ, NK = 512, 512, 80
+STORAGE = {"f64": ("float64", "float64"), "f32": ("float32", "float32"), "bf16": ("bfloat16", "float32")}
+
+
+def _field(rng, storage, halo, lo, hi):
+    shape = (NI + 2 * halo[0], NJ + 2 * halo[1], NK + 2 * halo[2])
+    host = sbarray.alloc_array(shape, storage, (2, 1, 0), 0, index_to_align=halo)
+    vals = rng.uniform(lo, hi, size=shape)
+    if storage == "bfloat16":
+        bits = vals.astype(np.float32).view(np.uint32).astype(np.uint64)
+        host[...] = ((bits + 0x7FFF + ((bits >> 16) & 1)) >> 16).astype(np.uint16)
+    else:
+        host[...] = vals
+    dev = Field.like_host(host, storage, halo)
+    dev.upload(host)
+    return dev
+
+
+def run_case(name, warmup, launches, rng):
+    stencil, form = name.split("-")
+    if stencil == "triad":
+        n = 1 << 27
+        bufs = [DeviceBuffer(n * 8) for _ in range(3)]
+        a, b, c = (x.ptr for x in bufs)
+        kernels.stream_op(_native.STREAM_INIT, "float64", a, b, c, n)
+
+        def launch(timed):
+            return kernels.stream_op(_native.STREAM_TRIAD, "float64", a, b, c, n, 3.0, timed=timed)
+    else:
+        storage, compute = STORAGE[form]
+        if stencil == "hdiff":
+            f = [_field(rng, storage, (2, 2, 0), 0.0, 1.0) for _ in range(3)]
+
+            def launch(timed):
+                return kernels.hdiff(*f, compute=compute, timed=timed)
+        elif stencil == "vadv":
+            f = [_field(rng, storage, (1, 1, 0), -1.0, 1.0) for _ in range(4)]
+            f.append(_field(rng, storage, (1, 1, 0), -0.5, 0.5))
+            out = _field(rng, storage, (1, 1, 0), 0.0, 0.0)
+            scratch = {}
+            tune = None
+            if form == "f64":
+                scratch = {"ccol": _field(rng, storage, (1, 1, 0), 0.0, 0.0),
+                           "dcol": _field(rng, storage, (1, 1, 0), 0.0, 0.0)}
+                tune = _native.tune(variant=_native.VADV_GLOBAL, block_x=64, unroll=2)
+
+            def launch(timed):
+                return kernels.vadv(*f, out=out, compute=compute, tune=tune, timed=timed, **scratch)
+        elif stencil in ("copy", "lap"):
+            f = [_field(rng, storage, (1, 1, 1), 0.0, 1.0) for _ in range(2)]
+
+            def launch(timed):
+                if stencil == "copy":
+                    return kernels.copy(*f, timed=timed)
+                return kernels.laplacian(*f, compute=compute, timed=timed)
+        else:
+            raise SystemExit(f"unknown case {name!r}")
+    for _ in range(warmup):
+        launch(False)
+    times = [launch(True) for _ in range(launches)]
+    print(f"{name}: {launches} launches, median {statistics.median(times) * 1e6:.1f} us", flush=True)
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("cases", nargs="+")
+    ap.add_argument("--warmup", type=int, default=2)
+    ap.add_argument("--launches", type=int, default=1)
+    args = ap.parse_args(argv)
+    cases = []
+    for c in args.cases:
+        if c == "all":
+            cases += [f"{s}-{f}" for s in ("hdiff", "vadv") for f in ("f64", "f32", "bf16")] + ["triad-f64"]
+        else:
+            cases.append(c)
+    _native.call("sb_set_device", 0)
+    rng = np.random.Generator(np.random.PCG64(7))
+    for c in cases:
+        run_case(c, args.warmup, args.launches, rng)
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())
