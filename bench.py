@@ -332,6 +332,65 @@ def run_gpu(args, dist):
     }
 
 
+def run_batched(seed=3, n_domains=64, storage="float32", reps=5):
+    """64 uneven fp32 domains (half hdiff, half vadv): per-domain launches vs one
+    autotuned persistent batched launch replayed from a CUDA graph."""
+    from stencil_benchmarks_gb300 import autotune, kernels
+    from stencil_benchmarks_gb300.batching import Batch
+    from stencil_benchmarks_gb300.device import Event, Stream
+    from stencil_benchmarks_gb300.workloads import device_domain, uneven_specs
+
+    specs = uneven_specs(seed=seed, n=n_domains)
+    built = [device_domain(s, storage) for s in specs]
+    doms = [b[0] for b in built]
+    itemsize = 4 if storage == "float32" else (8 if storage == "float64" else 2)
+    points = sum(s.points for s in specs)
+    cbytes = sum(s.compulsory_bytes(itemsize) for s in specs)
+    max_nk = max(s.nk for s in specs)
+    stream = Stream()
+
+    def plain(timed=False):
+        total = 0.0
+        for s, d in zip(specs, doms):
+            if s.op == "hdiff":
+                t = kernels.hdiff(d.inp, d.coeff, d.out, stream=stream, timed=timed)
+            else:
+                t = kernels.vadv(d.stage, d.pos, d.tens, d.tensstage, d.wcon, out=d.out, stream=stream, timed=timed)
+            total += t or 0.0
+        return total
+
+    plain()
+    stream.synchronize()
+    e0, e1 = Event(), Event()
+    t_async = []
+    for _ in range(reps):
+        e0.record(stream)
+        plain()
+        e1.record(stream)
+        e1.synchronize()
+        t_async.append(e0.elapsed(e1))
+    t_sync = [plain(timed=True) for _ in range(reps)]
+    best, table = autotune.autotune_batch(storage, doms, max_nk)
+    batch = Batch(storage, max_domains=n_domains, max_nk=max_nk, **best)
+    batch.set(doms)
+    t_batch = autotune.time_batch(batch, reps=reps, warmup=2, stream=stream)
+    info = batch.info()
+    ta, ts = statistics.median(t_async), statistics.median(t_sync)
+    return {
+        "workload": f"{n_domains} uneven domains (half hdiff, half vadv), ni,nj in {{32..512 step 32}}, "
+                    f"nk in [40,137], {storage}, seed {seed}",
+        "points": points, "compulsory_bytes": cbytes,
+        "plain_back_to_back": {"ms": ta * 1e3, "gpoints_s": points / ta / 1e9, "hbm_gbs": cbytes / ta / 1e9},
+        "plain_each_synchronised": {"ms": ts * 1e3, "gpoints_s": points / ts / 1e9, "hbm_gbs": cbytes / ts / 1e9},
+        "batched_graph": {"ms": t_batch * 1e3, "gpoints_s": points / t_batch / 1e9, "hbm_gbs": cbytes / t_batch / 1e9,
+                          "items": info["items"], "grid": info["grid"], "block": info["block"],
+                          "workspace_bytes": info["workspace_bytes"]},
+        "speedup_vs_back_to_back": ta / t_batch,
+        "speedup_vs_each_synchronised": ts / t_batch,
+        "autotuned": best, "candidates_timed": len(table),
+    }
+
+
 def cpu_baseline_sample(threads=None):
     """Time the C restatement on the full 512x512x80 hdiff+vadv fp64 step."""
     from oracle import cport
@@ -400,6 +459,7 @@ def main(argv=None):
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true", help="skip the timed CPU baseline")
     ap.add_argument("--no-triad", action="store_true", help="skip the STREAM triad calibration")
+    ap.add_argument("--no-batched", action="store_true", help="skip the batched-domains comparison")
     args = ap.parse_args(argv)
     if args.warmup < 3:
         print("warning: fewer than 3 warm-up steps", file=sys.stderr)
@@ -448,6 +508,8 @@ def main(argv=None):
         }
         if res["triad"]:
             line["stream_triad"]["frac_of_" + peak_kind] = res["triad"]["gbs"] / peak
+        if not args.no_batched:
+            line["batched"] = run_batched()
         if not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline_sample()
         print(json.dumps(line), flush=True)

@@ -159,6 +159,69 @@ int sb_vadv(int storage, int compute, const void* stage, const void* pos, const 
             int64_t nj, int64_t nk, int64_t si, int64_t sj, int64_t sk, int wshift_i, int wshift_j,
             const sb_tune* tune, void* stream, double* time_s);
 
+/* ---- batched execution: many domains, one persistent launch ----------------
+ * No single counterpart in the reference, which launches one generated kernel
+ * per domain (stencils/cuda_hip/templates/base.j2:68-193); this batches the
+ * same hdiff / vadv computations.  A batch holds up to max_domains domains of
+ * one (storage, compute) form; sb_batch_launch runs all of them in one graph
+ * launch (captured on the first launch) of persistent kernels -- one for the
+ * hdiff domains, one per nk bucket for the vadv domains, running side by side
+ * -- that pull work items from device-side queues.  Results
+ * are bit-identical to sb_hdiff / sb_vadv on the same domain.  The domain
+ * table lives in pinned host memory and is copied by each launch: do not
+ * call sb_batch_set while a launch of the same batch may still be pending
+ * (synchronise its stream first).  Distinct batches are independent.        */
+#define SB_OP_HDIFF 0
+#define SB_OP_VADV 1
+typedef struct sb_domain {
+    int32_t op;                 /* SB_OP_HDIFF or SB_OP_VADV                        */
+    int32_t wshift_i, wshift_j; /* vadv: wcon column shift (1,0) u, (0,1) v, (0,0) w */
+    int32_t reserved;
+    int64_t ni, nj, nk, si, sj, sk; /* interior size, element strides              */
+    const void* f[5];           /* hdiff: inp, coeff; vadv: stage, pos, tens, tensstage, wcon */
+    void* out;                  /* hdiff: out; vadv: new tensstage (may be tensstage) */
+} sb_domain;
+typedef struct sb_batch_tune {
+    int32_t block;         /* threads per block, multiple of 32, <= 256 (0: 128)   */
+    int32_t blocks_per_sm; /* persistent blocks per SM (0: 4)                      */
+    int32_t hdiff_rows;    /* rows of j per hdiff item (0: 32)                     */
+    int32_t hdiff_planes;  /* k-planes per hdiff item (0: 1)                       */
+    int32_t order;         /* reserved (vadv domains always run tallest-first)         */
+    int32_t vadv_block;    /* threads (= columns) per vadv block: 32 or 64 (0: 32)   */
+    int32_t vadv_blocks_per_sm; /* persistent vadv blocks per SM (0: as many as fit) */
+    int32_t reserved;
+} sb_batch_tune;
+typedef struct sb_batch sb_batch;
+int sb_batch_create(sb_batch** batch, int storage, int compute, int max_domains, int64_t max_nk,
+                    const sb_batch_tune* tune);
+int sb_batch_set(sb_batch* batch, const sb_domain* domains, int n);
+int sb_batch_launch(sb_batch* batch, void* stream, double* time_s);
+int sb_batch_info(sb_batch* batch, int64_t* total_items, size_t* workspace_bytes, int* grid, int* block);
+int sb_batch_destroy(sb_batch* batch);
+
+/* ---- serving support --------------------------------------------------------
+ * No counterpart in the reference (it runs one benchmark at a time).
+ * sb_fill_batch: fill n device fields in one launch with seeded uniform values
+ * (element e of a field: u = (splitmix64(seed + (e+1)*0x9E3779B97F4A7C15) >> 11)
+ * * 2^-53, value lo + (hi-lo)*u in double, rounded once to float32 storage, or
+ * to float32 then bfloat16).  The descriptors are copied (asynchronously on
+ * `stream`, from the caller's host memory, which must stay valid until the
+ * stream reaches the copy) into `desc_scratch`, a device buffer of at least n
+ * descriptors owned by the caller.
+ * sb_event_query: SB_OK if the event has completed, SB_NOT_READY if not.      */
+#define SB_NOT_READY 7
+typedef struct sb_fill_desc {
+    void* ptr;     /* device field (whole span, halo included)  */
+    int64_t count; /* elements                                   */
+    uint64_t seed;
+    double lo, hi;
+    int32_t storage; /* SB_F64, SB_F32, SB_BF16 */
+    int32_t reserved;
+} sb_fill_desc;
+int sb_fill_batch(const sb_fill_desc* descs, int n, void* desc_scratch, void* stream);
+int sb_event_query(void* event);
+int sb_stream_wait_event(void* stream, void* event); /* later work on stream waits for event */
+
 /* ---- vertical advection without device allocation -------------------------
  * No counterpart in the reference.  For callers that cannot call cudaMalloc:
  * code embedded in a host framework that owns every device allocation (fixed

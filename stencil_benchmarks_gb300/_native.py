@@ -26,6 +26,7 @@ SB_ERR_UNSUPPORTED = 3
 SB_ERR_NOMEM = 4
 SB_ERR_TIMEOUT = 5
 SB_ERR_BUDGET = 6
+SB_NOT_READY = 7
 
 SB_F64, SB_F32, SB_BF16 = 0, 1, 2
 H2H, H2D, D2H, D2D = 0, 1, 2, 3
@@ -115,6 +116,16 @@ SIGNATURES = {
     "sb_hdiff": [_int, _int, _vp, _vp, _vp] + [_i64] * 6 + [_tp, _vp, _dp],
     "sb_vadv": [_int, _int] + [_vp] * 8 + [_i64] * 6 + [_int, _int, _tp, _vp, _dp],
     "sb_vadv_noalloc": [_int, _int] + [_vp] * 6 + [_i64] * 6 + [_int, _int, _vp, _dp],
+    # batch entry points take struct pointers; batching.py narrows these types
+    "sb_batch_create": [ctypes.POINTER(_vp), _int, _int, _int, _i64, _vp],
+    "sb_batch_set": [_vp, _vp, _int],
+    "sb_batch_launch": [_vp, _vp, _dp],
+    "sb_batch_info": [_vp, ctypes.POINTER(_i64), ctypes.POINTER(_size), ctypes.POINTER(_int),
+                      ctypes.POINTER(_int)],
+    "sb_batch_destroy": [_vp],
+    "sb_fill_batch": [_vp, _int, _vp, _vp],
+    "sb_event_query": [_vp],
+    "sb_stream_wait_event": [_vp, _vp],
     "sb_probe_arith_rate": [_int, _dp],
 }
 _RESTYPES = {"sb_last_error": ctypes.c_char_p}

@@ -1,0 +1,487 @@
+// Batched execution: many hdiff / vadv domains of uneven size in one graph
+// launch of persistent kernels that pull work from device-side queues.
+//
+// One graph (captured on the first launch, replayed afterwards):
+//     copy the domain table from pinned host memory -> zero the queue counters
+//       -> fork:  hdiff kernel            (queue 0)
+//                 vadv kernel, nk bucket 0 (queue 1)
+//                 ...                      (one per bucket)
+//       -> join
+// Kernels of different branches run concurrently on the GPU, so the long
+// serial vadv columns overlap the bandwidth-bound hdiff strips.
+//
+// hdiff: persistent warps; an item is a strip of 28 output columns x `rows`
+//   rows x `planes` k-planes of one domain (stencil_core.cuh:
+//   hdiff_jscan_strip).  A warp takes the next item with one atomicAdd and
+//   finds its domain by binary search over first-item offsets staged in
+//   shared memory.
+// vadv: persistent blocks of BT threads; an item is BT consecutive columns of
+//   one j-row of one domain, one column per thread (stencil_core.cuh:
+//   vadv_async_column: cp.async-staged inputs, factors in shared memory).
+//   Domains are grouped into 8 nk buckets (caps max_nk/8, 2*max_nk/8, ...) and
+//   each bucket's kernel is sized for its cap, so short columns do not pay for
+//   the shared memory of the tallest one.
+// No kernel waits on another warp or kernel: every queue is one atomic counter.
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "stencil_core.cuh"
+
+namespace sb {
+namespace {
+
+constexpr int kMaxBatchDomains = 1024;
+constexpr int kBuckets = 8;
+constexpr int kVadvDepth = 4;
+
+struct DevDomain {
+    int32_t op;  // SB_OP_HDIFF / SB_OP_VADV
+    int32_t ni, nj, nk;
+    int64_t si, sj, sk, wsh;
+    const void* f[5];
+    void* out;
+    int64_t item_begin;  // first item of this domain in its queue
+    int32_t items_i, items_j;
+};
+
+struct DevTable {
+    int32_t ndomains, n_hdiff;
+    int32_t rows, planes;
+    int64_t hdiff_items;
+    int32_t bucket_first[kBuckets + 1];  // vadv bucket b: domains [bucket_first[b], bucket_first[b+1])
+    int32_t pad;
+    int64_t bucket_items[kBuckets];
+    DevDomain dom[1];  // ndomains entries: hdiff first, then vadv by bucket
+};
+
+size_t table_bytes(int n) { return offsetof(DevTable, dom) + sizeof(DevDomain) * (size_t)(n > 0 ? n : 1); }
+
+template <class S, class C, int U, class IDX>
+__global__ void __launch_bounds__(256)
+    batch_hdiff_kernel(const DevTable* __restrict__ tab, unsigned long long* __restrict__ counter) {
+    __shared__ int64_t s_begin[kMaxBatchDomains + 1];
+    const int nd = tab->n_hdiff;
+    const int64_t total = tab->hdiff_items;
+    if (total == 0) return;
+    const int rows = tab->rows, planes = tab->planes;
+    for (int d = threadIdx.x; d < nd; d += blockDim.x) s_begin[d] = tab->dom[d].item_begin;
+    if (threadIdx.x == 0) s_begin[nd] = total;
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    for (;;) {
+        unsigned long long item = 0;
+        if (lane == 0) item = atomicAdd(counter, 1ULL);
+        item = __shfl_sync(0xffffffffu, item, 0);
+        if ((int64_t)item >= total) break;
+        int lo = 0, hi = nd - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (s_begin[mid] <= (int64_t)item) lo = mid; else hi = mid - 1;
+        }
+        const DevDomain& dm = tab->dom[lo];
+        const int64_t local = (int64_t)item - s_begin[lo];
+        const int strip = (int)(local % dm.items_i);
+        const int64_t rest = local / dm.items_i;
+        const int jb = (int)(rest % dm.items_j);
+        const int k0 = (int)(rest / dm.items_j) * planes;
+        const int k1 = min(dm.nk, k0 + planes);
+        const int i = strip * kJscanOut - 2 + lane;
+        const int j0 = jb * rows;
+        const int j1 = min(dm.nj, j0 + rows);
+        for (int k = k0; k < k1; ++k) {
+            hdiff_jscan_strip<S, C, U, IDX>((const S*)dm.f[0], (const S*)dm.f[1], (S*)dm.out, dm.ni, dm.nj,
+                                            (IDX)dm.si, (IDX)dm.sj, (IDX)dm.sk, i, lane, j0, j1, k);
+        }
+    }
+}
+
+// Dynamic shared memory: ccol[cap][BT], dcol[cap][BT] (compute type), then the
+// staging ring [D+1][6][BT] (storage type) at ring_offset.
+template <class S, class C, int BT, int D, class IDX>
+__global__ void __launch_bounds__(BT)
+    batch_vadv_kernel(const DevTable* __restrict__ tab, unsigned long long* __restrict__ counter, int bucket,
+                      int cap, int ring_offset) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ int s_dom;
+    __shared__ int64_t s_local;
+    const int first = tab->bucket_first[bucket], last = tab->bucket_first[bucket + 1];
+    const int64_t total = tab->bucket_items[bucket];
+    if (total == 0) return;
+    const int t = threadIdx.x;
+    C* sc = reinterpret_cast<C*>(smem_raw) + t;
+    S* ring = reinterpret_cast<S*>(smem_raw + ring_offset) + t;
+    for (;;) {
+        if (t == 0) {
+            const int64_t item = (int64_t)atomicAdd(counter, 1ULL);
+            int d = -1;
+            if (item < total) {
+                int lo = first, hi = last - 1;
+                while (lo < hi) {
+                    const int mid = (lo + hi + 1) >> 1;
+                    if (tab->dom[mid].item_begin <= item) lo = mid; else hi = mid - 1;
+                }
+                d = lo;
+                s_local = item - tab->dom[lo].item_begin;
+            }
+            s_dom = d;
+        }
+        __syncthreads();
+        const int d = s_dom;
+        if (d < 0) break;
+        const DevDomain& dm = tab->dom[d];
+        const int group = (int)(s_local % dm.items_i);
+        const int j = (int)(s_local / dm.items_i);
+        const int i = group * BT + t;
+        if (i < dm.ni) {
+            const IDX col = (IDX)i * (IDX)dm.si + (IDX)j * (IDX)dm.sj;
+            if constexpr (sizeof(S) == 2) {
+                // 2-byte storage: cp.async copies 4+ bytes, so stage through registers
+                const SmemFactors<C> fac{sc, sc + dm.nk * BT, BT};
+                vadv_column<S, C, D>((const S*)dm.f[0], (const S*)dm.f[1], (const S*)dm.f[2], (const S*)dm.f[3],
+                                     (const S*)dm.f[4], (S*)dm.out, (int64_t)col, dm.nk, dm.sk, dm.wsh, fac);
+            } else {
+                vadv_async_column<S, C, BT, D, IDX>((const S*)dm.f[0], (const S*)dm.f[1], (const S*)dm.f[2],
+                                                    (const S*)dm.f[3], (const S*)dm.f[4], (S*)dm.out, col, dm.nk,
+                                                    (IDX)dm.sk, (IDX)dm.wsh, sc, sc + dm.nk * BT, ring);
+            }
+        }
+        __syncthreads();  // s_dom / s_local are rewritten by the next grab
+    }
+}
+
+struct Kinds {
+    void (*hdiff)(dim3, dim3, cudaStream_t, const DevTable*, unsigned long long*);
+    void (*vadv32)(dim3, dim3, size_t, cudaStream_t, const DevTable*, unsigned long long*, int, int, int);
+    void (*vadv64)(dim3, dim3, size_t, cudaStream_t, const DevTable*, unsigned long long*, int, int, int);
+    const void* vadv32_fn;
+    const void* vadv64_fn;
+    int storage_bytes, compute_bytes;
+};
+
+template <class S, class C, int U, class IDX>
+void run_hdiff(dim3 g, dim3 b, cudaStream_t s, const DevTable* t, unsigned long long* c) {
+    batch_hdiff_kernel<S, C, U, IDX><<<g, b, 0, s>>>(t, c);
+}
+template <class S, class C, int BT, class IDX>
+void run_vadv(dim3 g, dim3 b, size_t smem, cudaStream_t s, const DevTable* t, unsigned long long* c, int bucket,
+              int cap, int ring_offset) {
+    batch_vadv_kernel<S, C, BT, kVadvDepth, IDX><<<g, b, smem, s>>>(t, c, bucket, cap, ring_offset);
+}
+
+template <class S, class C, int U, class IDX>
+Kinds kinds_for() {
+    Kinds k;
+    k.hdiff = &run_hdiff<S, C, U, IDX>;
+    k.vadv32 = &run_vadv<S, C, 32, IDX>;
+    k.vadv64 = &run_vadv<S, C, 64, IDX>;
+    k.vadv32_fn = (const void*)&batch_vadv_kernel<S, C, 32, kVadvDepth, IDX>;
+    k.vadv64_fn = (const void*)&batch_vadv_kernel<S, C, 64, kVadvDepth, IDX>;
+    k.storage_bytes = sizeof(S);
+    k.compute_bytes = sizeof(C);
+    return k;
+}
+
+bool pick_kinds(int storage, int compute, bool idx64, Kinds* out) {
+#define SB_PICK(SC, CC, S, C, U)                                                          \
+    if (storage == SC && compute == CC) {                                                 \
+        *out = idx64 ? kinds_for<S, C, U, int64_t>() : kinds_for<S, C, U, int>();         \
+        return true;                                                                      \
+    }
+    SB_PICK(SB_F64, SB_F64, double, double, 2)
+    SB_PICK(SB_F32, SB_F32, float, float, 4)
+    SB_PICK(SB_F32, SB_F64, float, double, 2)
+    SB_PICK(SB_BF16, SB_F32, bf16, float, 4)
+#undef SB_PICK
+    return false;
+}
+
+}  // namespace
+}  // namespace sb
+
+using namespace sb;
+
+struct sb_batch {
+    int device = 0;
+    int storage = 0, compute = 0;
+    int max_domains = 0;
+    int64_t max_nk = 0;
+    sb_batch_tune tune{};
+    int hdiff_grid = 0, hdiff_block = 0;
+    int vadv_block = 32;
+    int cap[kBuckets] = {};
+    int vadv_grid[kBuckets] = {};
+    size_t vadv_smem[kBuckets] = {};
+    int ring_offset[kBuckets] = {};
+    bool idx64 = false;
+    DevTable* host_table = nullptr;  // pinned
+    DevTable* dev_table = nullptr;
+    unsigned long long* counters = nullptr;  // [1 + kBuckets]
+    cudaStream_t streams[1 + 1 + kBuckets] = {};
+    cudaEvent_t fork = nullptr;
+    cudaEvent_t joins[1 + kBuckets] = {};
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    bool graph_idx64 = false;
+    int64_t total_items = 0;
+};
+
+namespace {
+
+void release(sb_batch* b) {
+    if (!b) return;
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    for (auto& s : b->streams)
+        if (s) cudaStreamDestroy(s);
+    if (b->fork) cudaEventDestroy(b->fork);
+    for (auto& e : b->joins)
+        if (e) cudaEventDestroy(e);
+    if (b->counters) cudaFree(b->counters);
+    if (b->dev_table) cudaFree(b->dev_table);
+    if (b->host_table) cudaFreeHost(b->host_table);
+    delete b;
+}
+
+size_t vadv_smem_bytes(int cap, int bt, int cbytes, int sbytes, int* ring_offset) {
+    const size_t fac = ((2 * (size_t)cbytes * cap * bt) + 15) / 16 * 16;
+    if (ring_offset) *ring_offset = (int)fac;
+    return fac + (size_t)(kVadvDepth + 1) * 6 * bt * sbytes;
+}
+
+int capture_graph(sb_batch* b) {
+    if (b->exec) {
+        cudaGraphExecDestroy(b->exec);
+        b->exec = nullptr;
+    }
+    if (b->graph) {
+        cudaGraphDestroy(b->graph);
+        b->graph = nullptr;
+    }
+    Kinds k;
+    SB_CHECK(pick_kinds(b->storage, b->compute, b->idx64, &k), SB_ERR_UNSUPPORTED, "unsupported form");
+    auto vadv_run = b->vadv_block == 64 ? k.vadv64 : k.vadv32;
+    const void* vadv_fn = b->vadv_block == 64 ? k.vadv64_fn : k.vadv32_fn;
+    for (int q = 0; q < kBuckets; ++q) {
+        if (b->vadv_smem[q] > 48 * 1024)
+            SB_CUDA(cudaFuncSetAttribute(vadv_fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b->vadv_smem[q]));
+    }
+    cudaStream_t s0 = b->streams[0];
+    SB_CUDA(cudaStreamBeginCapture(s0, cudaStreamCaptureModeThreadLocal));
+    cudaMemcpyAsync(b->dev_table, b->host_table, table_bytes(b->max_domains), cudaMemcpyHostToDevice, s0);
+    cudaMemsetAsync(b->counters, 0, sizeof(unsigned long long) * (1 + kBuckets), s0);
+    cudaEventRecord(b->fork, s0);
+    cudaStreamWaitEvent(b->streams[1], b->fork, 0);
+    k.hdiff(dim3(b->hdiff_grid), dim3(b->hdiff_block), b->streams[1], b->dev_table, b->counters);
+    cudaEventRecord(b->joins[0], b->streams[1]);
+    for (int q = 0; q < kBuckets; ++q) {
+        cudaStreamWaitEvent(b->streams[2 + q], b->fork, 0);
+        vadv_run(dim3(b->vadv_grid[q]), dim3(b->vadv_block), b->vadv_smem[q], b->streams[2 + q], b->dev_table,
+                 b->counters + 1 + q, q, b->cap[q], b->ring_offset[q]);
+        cudaEventRecord(b->joins[1 + q], b->streams[2 + q]);
+    }
+    for (int q = 0; q < 1 + kBuckets; ++q) cudaStreamWaitEvent(s0, b->joins[q], 0);
+    cudaGraph_t graph = nullptr;
+    const cudaError_t ec = cudaStreamEndCapture(s0, &graph);
+    if (ec != cudaSuccess) {
+        cudaGetLastError();
+        return fail(SB_ERR_CUDA, "capturing the batch graph failed: %s", cudaGetErrorString(ec));
+    }
+    b->graph = graph;
+    SB_CUDA(cudaGraphInstantiate(&b->exec, graph, 0));
+    b->graph_idx64 = b->idx64;
+    return SB_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int sb_batch_create(sb_batch** out, int storage, int compute, int max_domains, int64_t max_nk,
+                    const sb_batch_tune* tune) {
+    clear_error();
+    SB_CHECK(out, SB_ERR_INVALID, "out is NULL");
+    *out = nullptr;
+    Kinds k;
+    SB_CHECK(pick_kinds(storage, compute, false, &k), SB_ERR_UNSUPPORTED,
+             "unsupported storage/compute combination (%d, %d)", storage, compute);
+    SB_CHECK(max_domains >= 1 && max_domains <= kMaxBatchDomains, SB_ERR_INVALID,
+             "max_domains must be in [1, %d]", kMaxBatchDomains);
+    SB_CHECK(max_nk >= 2 && max_nk <= (1 << 20), SB_ERR_INVALID, "max_nk must be in [2, 2^20]");
+    const DeviceProps* p;
+    int rc = device_props(&p);
+    if (rc) return rc;
+    sb_batch* b = new sb_batch();
+    b->device = p->device;
+    b->storage = storage;
+    b->compute = compute;
+    b->max_domains = max_domains;
+    b->max_nk = max_nk;
+    if (tune) b->tune = *tune;
+    b->hdiff_block = b->tune.block > 0 ? b->tune.block : 128;
+    const int per_sm = b->tune.blocks_per_sm > 0 ? b->tune.blocks_per_sm : 4;
+    b->vadv_block = b->tune.vadv_block > 0 ? b->tune.vadv_block : 32;
+    if (b->hdiff_block % 32 || b->hdiff_block > 256 || per_sm > 32 || (b->vadv_block != 32 && b->vadv_block != 64)) {
+        release(b);
+        return fail(SB_ERR_INVALID,
+                    "batch: hdiff block must be a multiple of 32 <= 256, blocks_per_sm <= 32, vadv block 32 or 64");
+    }
+    if (b->tune.hdiff_rows <= 0) b->tune.hdiff_rows = 32;
+    if (b->tune.hdiff_planes <= 0) b->tune.hdiff_planes = 1;
+    b->hdiff_grid = p->sm_count * per_sm;
+    for (int q = 0; q < kBuckets; ++q) {
+        b->cap[q] = (int)std::max<int64_t>(2, ceil_div(max_nk * (q + 1), kBuckets));
+        b->vadv_smem[q] = vadv_smem_bytes(b->cap[q], b->vadv_block, k.compute_bytes, k.storage_bytes,
+                                          &b->ring_offset[q]);
+        if ((int64_t)b->vadv_smem[q] > p->smem_optin) {
+            const size_t need = b->vadv_smem[q];
+            release(b);
+            return fail(SB_ERR_INVALID,
+                        "batch: columns of %lld levels need %zu bytes of shared memory per block (limit %d); "
+                        "use a smaller max_nk or vadv block",
+                        (long long)max_nk, need, p->smem_optin);
+        }
+        const int fit = (int)std::min<int64_t>(16, (p->smem_optin + 1024) / (int64_t)(b->vadv_smem[q] + 1024));
+        const int vper = b->tune.vadv_blocks_per_sm > 0 ? std::min(b->tune.vadv_blocks_per_sm, fit) : fit;
+        b->vadv_grid[q] = p->sm_count * std::max(1, vper);
+    }
+    cudaError_t e = cudaMallocHost((void**)&b->host_table, table_bytes(max_domains));
+    if (e == cudaSuccess) e = cudaMalloc((void**)&b->dev_table, table_bytes(max_domains));
+    if (e == cudaSuccess) e = cudaMalloc((void**)&b->counters, sizeof(unsigned long long) * (1 + kBuckets));
+    for (auto& s : b->streams)
+        if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming);
+    for (auto& ev : b->joins)
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        release(b);
+        return fail(e == cudaErrorMemoryAllocation ? SB_ERR_NOMEM : SB_ERR_CUDA, "batch allocation failed: %s",
+                    cudaGetErrorString(e));
+    }
+    memset(b->host_table, 0, table_bytes(max_domains));
+    b->host_table->rows = b->tune.hdiff_rows;
+    b->host_table->planes = b->tune.hdiff_planes;
+    *out = b;
+    return SB_OK;
+}
+
+int sb_batch_destroy(sb_batch* b) {
+    if (b) {
+        for (auto& s : b->streams)
+            if (s) cudaStreamSynchronize(s);
+        release(b);
+    }
+    return SB_OK;
+}
+
+int sb_batch_set(sb_batch* b, const sb_domain* domains, int n) {
+    clear_error();
+    SB_CHECK(b, SB_ERR_INVALID, "batch is NULL");
+    SB_CHECK(n >= 0 && n <= b->max_domains, SB_ERR_INVALID, "%d domains exceed the batch capacity %d", n,
+             b->max_domains);
+    SB_CHECK(n == 0 || domains, SB_ERR_INVALID, "domains is NULL");
+    // validate; classify: hdiff (in given order), vadv by bucket (decreasing nk within a bucket)
+    std::vector<int> hd, vd[kBuckets];
+    for (int q = 0; q < n; ++q) {
+        const sb_domain& s = domains[q];
+        int rc = check_domain(s.ni, s.nj, s.nk, s.si, s.sj, s.sk);
+        if (rc) return rc;
+        SB_CHECK(s.op == SB_OP_HDIFF || s.op == SB_OP_VADV, SB_ERR_INVALID, "domain %d: unknown op %d", q, s.op);
+        const int nin = s.op == SB_OP_HDIFF ? 2 : 5;
+        for (int f = 0; f < nin; ++f) SB_CHECK(s.f[f], SB_ERR_INVALID, "domain %d: NULL field %d", q, f);
+        SB_CHECK(s.out, SB_ERR_INVALID, "domain %d: NULL output", q);
+        if (s.op == SB_OP_HDIFF) {
+            hd.push_back(q);
+        } else {
+            SB_CHECK(s.nk >= 2 || s.ni == 0 || s.nj == 0, SB_ERR_INVALID,
+                     "domain %d: vertical advection needs nk >= 2", q);
+            SB_CHECK(s.nk <= b->max_nk, SB_ERR_INVALID, "domain %d: nk = %lld exceeds the batch's max_nk %lld", q,
+                     (long long)s.nk, (long long)b->max_nk);
+            SB_CHECK(s.wshift_i >= 0 && s.wshift_i <= 1 && s.wshift_j >= 0 && s.wshift_j <= 1 &&
+                         s.wshift_i + s.wshift_j <= 1,
+                     SB_ERR_INVALID, "domain %d: bad wcon shift", q);
+            int bucket = 0;
+            while (bucket < kBuckets - 1 && s.nk > b->cap[bucket]) ++bucket;
+            vd[bucket].push_back(q);
+        }
+    }
+    for (auto& v : vd)
+        std::stable_sort(v.begin(), v.end(), [&](int x, int y) { return domains[x].nk > domains[y].nk; });
+    bool idx64 = false;
+    DevTable* t = b->host_table;
+    int slot = 0;
+    auto fill = [&](int q, int64_t& items) {
+        const sb_domain& s = domains[q];
+        DevDomain& d = t->dom[slot++];
+        memset(&d, 0, sizeof(d));
+        d.op = s.op;
+        d.ni = (int32_t)s.ni;
+        d.nj = (int32_t)s.nj;
+        d.nk = (int32_t)s.nk;
+        d.si = s.si;
+        d.sj = s.sj;
+        d.sk = s.sk;
+        for (int f = 0; f < 5; ++f) d.f[f] = s.f[f];
+        d.out = s.out;
+        d.item_begin = items;
+        const int64_t span = (s.ni + 33) * std::abs(s.si) + (s.nj + 2) * std::abs(s.sj) + (s.nk + 1) * std::abs(s.sk);
+        if (span >= (1LL << 31)) idx64 = true;
+        if (s.ni == 0 || s.nj == 0 || s.nk == 0) return;
+        if (s.op == SB_OP_HDIFF) {
+            d.items_i = (int32_t)ceil_div(s.ni, kJscanOut);
+            d.items_j = (int32_t)ceil_div(s.nj, b->tune.hdiff_rows);
+            items += (int64_t)d.items_i * d.items_j * ceil_div(s.nk, b->tune.hdiff_planes);
+        } else {
+            d.wsh = (int64_t)s.wshift_i * s.si + (int64_t)s.wshift_j * s.sj;
+            d.items_i = (int32_t)ceil_div(s.ni, b->vadv_block);
+            d.items_j = (int32_t)s.nj;
+            items += (int64_t)d.items_i * d.items_j;
+        }
+    };
+    int64_t hitems = 0;
+    for (int q : hd) fill(q, hitems);
+    t->n_hdiff = (int32_t)hd.size();
+    t->hdiff_items = hitems;
+    int64_t total = hitems;
+    for (int bk = 0; bk < kBuckets; ++bk) {
+        t->bucket_first[bk] = slot;
+        int64_t items = 0;
+        for (int q : vd[bk]) fill(q, items);
+        t->bucket_items[bk] = items;
+        total += items;
+    }
+    t->bucket_first[kBuckets] = slot;
+    t->ndomains = n;
+    b->total_items = total;
+    b->idx64 = idx64;
+    return SB_OK;
+}
+
+int sb_batch_launch(sb_batch* b, void* stream, double* time_s) {
+    clear_error();
+    SB_CHECK(b, SB_ERR_INVALID, "batch is NULL");
+    int dev = 0;
+    SB_CUDA(cudaGetDevice(&dev));
+    SB_CHECK(dev == b->device, SB_ERR_INVALID, "batch was created on device %d, current device is %d", b->device,
+             dev);
+    if (!b->exec || b->graph_idx64 != b->idx64) {
+        int rc = capture_graph(b);
+        if (rc) return rc;
+    }
+    return timed((cudaStream_t)stream, time_s, [&]() {
+        SB_CUDA(cudaGraphLaunch(b->exec, (cudaStream_t)stream));
+        return SB_OK;
+    });
+}
+
+int sb_batch_info(sb_batch* b, int64_t* total_items, size_t* workspace_bytes, int* grid, int* block) {
+    SB_CHECK(b, SB_ERR_INVALID, "batch is NULL");
+    if (total_items) *total_items = b->total_items;
+    if (workspace_bytes) *workspace_bytes = 0;
+    if (grid) *grid = b->hdiff_grid;
+    if (block) *block = b->hdiff_block;
+    return SB_OK;
+}
+
+}  // extern "C"

@@ -22,7 +22,7 @@
 // relative to the interior pointer (a halo of at least 2 in i and j).
 #include <cstdlib>
 
-#include "common.cuh"
+#include "stencil_core.cuh"
 
 namespace sb {
 namespace {
@@ -118,78 +118,17 @@ __global__ void __launch_bounds__(TX* NTY)
 // (all loads of a chunk issued before its arithmetic) to keep U row
 // requests per warp in flight.  Block = (32, NW) warps side by side in i;
 // grid = (strips of 28*NW columns, j-segments of TY rows, k-chunks of KPER).
-constexpr int kJscanOut = 28;
-
 template <class S, class C, int U, class IDX>
 __global__ void __launch_bounds__(256)
     hdiff_jscan_kernel(const S* __restrict__ inp, const S* __restrict__ coeff, S* __restrict__ out,
                        int ni, int nj, int nk, IDX si, IDX sj, IDX sk, int TY, int kper) {
-    using A = Ar<C>;
     const int lane = threadIdx.x;
     const int i = (blockIdx.x * blockDim.y + threadIdx.y) * kJscanOut - 2 + lane;  // column of this lane
     const int j0 = blockIdx.y * TY;
     const int j1 = min(nj, j0 + TY);  // output rows [j0, j1)
     const int k0 = blockIdx.z * kper;
     const int k1 = min(nk, k0 + kper);
-    const bool col_in = i <= ni + 1;  // inside the halo'd array (i >= -2 always)
-    const bool writer = lane >= 2 && lane < 2 + kJscanOut && i < ni;
-    const int rmax = nj + 1;  // last row inside the halo'd array
-
-    for (int k = k0; k < k1; ++k) {
-        const IDX obase = (IDX)k * sk + (IDX)i * si;
-        auto load_row = [&](int r) -> C {
-            return (col_in && r <= rmax) ? ld<C, S>(inp + (obase + (IDX)r * sj)) : C(0);
-        };
-        auto lap_of = [&](C below, C center, C above) -> C {
-            const C left = __shfl_up_sync(0xffffffffu, center, 1);
-            const C right = __shfl_down_sync(0xffffffffu, center, 1);
-            return A::sub(A::template scale2<2>(center), A::add(A::add(A::add(right, left), above), below));
-        };
-        // preamble: rows j0-2 .. j0+1
-        const C am2 = load_row(j0 - 2);
-        C a0 = load_row(j0 - 1);  // inp(j-1) until rotated
-        C a1 = load_row(j0);
-        C a2 = load_row(j0 + 1);
-        const C lap_m1 = lap_of(am2, a0, a1);  // lap(j0-1)
-        C lap0 = lap_of(a0, a1, a2);           // lap(j0)
-        C fly_m1 = A::limit(A::sub(lap0, lap_m1), a1, a0);  // fly(j0-1)
-        C right0 = __shfl_down_sync(0xffffffffu, a1, 1);    // inp(i+1, j0)
-        // state for output row j: a0 = inp(j), a1 = inp(j+1), lap0 = lap(j)
-        a0 = a1;
-        a1 = a2;
-
-        for (int jb = j0; jb < j1; jb += U) {
-            C nxt[U], cf[U];
-#pragma unroll
-            for (int u = 0; u < U; ++u) {
-                const int j = jb + u;
-                nxt[u] = load_row(j + 2);
-                cf[u] = (writer && j < j1) ? ld<C, S>(coeff + (obase + (IDX)j * sj)) : C(0);
-            }
-#pragma unroll
-            for (int u = 0; u < U; ++u) {
-                const int j = jb + u;
-                if (jb + u >= j1) break;  // warp-uniform
-                const C a2n = nxt[u];
-                const C left1 = __shfl_up_sync(0xffffffffu, a1, 1);
-                const C right1 = __shfl_down_sync(0xffffffffu, a1, 1);
-                const C lap1 = A::sub(A::template scale2<2>(a1), A::add(A::add(A::add(right1, left1), a2n), a0));
-                const C fly0 = A::limit(A::sub(lap1, lap0), a1, a0);              // fly(i, j)
-                const C lapR = __shfl_down_sync(0xffffffffu, lap0, 1);            // lap(i+1, j)
-                const C flx0 = A::limit(A::sub(lapR, lap0), right0, a0);          // flx(i, j)
-                const C flxL = __shfl_up_sync(0xffffffffu, flx0, 1);              // flx(i-1, j)
-                if (writer) {
-                    const C d = A::sub(A::add(A::sub(flx0, flxL), fly0), fly_m1);
-                    st<S, C>(out + (obase + (IDX)j * sj), A::sub(a0, A::mul(cf[u], d)));
-                }
-                a0 = a1;
-                a1 = a2n;
-                lap0 = lap1;
-                fly_m1 = fly0;
-                right0 = right1;
-            }
-        }
-    }
+    for (int k = k0; k < k1; ++k) hdiff_jscan_strip<S, C, U, IDX>(inp, coeff, out, ni, nj, si, sj, sk, i, lane, j0, j1, k);
 }
 
 template <class S, class C, class IDX>

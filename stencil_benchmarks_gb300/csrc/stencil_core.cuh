@@ -1,0 +1,335 @@
+// Per-warp / per-thread stencil bodies shared by the per-domain kernels
+// (hdiff.cu, vadv.cu) and the persistent batched kernel (batch.cu).
+#pragma once
+
+#include "common.cuh"
+
+namespace sb {
+
+// ---------------------------------------------------------------------------
+// horizontal diffusion, one warp, one k-plane strip of 32 columns
+// ---------------------------------------------------------------------------
+// Lane L owns column i = i_lane (caller passes i0 - 2 + L); lanes 2..29 write
+// rows [j0, j1) of the output (28 columns), lanes 0-1 and 30-31 supply the
+// i-halo.  Arithmetic and order as stencil_benchmarks/benchmarks_collection/
+// stencils/base.py:284-311; inp(i+-1), lap(i+1), flx(i-1) by shuffles; U rows
+// of loads issued together.  All 32 lanes must call this (full-mask shuffles).
+constexpr int kJscanOut = 28;
+
+template <class S, class C, int U, class IDX>
+__device__ __forceinline__ void hdiff_jscan_strip(const S* __restrict__ inp, const S* __restrict__ coeff,
+                                                  S* __restrict__ out, int ni, int nj, IDX si, IDX sj, IDX sk,
+                                                  int i, int lane, int j0, int j1, int k) {
+    using A = Ar<C>;
+    const bool col_in = i <= ni + 1;  // inside the halo'd array (i >= -2 always)
+    const bool writer = lane >= 2 && lane < 2 + kJscanOut && i < ni;
+    const int rmax = nj + 1;  // last row inside the halo'd array
+    const IDX obase = (IDX)k * sk + (IDX)i * si;
+    auto load_row = [&](int r) -> C {
+        return (col_in && r <= rmax) ? ld<C, S>(inp + (obase + (IDX)r * sj)) : C(0);
+    };
+    auto lap_of = [&](C below, C center, C above) -> C {
+        const C left = __shfl_up_sync(0xffffffffu, center, 1);
+        const C right = __shfl_down_sync(0xffffffffu, center, 1);
+        return A::sub(A::template scale2<2>(center), A::add(A::add(A::add(right, left), above), below));
+    };
+    // preamble: rows j0-2 .. j0+1
+    const C am2 = load_row(j0 - 2);
+    C a0 = load_row(j0 - 1);
+    C a1 = load_row(j0);
+    C a2 = load_row(j0 + 1);
+    const C lap_m1 = lap_of(am2, a0, a1);               // lap(j0-1)
+    C lap0 = lap_of(a0, a1, a2);                        // lap(j0)
+    C fly_m1 = A::limit(A::sub(lap0, lap_m1), a1, a0);  // fly(j0-1)
+    C right0 = __shfl_down_sync(0xffffffffu, a1, 1);    // inp(i+1, j0)
+    // state for output row j: a0 = inp(j), a1 = inp(j+1), lap0 = lap(j)
+    a0 = a1;
+    a1 = a2;
+    for (int jb = j0; jb < j1; jb += U) {
+        C nxt[U], cf[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int j = jb + u;
+            nxt[u] = load_row(j + 2);
+            cf[u] = (writer && j < j1) ? ld<C, S>(coeff + (obase + (IDX)j * sj)) : C(0);
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int j = jb + u;
+            if (j >= j1) break;  // warp-uniform
+            const C a2n = nxt[u];
+            const C left1 = __shfl_up_sync(0xffffffffu, a1, 1);
+            const C right1 = __shfl_down_sync(0xffffffffu, a1, 1);
+            const C lap1 = A::sub(A::template scale2<2>(a1), A::add(A::add(A::add(right1, left1), a2n), a0));
+            const C fly0 = A::limit(A::sub(lap1, lap0), a1, a0);      // fly(i, j)
+            const C lapR = __shfl_down_sync(0xffffffffu, lap0, 1);    // lap(i+1, j)
+            const C flx0 = A::limit(A::sub(lapR, lap0), right0, a0);  // flx(i, j)
+            const C flxL = __shfl_up_sync(0xffffffffu, flx0, 1);      // flx(i-1, j)
+            if (writer) {
+                const C d = A::sub(A::add(A::sub(flx0, flxL), fly0), fly_m1);
+                st<S, C>(out + (obase + (IDX)j * sj), A::sub(a0, A::mul(cf[u], d)));
+            }
+            a0 = a1;
+            a1 = a2n;
+            lap0 = lap1;
+            fly_m1 = fly0;
+            right0 = right1;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// vertical advection, one thread, one column
+// ---------------------------------------------------------------------------
+// Storage of the per-level elimination factors (ccol, dcol):
+template <class C>
+struct SmemFactors {  // shared memory, level k at c[k * stride]
+    C* c;
+    C* d;
+    int stride;
+    static constexpr bool kPrefetch = false;
+    __device__ __forceinline__ void put(int k, C cv, C dv) const {
+        c[(size_t)k * stride] = cv;
+        d[(size_t)k * stride] = dv;
+    }
+    __device__ __forceinline__ C getc(int k) const { return c[(size_t)k * stride]; }
+    __device__ __forceinline__ C getd(int k) const { return d[(size_t)k * stride]; }
+};
+
+template <class C>
+struct GlobalFactors {  // global memory, level k at c[k * stride] (read back with prefetch)
+    C* c;
+    C* d;
+    int64_t stride;
+    static constexpr bool kPrefetch = true;
+    __device__ __forceinline__ void put(int k, C cv, C dv) const {
+        c[k * stride] = cv;
+        d[k * stride] = dv;
+    }
+    __device__ __forceinline__ C getc(int k) const { return c[k * stride]; }
+    __device__ __forceinline__ C getd(int k) const { return d[k * stride]; }
+};
+
+// Thomas solve of the column at offset `col`; oracle
+// stencil_benchmarks/benchmarks_collection/stencils/base.py:410-473 with the
+// exact rewrites documented in vadv.cu.  Inputs of the forward sweep are
+// prefetched D levels ahead in a register ring (slot u holds level kb+u);
+// pos (and factors kept in global memory) likewise in the backward sweep.
+// The new tensstage goes to `out` (may equal tensstage: each level is read
+// before it is written, by the same thread).
+template <class S, class C, int D, class F>
+__device__ __forceinline__ void vadv_column(const S* __restrict__ stage, const S* __restrict__ pos,
+                                            const S* __restrict__ tens, const S* tensstage,
+                                            const S* __restrict__ wcon, S* out, int64_t col, int nk, int64_t sk,
+                                            int64_t wsh, const F& fac) {
+    using A = Ar<C>;
+    const C dtr = (C)(3.0 / 20.0);
+    // ---- forward sweep, k = 0
+    int64_t o = col;
+    C gcv = A::template scale2<-2>(A::add(ld<C, S>(wcon + o + sk + wsh), ld<C, S>(wcon + o + sk)));
+    C cs = A::template scale2<-1>(gcv);  // gcv * bet_m == gcv * bet_p
+    C sprev = ld<C, S>(stage + o);
+    C scur = ld<C, S>(stage + o + sk);
+    C dup = A::sub(scur, sprev);  // stage[k+1] - stage[k]
+    C bcol = A::sub(dtr, cs);
+    C corr = A::mul(-cs, dup);
+    C dv = A::add(A::add(A::add(A::mul(dtr, ld<C, S>(pos + o)), ld<C, S>(tens + o)), ldc<C, S>(tensstage + o)), corr);
+    C cp = A::div(cs, bcol);
+    C dp = A::div(dv, bcol);
+    fac.put(0, cp, dp);
+
+    // ---- forward sweep, 0 < k < nk-1
+    C rw1[D], rw0[D], rst[D], rpo[D], rte[D], rts[D];
+    auto fetch = [&](C& w1, C& w0, C& s1, C& p0, C& t0, C& ts0, int k) {
+        if (k < nk - 1) {
+            const int64_t q = col + (int64_t)k * sk;
+            w1 = ld<C, S>(wcon + q + sk + wsh);
+            w0 = ld<C, S>(wcon + q + sk);
+            s1 = ld<C, S>(stage + q + sk);
+            p0 = ld<C, S>(pos + q);
+            t0 = ld<C, S>(tens + q);
+            ts0 = ldc<C, S>(tensstage + q);
+        }
+    };
+#pragma unroll
+    for (int u = 0; u < D; ++u) fetch(rw1[u], rw0[u], rst[u], rpo[u], rte[u], rts[u], 1 + u);
+    for (int kb = 1; kb < nk - 1; kb += D) {
+#pragma unroll
+        for (int u = 0; u < D; ++u) {
+            const int k = kb + u;
+            if (k >= nk - 1) break;                      // uniform: every thread has the same nk
+            const C as_ = A::template scale2<-1>(-gcv);  // gav * bet_m == acol, gav = -gcv(k-1)
+            gcv = A::template scale2<-2>(A::add(rw1[u], rw0[u]));
+            cs = A::template scale2<-1>(gcv);
+            const C snext = rst[u];
+            const C ddown = A::neg_diff(dup, scur, sprev);  // stage[k-1] - stage[k]
+            dup = A::sub(snext, scur);                     // stage[k+1] - stage[k]
+            bcol = A::sub(A::sub(dtr, as_), cs);
+            corr = A::sub(A::mul(-as_, ddown), A::mul(cs, dup));
+            dv = A::add(A::add(A::add(A::mul(dtr, rpo[u]), rte[u]), rts[u]), corr);
+            fetch(rw1[u], rw0[u], rst[u], rpo[u], rte[u], rts[u], k + D);
+            const C divided = A::rcp(A::sub(bcol, A::mul(cp, as_)));
+            cp = A::mul(cs, divided);
+            dp = A::mul(A::sub(dv, A::mul(dp, as_)), divided);
+            fac.put(k, cp, dp);
+            sprev = scur;
+            scur = snext;
+        }
+    }
+
+    // ---- forward sweep, k = nk-1
+    {
+        const int k = nk - 1;
+        o = col + (int64_t)k * sk;
+        const C as_ = A::template scale2<-1>(-gcv);
+        bcol = A::sub(dtr, as_);
+        const C ddown = A::neg_diff(dup, scur, sprev);
+        corr = A::mul(-as_, ddown);
+        dv = A::add(A::add(A::add(A::mul(dtr, ld<C, S>(pos + o)), ld<C, S>(tens + o)), ldc<C, S>(tensstage + o)), corr);
+        dp = A::div(A::sub(dv, A::mul(dp, as_)), A::sub(bcol, A::mul(cp, as_)));
+    }
+
+    // ---- backward sweep
+    C data = dp;
+    o = col + (int64_t)(nk - 1) * sk;
+    st<S, C>(out + o, A::mul(dtr, A::sub(data, ld<C, S>(pos + o))));
+    C bpo[D], bcc[D], bdd[D];
+    auto fetch_back = [&](C& p0, C& c0, C& d0, int k) {
+        if (k >= 0) {
+            p0 = ld<C, S>(pos + col + (int64_t)k * sk);
+            if (F::kPrefetch) {
+                c0 = fac.getc(k);
+                d0 = fac.getd(k);
+            }
+        }
+    };
+#pragma unroll
+    for (int u = 0; u < D; ++u) fetch_back(bpo[u], bcc[u], bdd[u], nk - 2 - u);
+    for (int kb = nk - 2; kb >= 0; kb -= D) {
+#pragma unroll
+        for (int u = 0; u < D; ++u) {
+            const int k = kb - u;
+            if (k < 0) break;
+            const C cv = F::kPrefetch ? bcc[u] : fac.getc(k);
+            const C dvv = F::kPrefetch ? bdd[u] : fac.getd(k);
+            const C p0 = bpo[u];
+            fetch_back(bpo[u], bcc[u], bdd[u], k - D);
+            data = A::sub(dvv, A::mul(cv, data));
+            st<S, C>(out + col + (int64_t)k * sk, A::mul(dtr, A::sub(data, p0)));
+        }
+    }
+}
+
+// SMEM-async column solve (one thread): inputs staged global -> shared with
+// cp.async into a ring of R = D+1 slots ([R][6][BT] storage elements, this
+// thread's entries at stride BT), factors in sc/sd ([nk][BT], stride BT).
+// Every address below is a per-thread base plus a compile-time offset.
+template <class S, class C, int BT, int D, class IDX>
+__device__ __forceinline__ void vadv_async_column(const S* __restrict__ stage, const S* __restrict__ pos,
+                                                  const S* __restrict__ tens, const S* tensstage,
+                                                  const S* __restrict__ wcon, S* out, IDX col, int nk, IDX sk,
+                                                  IDX wsh, C* sc, C* sd, S* ring) {
+    using A = Ar<C>;
+    constexpr int R = D + 1;
+    const C dtr = (C)(3.0 / 20.0);
+
+    auto issue = [&](int slot, int k) {
+        if (k < nk - 1) {
+            const IDX q = col + (IDX)k * sk;
+            S* d = ring + slot * 6 * BT;
+            cp_async<sizeof(S)>(d, wcon + q + sk + wsh);
+            cp_async<sizeof(S)>(d + BT, wcon + q + sk);
+            cp_async<sizeof(S)>(d + 2 * BT, stage + q + sk);
+            cp_async<sizeof(S)>(d + 3 * BT, pos + q);
+            cp_async<sizeof(S)>(d + 4 * BT, tens + q);
+            cp_async<sizeof(S)>(d + 5 * BT, tensstage + q);
+        }
+        cp_async_commit();
+    };
+    // level L is staged in slot (L-1) % R
+#pragma unroll
+    for (int u = 0; u < D; ++u) issue(u, 1 + u);
+
+    // ---- forward sweep, k = 0 (direct loads)
+    C gcv = A::template scale2<-2>(A::add(ld<C, S>(wcon + col + sk + wsh), ld<C, S>(wcon + col + sk)));
+    C cs = A::template scale2<-1>(gcv);
+    C sprev = ld<C, S>(stage + col);
+    C scur = ld<C, S>(stage + col + sk);
+    C dup = A::sub(scur, sprev);
+    C bcol = A::sub(dtr, cs);
+    C corr = A::mul(-cs, dup);
+    C dv = A::add(A::add(A::add(A::mul(dtr, ld<C, S>(pos + col)), ld<C, S>(tens + col)), ldc<C, S>(tensstage + col)), corr);
+    C cp = A::div(cs, bcol);
+    C dp = A::div(dv, bcol);
+    sc[0] = cp;
+    sd[0] = dp;
+
+    // ---- forward sweep, 0 < k < nk-1
+    for (int kb = 1; kb < nk - 1; kb += R) {
+#pragma unroll
+        for (int u = 0; u < R; ++u) {
+            const int k = kb + u;
+            if (k >= nk - 1) break;  // uniform
+            cp_async_wait<D - 1>();
+            const S* sl = ring + u * 6 * BT;
+            const C w1 = cvt<C, S>(sl[0]), w0 = cvt<C, S>(sl[BT]), snext = cvt<C, S>(sl[2 * BT]);
+            const C p0 = cvt<C, S>(sl[3 * BT]), t0 = cvt<C, S>(sl[4 * BT]), ts0 = cvt<C, S>(sl[5 * BT]);
+            issue((u + D) % R, k + D);  // the slot of level k-1, already consumed
+            const C as_ = A::template scale2<-1>(-gcv);
+            gcv = A::template scale2<-2>(A::add(w1, w0));
+            cs = A::template scale2<-1>(gcv);
+            const C ddown = A::neg_diff(dup, scur, sprev);
+            dup = A::sub(snext, scur);
+            bcol = A::sub(A::sub(dtr, as_), cs);
+            corr = A::sub(A::mul(-as_, ddown), A::mul(cs, dup));
+            dv = A::add(A::add(A::add(A::mul(dtr, p0), t0), ts0), corr);
+            const C divided = A::rcp(A::sub(bcol, A::mul(cp, as_)));
+            cp = A::mul(cs, divided);
+            dp = A::mul(A::sub(dv, A::mul(dp, as_)), divided);
+            sc[k * BT] = cp;
+            sd[k * BT] = dp;
+            sprev = scur;
+            scur = snext;
+        }
+    }
+    cp_async_wait<0>();
+
+    // ---- forward sweep, k = nk-1
+    {
+        const IDX o = col + (IDX)(nk - 1) * sk;
+        const C as_ = A::template scale2<-1>(-gcv);
+        bcol = A::sub(dtr, as_);
+        const C ddown = A::neg_diff(dup, scur, sprev);
+        corr = A::mul(-as_, ddown);
+        dv = A::add(A::add(A::add(A::mul(dtr, ld<C, S>(pos + o)), ld<C, S>(tens + o)), ldc<C, S>(tensstage + o)), corr);
+        dp = A::div(A::sub(dv, A::mul(dp, as_)), A::sub(bcol, A::mul(cp, as_)));
+    }
+
+    // ---- backward sweep; pos of level L staged in slot (nk-2-L) % R, field 3
+    auto issue_b = [&](int slot, int k) {
+        if (k >= 0) cp_async<sizeof(S)>(ring + slot * 6 * BT + 3 * BT, pos + (col + (IDX)k * sk));
+        cp_async_commit();
+    };
+#pragma unroll
+    for (int u = 0; u < D; ++u) issue_b(u, nk - 2 - u);
+    C data = dp;
+    {
+        const IDX o = col + (IDX)(nk - 1) * sk;
+        st<S, C>(out + o, A::mul(dtr, A::sub(data, ld<C, S>(pos + o))));
+    }
+    for (int kb = nk - 2; kb >= 0; kb -= R) {
+#pragma unroll
+        for (int u = 0; u < R; ++u) {
+            const int k = kb - u;
+            if (k < 0) break;
+            cp_async_wait<D - 1>();
+            const C p0 = cvt<C, S>(ring[u * 6 * BT + 3 * BT]);
+            issue_b((u + D) % R, k - D);
+            data = A::sub(sd[k * BT], A::mul(sc[k * BT], data));
+            st<S, C>(out + (col + (IDX)k * sk), A::mul(dtr, A::sub(data, p0)));
+        }
+    }
+    cp_async_wait<0>();
+}
+
+}  // namespace sb

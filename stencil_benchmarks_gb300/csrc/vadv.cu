@@ -28,7 +28,7 @@
 //   GLOBAL : the caller's ccol/dcol fields (the reference's arguments of the
 //            same names), for columns too tall for shared memory.
 // The backward sweep reads them back in reverse order.
-#include "common.cuh"
+#include "stencil_core.cuh"
 
 namespace sb {
 namespace {
@@ -39,129 +39,20 @@ __global__ void __launch_bounds__(256)
                 const S* tensstage, const S* __restrict__ wcon, S* out, C* __restrict__ gccol,
                 C* __restrict__ gdcol, int ni, int nj, int nk, int64_t si, int64_t sj, int64_t sk,
                 int64_t wsh) {
-    using A = Ar<C>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int nthr = blockDim.x * blockDim.y;
     const int t = threadIdx.y * blockDim.x + threadIdx.x;
-    C* sc = reinterpret_cast<C*>(smem_raw);
-    C* sd = sc + (size_t)nk * nthr;
-
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     if (i >= ni || j >= nj) return;  // no block-wide barrier below
-
-    const C dtr = (C)(3.0 / 20.0);
     const int64_t col = (int64_t)i * si + (int64_t)j * sj;
-
-    auto put = [&](int k, C cv, C dv) {
-        if (GLOBAL) {
-            gccol[col + (int64_t)k * sk] = cv;
-            gdcol[col + (int64_t)k * sk] = dv;
-        } else {
-            sc[(size_t)k * nthr + t] = cv;
-            sd[(size_t)k * nthr + t] = dv;
-        }
-    };
-
-    // ---- forward sweep, k = 0
-    int64_t o = col;
-    C gcv = A::template scale2<-2>(A::add(ld<C, S>(wcon + o + sk + wsh), ld<C, S>(wcon + o + sk)));
-    C cs = A::template scale2<-1>(gcv);  // gcv * bet_m == gcv * bet_p
-    C sprev = ld<C, S>(stage + o);
-    C scur = ld<C, S>(stage + o + sk);
-    C dup = A::sub(scur, sprev);  // stage[k+1] - stage[k]
-    C bcol = A::sub(dtr, cs);
-    C corr = A::mul(-cs, dup);
-    C dv = A::add(A::add(A::add(A::mul(dtr, ld<C, S>(pos + o)), ld<C, S>(tens + o)), ldc<C, S>(tensstage + o)), corr);
-    C cp = A::div(cs, bcol);
-    C dp = A::div(dv, bcol);
-    put(0, cp, dp);
-
-    // ---- forward sweep, 0 < k < nk-1, with a D-deep register prefetch ring:
-    // slot u holds the inputs of level k (wcon at k+1 in both columns,
-    // stage at k+1, pos/tens/tensstage at k); after level k is consumed the
-    // slot is refilled with level k+D, so D levels of loads stay in flight
-    // while the serial recurrence runs.
-    C rw1[D], rw0[D], rst[D], rpo[D], rte[D], rts[D];
-    auto fetch = [&](C& w1, C& w0, C& s1, C& p0, C& t0, C& ts0, int k) {
-        if (k < nk - 1) {
-            const int64_t q = col + (int64_t)k * sk;
-            w1 = ld<C, S>(wcon + q + sk + wsh);
-            w0 = ld<C, S>(wcon + q + sk);
-            s1 = ld<C, S>(stage + q + sk);
-            p0 = ld<C, S>(pos + q);
-            t0 = ld<C, S>(tens + q);
-            ts0 = ldc<C, S>(tensstage + q);
-        }
-    };
-#pragma unroll
-    for (int u = 0; u < D; ++u) fetch(rw1[u], rw0[u], rst[u], rpo[u], rte[u], rts[u], 1 + u);
-
-    for (int kb = 1; kb < nk - 1; kb += D) {
-#pragma unroll
-        for (int u = 0; u < D; ++u) {
-            const int k = kb + u;
-            if (k >= nk - 1) break;  // uniform: every thread has the same nk
-            const C as_ = A::template scale2<-1>(-gcv);  // gav * bet_m == acol, gav = -gcv(k-1)
-            gcv = A::template scale2<-2>(A::add(rw1[u], rw0[u]));
-            cs = A::template scale2<-1>(gcv);
-            const C snext = rst[u];
-            const C ddown = A::neg_diff(dup, scur, sprev);  // stage[k-1] - stage[k]
-            dup = A::sub(snext, scur);                     // stage[k+1] - stage[k]
-            bcol = A::sub(A::sub(dtr, as_), cs);
-            corr = A::sub(A::mul(-as_, ddown), A::mul(cs, dup));
-            dv = A::add(A::add(A::add(A::mul(dtr, rpo[u]), rte[u]), rts[u]), corr);
-            fetch(rw1[u], rw0[u], rst[u], rpo[u], rte[u], rts[u], k + D);
-            const C divided = A::rcp(A::sub(bcol, A::mul(cp, as_)));
-            cp = A::mul(cs, divided);
-            dp = A::mul(A::sub(dv, A::mul(dp, as_)), divided);
-            put(k, cp, dp);
-            sprev = scur;
-            scur = snext;
-        }
-    }
-
-    // ---- forward sweep, k = nk-1
-    {
-        const int k = nk - 1;
-        o = col + (int64_t)k * sk;
-        const C as_ = A::template scale2<-1>(-gcv);
-        bcol = A::sub(dtr, as_);
-        const C ddown = A::neg_diff(dup, scur, sprev);
-        corr = A::mul(-as_, ddown);
-        dv = A::add(A::add(A::add(A::mul(dtr, ld<C, S>(pos + o)), ld<C, S>(tens + o)), ldc<C, S>(tensstage + o)), corr);
-        dp = A::div(A::sub(dv, A::mul(dp, as_)), A::sub(bcol, A::mul(cp, as_)));
-    }
-
-    // ---- backward sweep; pos (and, for GLOBAL, ccol/dcol) prefetched D levels ahead
-    C data = dp;
-    o = col + (int64_t)(nk - 1) * sk;
-    st<S, C>(out + o, A::mul(dtr, A::sub(data, ld<C, S>(pos + o))));
-    C bpo[D], bcc[D], bdd[D];
-    auto fetch_back = [&](C& p0, C& c0, C& d0, int k) {
-        if (k >= 0) {
-            const int64_t q = col + (int64_t)k * sk;
-            p0 = ld<C, S>(pos + q);
-            if (GLOBAL) {
-                c0 = gccol[q];
-                d0 = gdcol[q];
-            }
-        }
-    };
-#pragma unroll
-    for (int u = 0; u < D; ++u) fetch_back(bpo[u], bcc[u], bdd[u], nk - 2 - u);
-    for (int kb = nk - 2; kb >= 0; kb -= D) {
-#pragma unroll
-        for (int u = 0; u < D; ++u) {
-            const int k = kb - u;
-            if (k < 0) break;
-            const C cv = GLOBAL ? bcc[u] : sc[(size_t)k * nthr + t];
-            const C dvv = GLOBAL ? bdd[u] : sd[(size_t)k * nthr + t];
-            const C p0 = bpo[u];
-            fetch_back(bpo[u], bcc[u], bdd[u], k - D);
-            data = A::sub(dvv, A::mul(cv, data));
-            st<S, C>(out + col + (int64_t)k * sk, A::mul(dtr, A::sub(data, p0)));
-        }
+    if (GLOBAL) {
+        const GlobalFactors<C> fac{gccol + col, gdcol + col, sk};
+        vadv_column<S, C, D>(stage, pos, tens, tensstage, wcon, out, col, nk, sk, wsh, fac);
+    } else {
+        C* sc = reinterpret_cast<C*>(smem_raw);
+        const SmemFactors<C> fac{sc + t, sc + (size_t)nk * nthr + t, nthr};
+        vadv_column<S, C, D>(stage, pos, tens, tensstage, wcon, out, col, nk, sk, wsh, fac);
     }
 }
 
@@ -179,117 +70,15 @@ __global__ void __launch_bounds__(BT)
     vadv_async_kernel(const S* __restrict__ stage, const S* __restrict__ pos, const S* __restrict__ tens,
                       const S* tensstage, const S* __restrict__ wcon, S* out, int ni, int nj, int nk,
                       int si, int sj, int sk, int wsh, int ring_offset) {
-    using A = Ar<C>;
-    constexpr int R = D + 1;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int t = threadIdx.x;
     C* sc = reinterpret_cast<C*>(smem_raw) + t;
-    C* sd = sc + nk * BT;
     S* ring = reinterpret_cast<S*>(smem_raw + ring_offset) + t;
-
     const int i = blockIdx.x * BT + t;
     const int j = blockIdx.y;
     if (i >= ni) return;  // no block-wide barrier below
-    const C dtr = (C)(3.0 / 20.0);
-    const int col = i * si + j * sj;
-
-    auto issue = [&](int slot, int k) {
-        if (k < nk - 1) {
-            const int q = col + k * sk;
-            S* d = ring + slot * 6 * BT;
-            cp_async<sizeof(S)>(d, wcon + q + sk + wsh);
-            cp_async<sizeof(S)>(d + BT, wcon + q + sk);
-            cp_async<sizeof(S)>(d + 2 * BT, stage + q + sk);
-            cp_async<sizeof(S)>(d + 3 * BT, pos + q);
-            cp_async<sizeof(S)>(d + 4 * BT, tens + q);
-            cp_async<sizeof(S)>(d + 5 * BT, tensstage + q);
-        }
-        cp_async_commit();
-    };
-    // level L is staged in slot (L-1) % R
-#pragma unroll
-    for (int u = 0; u < D; ++u) issue(u, 1 + u);
-
-    // ---- forward sweep, k = 0 (direct loads)
-    C gcv = A::template scale2<-2>(A::add(ld<C, S>(wcon + col + sk + wsh), ld<C, S>(wcon + col + sk)));
-    C cs = A::template scale2<-1>(gcv);
-    C sprev = ld<C, S>(stage + col);
-    C scur = ld<C, S>(stage + col + sk);
-    C dup = A::sub(scur, sprev);
-    C bcol = A::sub(dtr, cs);
-    C corr = A::mul(-cs, dup);
-    C dv = A::add(A::add(A::add(A::mul(dtr, ld<C, S>(pos + col)), ld<C, S>(tens + col)), ldc<C, S>(tensstage + col)), corr);
-    C cp = A::div(cs, bcol);
-    C dp = A::div(dv, bcol);
-    sc[0] = cp;
-    sd[0] = dp;
-
-    // ---- forward sweep, 0 < k < nk-1
-    for (int kb = 1; kb < nk - 1; kb += R) {
-#pragma unroll
-        for (int u = 0; u < R; ++u) {
-            const int k = kb + u;
-            if (k >= nk - 1) break;  // uniform
-            cp_async_wait<D - 1>();
-            const S* sl = ring + u * 6 * BT;
-            const C w1 = cvt<C, S>(sl[0]), w0 = cvt<C, S>(sl[BT]), snext = cvt<C, S>(sl[2 * BT]);
-            const C p0 = cvt<C, S>(sl[3 * BT]), t0 = cvt<C, S>(sl[4 * BT]), ts0 = cvt<C, S>(sl[5 * BT]);
-            issue((u + D) % R, k + D);  // the slot of level k-1, already consumed
-            const C as_ = A::template scale2<-1>(-gcv);
-            gcv = A::template scale2<-2>(A::add(w1, w0));
-            cs = A::template scale2<-1>(gcv);
-            const C ddown = A::neg_diff(dup, scur, sprev);
-            dup = A::sub(snext, scur);
-            bcol = A::sub(A::sub(dtr, as_), cs);
-            corr = A::sub(A::mul(-as_, ddown), A::mul(cs, dup));
-            dv = A::add(A::add(A::add(A::mul(dtr, p0), t0), ts0), corr);
-            const C divided = A::rcp(A::sub(bcol, A::mul(cp, as_)));
-            cp = A::mul(cs, divided);
-            dp = A::mul(A::sub(dv, A::mul(dp, as_)), divided);
-            sc[k * BT] = cp;
-            sd[k * BT] = dp;
-            sprev = scur;
-            scur = snext;
-        }
-    }
-    cp_async_wait<0>();
-
-    // ---- forward sweep, k = nk-1
-    {
-        const int o = col + (nk - 1) * sk;
-        const C as_ = A::template scale2<-1>(-gcv);
-        bcol = A::sub(dtr, as_);
-        const C ddown = A::neg_diff(dup, scur, sprev);
-        corr = A::mul(-as_, ddown);
-        dv = A::add(A::add(A::add(A::mul(dtr, ld<C, S>(pos + o)), ld<C, S>(tens + o)), ldc<C, S>(tensstage + o)), corr);
-        dp = A::div(A::sub(dv, A::mul(dp, as_)), A::sub(bcol, A::mul(cp, as_)));
-    }
-
-    // ---- backward sweep; pos of level L staged in slot (nk-2-L) % R, field 3
-    auto issue_b = [&](int slot, int k) {
-        if (k >= 0) cp_async<sizeof(S)>(ring + slot * 6 * BT + 3 * BT, pos + col + k * sk);
-        cp_async_commit();
-    };
-#pragma unroll
-    for (int u = 0; u < D; ++u) issue_b(u, nk - 2 - u);
-    C data = dp;
-    {
-        const int o = col + (nk - 1) * sk;
-        st<S, C>(out + o, A::mul(dtr, A::sub(data, ld<C, S>(pos + o))));
-    }
-    for (int kb = nk - 2; kb >= 0; kb -= R) {
-#pragma unroll
-        for (int u = 0; u < R; ++u) {
-            const int k = kb - u;
-            if (k < 0) break;
-            cp_async_wait<D - 1>();
-            const C p0 = cvt<C, S>(ring[u * 6 * BT + 3 * BT]);
-            issue_b((u + D) % R, k - D);
-            data = A::sub(sd[k * BT], A::mul(sc[k * BT], data));
-            st<S, C>(out + col + k * sk, A::mul(dtr, A::sub(data, p0)));
-        }
-    }
-    cp_async_wait<0>();
+    vadv_async_column<S, C, BT, D, int>(stage, pos, tens, tensstage, wcon, out, i * si + j * sj, nk, sk, wsh, sc,
+                                        sc + nk * BT, ring);
 }
 
 template <class S, class C, bool GLOBAL, int D>
