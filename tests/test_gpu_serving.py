@@ -1,0 +1,87 @@
+"""The server on the GPU: generated inputs are reproducible, every served
+result equals the oracle, and a request gives the same bits alone and in a
+mix of concurrent requests of other sizes and precisions."""
+
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+import pytest
+
+from stencil_benchmarks_gb300 import _native, serving
+from stencil_benchmarks_gb300.array import storage_numpy_dtype
+from stencil_benchmarks_gb300.device import DeviceBuffer, Stream
+from tests.gpu_helpers import bits_equal, mismatch_report
+from tests.serving_helpers import download_output, expected_output, fill_values
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("storage", ["float64", "float32", "bfloat16"])
+def test_device_fill_matches_host_reproduction(storage, lib):
+    count = 100_003
+    buf = DeviceBuffer(count * 8)
+    scratch = DeviceBuffer(1024)
+    desc = serving.SbFillDesc(buf.ptr, count, 0x1234567890ABCDEF, -0.5, 0.5, _native.storage_code(storage), 0)
+    stream = Stream()
+    serving._fill([desc], scratch, stream)
+    stream.synchronize()
+    host = np.empty(count, dtype=storage_numpy_dtype(storage))
+    from stencil_benchmarks_gb300.device import copy_to_host
+
+    copy_to_host(host, buf.ptr)
+    want = fill_values(0x1234567890ABCDEF, count, -0.5, 0.5, storage)
+    assert bits_equal(host, want), mismatch_report(host, want)
+
+
+def _small_mix(n, seed):
+    rng = np.random.Generator(np.random.PCG64(seed))
+    forms = ["float64", "float32", "bfloat16"]
+    return [serving.Request(rid, ("hdiff", "vadv")[int(rng.integers(0, 2))], int(rng.integers(20, 97)),
+                            int(rng.integers(20, 97)), int(rng.integers(2, 41)), forms[int(rng.integers(0, 3))],
+                            int(rng.integers(0, 2**62)))
+            for rid in range(n)]
+
+
+def test_served_results_match_the_oracle(lib):
+    server = serving.Server(budget_bytes=8e9, max_batch=8, max_nk=48, slots_per_form=2, keep_outputs=True)
+    reqs = _small_mix(18, 7)
+    for r in reqs:
+        server.submit(r)
+    server.drain()
+    for r in reqs:
+        got, want = download_output(r), expected_output(r)
+        assert bits_equal(got, want), f"request {r}: " + mismatch_report(got, want)
+        server.release(r)
+
+
+def test_same_result_alone_and_in_a_mix(lib):
+    probe = serving.Request(0, "vadv", 77, 45, 33, "float32", 987654321)
+    alone_srv = serving.Server(budget_bytes=4e9, max_batch=4, max_nk=48, slots_per_form=1, keep_outputs=True)
+    alone_srv.submit(probe)
+    alone_srv.drain()
+    alone = download_output(probe).copy()
+
+    twin = serving.Request(1000, "vadv", 77, 45, 33, "float32", 987654321)
+    others = _small_mix(40, 8)
+    mixed = others[:20] + [twin] + others[20:]
+    srv = serving.Server(budget_bytes=8e9, max_batch=6, max_nk=48, slots_per_form=3, keep_outputs=True)
+    for r in mixed:
+        srv.submit(r)
+        srv.step()  # arrivals interleave with execution
+    srv.drain()
+    in_mix = download_output(twin)
+    assert bits_equal(alone, in_mix), mismatch_report(alone, in_mix)
+    assert bits_equal(in_mix, expected_output(twin))
+
+
+def test_budget_bounded_load(lib):
+    reqs = _small_mix(60, 9)
+    biggest = max(r.footprint() for r in reqs)
+    srv = serving.Server(budget_bytes=2 * biggest, max_batch=4, max_nk=48, slots_per_form=2)
+    stats = serving.run_load(srv, reqs, rate=5000.0)
+    assert stats["requests"] == 60 and all(r.completed for r in reqs)
+    assert srv.pool.peak <= srv.pool.budget
+    assert stats["p99_ms"] >= stats["p50_ms"] > 0
+    assert srv.pool.in_use == 0
