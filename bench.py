@@ -391,6 +391,23 @@ def run_batched(seed=3, n_domains=64, storage="float32", reps=5):
     }
 
 
+def run_served(n_requests=2000, rates=(1000.0, 5000.0, 20000.0), seed=11):
+    """Continuous-batching server under Poisson arrivals (mixed hdiff/vadv,
+    sizes log-uniform 32..1024, nk 40..137, fp64/fp32/bf16 at 20/60/20 %,
+    150 GB budget).  The full 10,000-request sweep is
+    ``python -m stencil_benchmarks_gb300.serving``."""
+    from stencil_benchmarks_gb300 import serving
+
+    server = serving.Server(budget_bytes=150e9, max_batch=64, slots_per_form=3)
+    serving.run_load(server, serving.request_specs(64, seed=seed + 1000), rate=1e6)  # warm-up
+    out = []
+    for rate in rates:
+        stats = serving.run_load(server, serving.request_specs(n_requests, seed=seed), rate=rate)
+        out.append({k: stats[k] for k in ("rate_offered", "requests", "p50_ms", "p99_ms", "throughput_req_s",
+                                          "gpoints_s", "peak_pool_gb")})
+    return out
+
+
 def cpu_baseline_sample(threads=None):
     """Time the C restatement on the full 512x512x80 hdiff+vadv fp64 step."""
     from oracle import cport
@@ -460,6 +477,7 @@ def main(argv=None):
     ap.add_argument("--no-cpu-baseline", action="store_true", help="skip the timed CPU baseline")
     ap.add_argument("--no-triad", action="store_true", help="skip the STREAM triad calibration")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-domains comparison")
+    ap.add_argument("--no-served", action="store_true", help="skip the serving-loop measurement")
     args = ap.parse_args(argv)
     if args.warmup < 3:
         print("warning: fewer than 3 warm-up steps", file=sys.stderr)
@@ -510,6 +528,8 @@ def main(argv=None):
             line["stream_triad"]["frac_of_" + peak_kind] = res["triad"]["gbs"] / peak
         if not args.no_batched:
             line["batched"] = run_batched()
+        if not args.no_served:
+            line["served"] = run_served()
         if not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline_sample()
         print(json.dumps(line), flush=True)

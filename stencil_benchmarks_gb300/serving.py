@@ -362,3 +362,37 @@ def run_load(server: Server, requests: List[Request], rate: float, seed: int = 5
         "peak_pool_gb": server.pool.peak / 1e9,
         "max_waiting": server.max_waiting,
     }
+
+
+def main(argv=None):
+    """Sweep Poisson arrival rates over the serving workload; one JSON line per rate."""
+    import argparse
+    import json
+
+    ap = argparse.ArgumentParser(description="continuous-batching serving sweep")
+    ap.add_argument("--requests", type=int, default=10000)
+    ap.add_argument("--rates", default="1000,2000,5000,10000,20000,50000")
+    ap.add_argument("--budget-gb", type=float, default=150.0)
+    ap.add_argument("--max-batch", type=int, default=64)
+    ap.add_argument("--slots", type=int, default=3)
+    ap.add_argument("--seed", type=int, default=11)
+    args = ap.parse_args(argv)
+    server = Server(budget_bytes=args.budget_gb * 1e9, max_batch=args.max_batch, slots_per_form=args.slots)
+    warm = request_specs(64, seed=args.seed + 1000)
+    run_load(server, warm, rate=1e6)
+    for rate in (float(r) for r in args.rates.split(",")):
+        reqs = request_specs(args.requests, seed=args.seed)
+        stats = run_load(server, reqs, rate=rate)
+        by_form = {}
+        for form in FORMS:
+            lat = [r.latency for r in reqs if r.storage == form]
+            if lat:
+                by_form[form] = {"n": len(lat), "p50_ms": float(np.percentile(lat, 50) * 1e3),
+                                 "p99_ms": float(np.percentile(lat, 99) * 1e3)}
+        stats["by_precision"] = by_form
+        print(json.dumps(stats), flush=True)
+    return 0
+
+
+if __name__ == "__main__":
+    raise SystemExit(main())
