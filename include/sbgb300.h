@@ -202,12 +202,20 @@ int sb_batch_destroy(sb_batch* batch);
 /* ---- serving support --------------------------------------------------------
  * No counterpart in the reference (it runs one benchmark at a time).
  * sb_fill_batch: fill n device fields in one launch with seeded uniform values
- * (element e of a field: u = (splitmix64(seed + (e+1)*0x9E3779B97F4A7C15) >> 11)
- * * 2^-53, value lo + (hi-lo)*u in double, rounded once to float32 storage, or
- * to float32 then bfloat16).  The descriptors are copied (asynchronously on
+ * in [lo, hi), generated without fp64 arithmetic on the device.  With H the
+ * 32-bit lowbias32 hash, k0/k1 the low/high words of seed and e the element:
+ *   h1 = H(H(lo32(e) ^ k0) ^ (k1 ^ hi32(e) * 0x9E3779B9))
+ *   float32 / bfloat16:  v = lo_f + span_f * ((h1 >> 8) * 2^-24)  in float32
+ *                        (lo_f = (float)lo, span_f = (float)(hi - lo)), then
+ *                        rounded to bfloat16 for bfloat16 storage;
+ *   float64:  h2 = H(h1 ^ (k0 + 0x632BE5AB)), k = h1 << 21 | h2 >> 11,
+ *             v = lo + (hi - lo) * (k * 2^-53)  in double;
+ * each operation rounded to nearest even, no fused multiply-add.  The
+ * descriptors are copied (asynchronously on
  * `stream`, from the caller's host memory, which must stay valid until the
  * stream reaches the copy) into `desc_scratch`, a device buffer of at least n
- * descriptors owned by the caller.
+ * descriptors owned by the caller.  From page-locked host memory the copy is
+ * queued; from pageable memory CUDA first waits for `stream` to drain.
  * sb_event_query: SB_OK if the event has completed, SB_NOT_READY if not.      */
 #define SB_NOT_READY 7
 typedef struct sb_fill_desc {
@@ -221,6 +229,19 @@ typedef struct sb_fill_desc {
 int sb_fill_batch(const sb_fill_desc* descs, int n, void* desc_scratch, void* stream);
 int sb_event_query(void* event);
 int sb_stream_wait_event(void* stream, void* event); /* later work on stream waits for event */
+
+/* ---- device-memory arena (serving) -------------------------------------------
+ * Best-fit allocator with coalescing over a caller-provided address range
+ * [base, base + bytes) (normally one cudaMalloc); pure host bookkeeping, no
+ * CUDA call, thread-safe.  sb_arena_alloc returns SB_ERR_BUDGET when no free
+ * block is large enough.                                                     */
+typedef struct sb_arena sb_arena;
+int sb_arena_create(sb_arena** arena, uint64_t base, uint64_t bytes, uint64_t align);
+int sb_arena_alloc(sb_arena* arena, uint64_t bytes, uint64_t* address);
+int sb_arena_free(sb_arena* arena, uint64_t address);
+int sb_arena_stats(sb_arena* arena, uint64_t* in_use, uint64_t* peak, uint64_t* largest_free,
+                   uint64_t* free_blocks);
+int sb_arena_destroy(sb_arena* arena);
 
 /* ---- vertical advection without device allocation -------------------------
  * No counterpart in the reference.  For callers that cannot call cudaMalloc:

@@ -126,6 +126,11 @@ SIGNATURES = {
     "sb_fill_batch": [_vp, _int, _vp, _vp],
     "sb_event_query": [_vp],
     "sb_stream_wait_event": [_vp, _vp],
+    "sb_arena_create": [ctypes.POINTER(_vp), ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64],
+    "sb_arena_alloc": [_vp, ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint64)],
+    "sb_arena_free": [_vp, ctypes.c_uint64],
+    "sb_arena_stats": [_vp] + [ctypes.POINTER(ctypes.c_uint64)] * 4,
+    "sb_arena_destroy": [_vp],
     "sb_probe_arith_rate": [_int, _dp],
 }
 _RESTYPES = {"sb_last_error": ctypes.c_char_p}

@@ -34,6 +34,7 @@ import collections
 import ctypes
 import math
 import time
+import weakref
 from dataclasses import dataclass, field
 from typing import Dict, List, Optional
 
@@ -41,9 +42,10 @@ import numpy as np
 
 from . import _native
 from .batching import Batch, HdiffDomain, VadvDomain
-from .device import DeviceBuffer, Event, Field, Stream
+from .device import DeviceBuffer, Event, Field, PinnedBuffer, Stream
 
-GRANULE = 2 << 20  # pool size classes: multiples of 2 MiB
+ALIGN = 256  # field allocations start on 256-byte boundaries
+FILL_DEPTH = 8  # page-locked staging slots for fill descriptors
 
 FORMS = {"float64": ("float64", "float64"), "float32": ("float32", "float32"), "bfloat16": ("bfloat16", "float32")}
 ITEMSIZE = {"float64": 8, "float32": 4, "bfloat16": 2}
@@ -98,7 +100,7 @@ class Request:
     def footprint(self) -> int:
         shape, _, _ = field_layout(self.op, self.ni, self.nj, self.nk)
         n = len(HDIFF_FIELDS if self.op == "hdiff" else VADV_FIELDS)
-        return n * _round(int(np.prod(shape)) * ITEMSIZE[self.storage])
+        return n * _round(math.prod(shape) * ITEMSIZE[self.storage])
 
     def domain(self):
         f = self.fields
@@ -108,54 +110,63 @@ class Request:
 
 
 def _round(nbytes: int) -> int:
-    return max(GRANULE, -(-nbytes // GRANULE) * GRANULE)
+    return max(ALIGN, -(-nbytes // ALIGN) * ALIGN)
+
+
+@dataclass
+class Block:
+    """A piece of the pool's device region (what a Field needs of a buffer)."""
+
+    ptr: int
+    nbytes: int
 
 
 class DevicePool:
-    """Budget-capped caching allocator: buffers are kept per 2 MiB size class
-    after release and reused; cached buffers are freed when a new size would
-    exceed the budget."""
+    """Budget-capped device memory: the whole budget is allocated once and
+    carved by the library's best-fit arena (``sb_arena_*``), so admitting and
+    retiring requests makes no CUDA allocation call (cudaMalloc / cudaFree
+    synchronise the device and would stall every batch in flight)."""
 
     def __init__(self, budget_bytes: int):
-        self.budget = int(budget_bytes)
-        self.in_use = 0
-        self.cached = 0
-        self.peak = 0
-        self._free: Dict[int, List[DeviceBuffer]] = collections.defaultdict(list)
+        self.budget = int(budget_bytes) // ALIGN * ALIGN
+        self.region = DeviceBuffer(self.budget)
+        self._lib = _native.lib()
+        handle = ctypes.c_void_p()
+        self._check("sb_arena_create", self._lib.sb_arena_create(ctypes.byref(handle), self.region.ptr,
+                                                                 self.budget, ALIGN))
+        self._arena = handle.value
+        self._finalizer = weakref.finalize(self, self._lib.sb_arena_destroy, ctypes.c_void_p(self._arena))
 
-    def try_alloc(self, nbytes: int) -> Optional[DeviceBuffer]:
-        size = _round(nbytes)
-        if self._free[size]:
-            buf = self._free[size].pop()
-            self.cached -= size
-        else:
-            if self.in_use + size > self.budget:
-                return None
-            self._evict(self.in_use + self.cached + size - self.budget)
-            try:
-                buf = DeviceBuffer(size)
-            except _native.SbError:
-                self._evict(self.cached)
-                try:
-                    buf = DeviceBuffer(size)
-                except _native.SbError:
-                    return None
-        self.in_use += size
-        self.peak = max(self.peak, self.in_use)
-        return buf
+    @staticmethod
+    def _check(name, rc):
+        if rc != _native.SB_OK:
+            raise _native.SbError(name, rc, _native.last_error())
 
-    def release(self, buf: DeviceBuffer):
-        size = buf.nbytes
-        self.in_use -= size
-        self.cached += size
-        self._free[size].append(buf)
+    def try_alloc(self, nbytes: int) -> Optional[Block]:
+        """A block of at least ``nbytes`` bytes, or None when no free piece is large enough."""
+        addr = ctypes.c_uint64()
+        rc = self._lib.sb_arena_alloc(ctypes.c_void_p(self._arena), max(1, int(nbytes)), ctypes.byref(addr))
+        if rc == _native.SB_ERR_BUDGET:
+            return None
+        self._check("sb_arena_alloc", rc)
+        return Block(addr.value, _round(nbytes))
 
-    def _evict(self, need: int):
-        for size in sorted(self._free, reverse=True):
-            while need > 0 and self._free[size]:
-                self._free[size].pop().free()
-                self.cached -= size
-                need -= size
+    def release(self, block: Block):
+        self._check("sb_arena_free", self._lib.sb_arena_free(ctypes.c_void_p(self._arena), block.ptr))
+
+    def stats(self) -> Dict[str, int]:
+        vals = [ctypes.c_uint64() for _ in range(4)]
+        self._check("sb_arena_stats", self._lib.sb_arena_stats(ctypes.c_void_p(self._arena),
+                                                               *[ctypes.byref(v) for v in vals]))
+        return dict(zip(("in_use", "peak", "largest_free", "free_blocks"), (v.value for v in vals)))
+
+    @property
+    def in_use(self) -> int:
+        return self.stats()["in_use"]
+
+    @property
+    def peak(self) -> int:
+        return self.stats()["peak"]
 
 
 def _event_done(event: Event) -> bool:
@@ -167,10 +178,17 @@ def _event_done(event: Event) -> bool:
     return True
 
 
-def _fill(descs, scratch: DeviceBuffer, stream: Stream):
+def _fill(descs, scratch: DeviceBuffer, stream: Stream, staging: Optional[int] = None):
+    """Generate the fields ``descs`` describe on ``stream``.  With ``staging``
+    (page-locked host memory for ``len(descs)`` descriptors, left untouched
+    until the stream has run the fill) the descriptor copy is queued; from
+    pageable memory it first waits for ``stream`` to drain."""
     arr = (SbFillDesc * len(descs))(*descs)
-    _native.call("sb_fill_batch", ctypes.cast(arr, ctypes.c_void_p), len(descs), ctypes.c_void_p(scratch.ptr),
-                 stream.as_parameter)
+    src = ctypes.addressof(arr)
+    if staging is not None:
+        ctypes.memmove(staging, src, ctypes.sizeof(arr))
+        src = staging
+    _native.call("sb_fill_batch", ctypes.c_void_p(src), len(descs), ctypes.c_void_p(scratch.ptr), stream.as_parameter)
 
 
 def _wait(stream: Stream, event: Event):
@@ -202,11 +220,17 @@ class Server:
         self.waiting: collections.deque = collections.deque()
         self.ready = {form: collections.deque() for form in FORMS}
         self.completed: List[Request] = []
+        # fills go out on their own stream; their descriptors are staged in a
+        # page-locked ring of FILL_DEPTH slots, each reused once the fill that
+        # last read it has run (its event)
         self.fill_stream = Stream()
-        self.fill_done = Event()
         self.fill_capacity = fill_capacity
         self.fill_scratch = DeviceBuffer(ctypes.sizeof(SbFillDesc) * fill_capacity)
-        self._fill_pending = False
+        self.fill_staging = PinnedBuffer(ctypes.sizeof(SbFillDesc) * fill_capacity * FILL_DEPTH)
+        self.fill_events = [Event() for _ in range(FILL_DEPTH)]
+        self._fill_used = [False] * FILL_DEPTH
+        self._fill_next = 0
+        self.fill_done = self.fill_events[0]
         self.max_waiting = 0
 
     # -- client side ------------------------------------------------------------
@@ -269,7 +293,7 @@ class Server:
             req = self.waiting[0]
             specs = HDIFF_FIELDS if req.op == "hdiff" else VADV_FIELDS
             shape, strides, halo = field_layout(req.op, req.ni, req.nj, req.nk)
-            count = int(np.prod(shape))
+            count = math.prod(shape)
             bufs = []
             for _ in specs:
                 buf = self.pool.try_alloc(count * ITEMSIZE[req.storage])
@@ -289,9 +313,15 @@ class Server:
             req.admitted = now
             self.ready[req.storage].append(req)
         if descs:
-            _fill(descs, self.fill_scratch, self.fill_stream)
-            self.fill_done.record(self.fill_stream)
-            self._fill_pending = True
+            k = self._fill_next
+            self._fill_next = (k + 1) % FILL_DEPTH
+            if self._fill_used[k]:
+                self.fill_events[k].synchronize()  # normally long done
+            staging = self.fill_staging.ptr + k * self.fill_capacity * ctypes.sizeof(SbFillDesc)
+            _fill(descs, self.fill_scratch, self.fill_stream, staging)
+            self.fill_events[k].record(self.fill_stream)
+            self._fill_used[k] = True
+            self.fill_done = self.fill_events[k]
 
     def _dispatch(self):
         for form, queue in self.ready.items():

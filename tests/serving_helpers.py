@@ -8,27 +8,36 @@ import numpy as np
 from oracle import stencils as ora
 from stencil_benchmarks_gb300 import serving
 
-_G = np.uint64(0x9E3779B97F4A7C15)
-
-
-def splitmix64(z):
-    z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
-    z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
-    return z ^ (z >> np.uint64(31))
+def lowbias32(x):
+    """C. Wellons' lowbias32 hash on uint32 arrays."""
+    x = x ^ (x >> np.uint32(16))
+    x = x * np.uint32(0x7FEB352D)
+    x = x ^ (x >> np.uint32(15))
+    x = x * np.uint32(0x846CA68B)
+    return x ^ (x >> np.uint32(16))
 
 
 def fill_values(seed, count, lo, hi, storage):
     """What sb_fill_batch writes: storage values (bf16 as uint16 bits)."""
+    k0, k1 = np.uint32(seed & 0xFFFFFFFF), np.uint32(seed >> 32)
     with np.errstate(over="ignore"):
         e = np.arange(count, dtype=np.uint64)
-        z = np.uint64(seed) + (e + np.uint64(1)) * _G
-        u = (splitmix64(z) >> np.uint64(11)).astype(np.float64) * 2.0**-53
-    v = lo + (hi - lo) * u
-    if storage == "float64":
-        return v
+        lo32 = (e & np.uint64(0xFFFFFFFF)).astype(np.uint32)
+        hi32 = (e >> np.uint64(32)).astype(np.uint32)
+        h1 = lowbias32(lowbias32(lo32 ^ k0) ^ (k1 ^ (hi32 * np.uint32(0x9E3779B9))))
+        if storage == "float64":
+            h2 = lowbias32(h1 ^ np.uint32((int(k0) + 0x632BE5AB) & 0xFFFFFFFF))
+            k = (h1.astype(np.uint64) << np.uint64(21)) | (h2 >> np.uint32(11)).astype(np.uint64)
+            span = np.float64(hi) - np.float64(lo)
+            return np.float64(lo) + span * (k.astype(np.float64) * 2.0**-53)
+    lo_f = np.float32(lo)
+    span_f = np.float32(np.float64(hi) - np.float64(lo))
+    u = (h1 >> np.uint32(8)).astype(np.float32) * np.float32(2.0**-24)
+    v = lo_f + span_f * u
+    assert v.dtype == np.float32
     if storage == "float32":
-        return v.astype(np.float32)
-    return ora.f32_to_bf16_bits(v.astype(np.float32))
+        return v
+    return ora.f32_to_bf16_bits(v)
 
 
 def request_inputs(req):

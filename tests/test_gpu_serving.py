@@ -19,20 +19,50 @@ pytestmark = pytest.mark.gpu
 
 
 @pytest.mark.parametrize("storage", ["float64", "float32", "bfloat16"])
-def test_device_fill_matches_host_reproduction(storage, lib):
+@pytest.mark.parametrize("lo,hi", [(-0.5, 0.5), (0.0, 1.0), (-1.0, 1.0), (0.25, 1.0), (-3.0, 5.0)])
+@pytest.mark.parametrize("offset", [0, 8])
+def test_device_fill_matches_host_reproduction(storage, lo, hi, offset, lib):
+    """Power-of-two spans from 0 or centred take the exact integer route for
+    float64, the others the fp64 formula; an offset of 8 bytes takes the
+    element-wise path; 100003 elements leave a ragged end."""
     count = 100_003
-    buf = DeviceBuffer(count * 8)
+    itemsize = storage_numpy_dtype(storage).itemsize
+    offset = offset // 8 * itemsize  # keeps the element alignment
+    buf = DeviceBuffer(count * 8 + 64)
     scratch = DeviceBuffer(1024)
-    desc = serving.SbFillDesc(buf.ptr, count, 0x1234567890ABCDEF, -0.5, 0.5, _native.storage_code(storage), 0)
+    desc = serving.SbFillDesc(buf.ptr + offset, count, 0x1234567890ABCDEF, lo, hi, _native.storage_code(storage), 0)
     stream = Stream()
     serving._fill([desc], scratch, stream)
     stream.synchronize()
     host = np.empty(count, dtype=storage_numpy_dtype(storage))
     from stencil_benchmarks_gb300.device import copy_to_host
 
-    copy_to_host(host, buf.ptr)
-    want = fill_values(0x1234567890ABCDEF, count, -0.5, 0.5, storage)
+    copy_to_host(host, buf.ptr + offset)
+    want = fill_values(0x1234567890ABCDEF, count, lo, hi, storage)
     assert bits_equal(host, want), mismatch_report(host, want)
+
+
+def test_fill_many_fields_in_one_launch(lib):
+    """Several descriptors of mixed storage and size in one call, from a
+    page-locked staging area."""
+    from stencil_benchmarks_gb300.device import PinnedBuffer, copy_to_host
+
+    specs = [("float64", 1, 0.0, 1.0), ("float32", 17, -1.0, 1.0), ("bfloat16", 4099, -0.5, 0.5),
+             ("float64", 70_001, 0.1, 0.7), ("float32", 0, 0.0, 1.0), ("bfloat16", 33, 0.0, 1.0)]
+    bufs = [DeviceBuffer(max(1, n) * 8) for _, n, _, _ in specs]
+    descs = [serving.SbFillDesc(b.ptr, n, 1000 + q, lo, hi, _native.storage_code(st), 0)
+             for q, (b, (st, n, lo, hi)) in enumerate(zip(bufs, specs))]
+    staging = PinnedBuffer(ctypes.sizeof(serving.SbFillDesc) * len(descs))
+    scratch = DeviceBuffer(ctypes.sizeof(serving.SbFillDesc) * len(descs))
+    stream = Stream()
+    serving._fill(descs, scratch, stream, staging.ptr)
+    stream.synchronize()
+    for q, (b, (st, n, lo, hi)) in enumerate(zip(bufs, specs)):
+        host = np.empty(n, dtype=storage_numpy_dtype(st))
+        if n:
+            copy_to_host(host, b.ptr)
+        want = fill_values(1000 + q, n, lo, hi, st)
+        assert bits_equal(host, want), f"field {q}: " + mismatch_report(host, want)
 
 
 def _small_mix(n, seed):

@@ -47,6 +47,17 @@ class FakeHandle:
     def record(self, stream=None):
         pass
 
+    def synchronize(self):
+        pass
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _library_built():
+    """The pool's arena is host code in the native library (no GPU needed)."""
+    from stencil_benchmarks_gb300 import build
+
+    build.build()
+
 
 @pytest.fixture
 def fake_device(monkeypatch):
@@ -55,7 +66,7 @@ def fake_device(monkeypatch):
     monkeypatch.setattr(serving, "Batch", FakeBatch)
     monkeypatch.setattr(serving, "Stream", FakeHandle)
     monkeypatch.setattr(serving, "Event", FakeHandle)
-    monkeypatch.setattr(serving, "_fill", lambda descs, scratch, stream: None)
+    monkeypatch.setattr(serving, "_fill", lambda descs, scratch, stream, staging=None: None)
     monkeypatch.setattr(serving, "_wait", lambda stream, event: None)
     monkeypatch.setattr(serving, "_event_done", lambda ev: id(ev) in done)
     monkeypatch.setattr(serving._native, "call", lambda *a, **k: 0)
@@ -137,20 +148,51 @@ def test_slots_limit_in_flight_batches(fake_device):
     assert sum(n for _, n in FakeBatch.launches) == 9
 
 
-def test_pool_reuses_size_classes_and_evicts_cached(fake_device):
-    pool = serving.DevicePool(budget_bytes=10 * serving.GRANULE)
-    a = pool.try_alloc(3 * serving.GRANULE - 5)
-    assert a.nbytes == 3 * serving.GRANULE
+def test_pool_arena_best_fit_and_coalescing(fake_device):
+    A = serving.ALIGN
+    pool = serving.DevicePool(budget_bytes=100 * A)
+    base = pool.region.ptr
+    a = pool.try_alloc(10 * A - 5)
+    assert (a.ptr, a.nbytes) == (base, 10 * A)
+    b = pool.try_alloc(20 * A)
+    c = pool.try_alloc(30 * A)
+    d = pool.try_alloc(40 * A)
+    assert [x.ptr - base for x in (b, c, d)] == [10 * A, 30 * A, 60 * A]
+    assert pool.in_use == 100 * A and pool.try_alloc(1) is None  # budget exhausted
+    pool.release(b)
+    pool.release(d)
+    e = pool.try_alloc(15 * A)  # best fit: the 20-unit hole, not the 40-unit one
+    assert e.ptr == base + 10 * A
     pool.release(a)
-    b = pool.try_alloc(3 * serving.GRANULE)
-    assert b is a  # same size class: reused
-    c = pool.try_alloc(6 * serving.GRANULE)
-    assert c is not None and pool.in_use == 9 * serving.GRANULE
-    assert pool.try_alloc(2 * serving.GRANULE) is None  # over budget
-    pool.release(c)
-    d = pool.try_alloc(5 * serving.GRANULE)  # evicts the cached 6-granule buffer
-    assert d is not None and c.freed
-    assert pool.in_use + pool.cached <= pool.budget
+    pool.release(e)  # coalesces with the freed head: 0..30 is one free piece
+    assert pool.stats()["largest_free"] == 40 * A and pool.stats()["free_blocks"] == 2
+    pool.release(c)  # everything merges back into one piece
+    st = pool.stats()
+    assert st == {"in_use": 0, "peak": 100 * A, "largest_free": 100 * A, "free_blocks": 1}
+    with pytest.raises(serving._native.SbError):
+        pool.release(c)  # double free is an error, not silent corruption
+
+
+def test_pool_random_churn_keeps_invariants(fake_device):
+    A = serving.ALIGN
+    pool = serving.DevicePool(budget_bytes=4096 * A)
+    base = pool.region.ptr
+    rng = np.random.Generator(np.random.PCG64(1))
+    live = []
+    for _ in range(3000):
+        if live and rng.random() < 0.45:
+            pool.release(live.pop(int(rng.integers(0, len(live)))))
+        else:
+            blk = pool.try_alloc(int(rng.integers(1, 200 * A)))
+            if blk is not None:
+                live.append(blk)
+        spans = sorted((x.ptr - base, x.ptr - base + x.nbytes) for x in live)
+        assert all(s[1] <= t[0] for s, t in zip(spans, spans[1:]))  # no overlap
+        assert all(0 <= s[0] and s[1] <= 4096 * A and s[0] % A == 0 for s in spans)
+        assert pool.in_use == sum(x.nbytes for x in live)
+    for blk in live:
+        pool.release(blk)
+    assert pool.stats()["free_blocks"] == 1 and pool.in_use == 0
 
 
 def test_invalid_requests_rejected(fake_device):
@@ -187,3 +229,30 @@ def test_request_specs_distribution():
     assert abs(np.mean([r.op == "hdiff" for r in reqs]) - 0.5) < 0.03
     # log-uniform: the median size is near the geometric mean of 32 and 1024
     assert 120 < np.median(sizes) < 260
+
+
+def _f64_exact_route(k, lo, span):
+    """The fill kernel's integer construction of lo + span * k * 2^-53 (for a
+    power-of-two span with lo = 0 or lo = -span/2), restated on integers."""
+    import struct
+
+    P = int(np.log2(span))
+    x = k - (1 << 52 if lo != 0.0 else 0)
+    if x == 0:
+        return 0.0
+    sign = 1 << 63 if x < 0 else 0
+    a = abs(x)
+    msb = a.bit_length() - 1
+    mant = (a << (52 - msb)) & ((1 << 52) - 1)
+    return struct.unpack("<d", struct.pack("<Q", sign | ((1023 + msb + P - 53) << 52) | mant))[0]
+
+
+@pytest.mark.parametrize("lo,span", [(0.0, 1.0), (-1.0, 2.0), (-0.5, 1.0), (0.0, 2.0**-40), (-2.0**9, 2.0**10)])
+def test_fill_integer_route_equals_fp64_formula(lo, span):
+    rng = np.random.Generator(np.random.PCG64(4))
+    ks = [0, 1, 2, (1 << 52) - 1, 1 << 52, (1 << 52) + 1, (1 << 53) - 1]
+    ks += [int(v) for v in rng.integers(0, 1 << 53, size=3000, dtype=np.int64)]
+    for k in ks:
+        want = lo + span * (float(k) * 2.0**-53)
+        got = _f64_exact_route(k, lo, span)
+        assert np.float64(got).tobytes() == np.float64(want).tobytes(), (k, got, want)
