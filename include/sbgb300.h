@@ -48,6 +48,10 @@ extern "C" {
 #define SB_F64 0
 #define SB_F32 1
 #define SB_BF16 2 /* storage only; computed in f32 (or f64) */
+#define SB_F32X2 3 /* compute only, with f64 storage: float pair ("double-float"),
+                    * ~48-bit significand on the fp32 pipe; results within a few
+                    * 2^-48 (relative to the operands) of the f64 ones, not
+                    * bit-identical */
 
 /* ---- memcpy kinds (same values as cudaMemcpyKind) ------------------------ */
 #define SB_H2H 0
@@ -62,6 +66,10 @@ extern "C" {
 #define SB_HDIFF_JSCAN 2  /* register j-march, i-neighbours by warp shuffles       */
 #define SB_VADV_SMEM 1    /* one thread per column, ccol/dcol in shared memory     */
 #define SB_VADV_GLOBAL 2  /* one thread per column, ccol/dcol in caller scratch    */
+#define SB_VADV_SLAB 3    /* persistent threads, factors in compact per-thread slabs of
+                           * the caller's ccol/dcol (L2-resident), cp.async staging;
+                           * tune: block_x 32/64, unroll = depth 2/4/8, k_per_cta =
+                           * blocks per SM (0: as many as fit with slabs <= L2/2)  */
 
 /*
  * Launch tuning.  Zero in any field means "choose the default".  The
@@ -269,8 +277,10 @@ int sb_vadv_noalloc(int storage, int compute, const void* stage, const void* pos
                     double* time_s);
 
 /* ---- measurement helpers ---------------------------------------------------- */
-/* Throughput of dependent-free fp64 / fp32 arithmetic on this device, in
- * operations per second (kind 0: f64 add, 1: f64 fma, 2: f32 fma). */
+/* Throughput of dependent-free arithmetic on this device, in operations per
+ * second (kind 0: f64 add, 1: f64 fma, 2: f32 fma, 3: f64->f32 conversion,
+ * 4: f32->f64 conversion, 5: 32-bit integer shift/xor/multiply, 6: u32->f32
+ * conversion). */
 int sb_probe_arith_rate(int kind, double* ops_per_s);
 
 #ifdef __cplusplus

@@ -97,7 +97,7 @@ __global__ void __launch_bounds__(256)
 }
 
 // Dynamic shared memory: ccol[cap][BT], dcol[cap][BT] (compute type), then the
-// staging ring [D+1][6][BT] (storage type) at ring_offset.
+// staging ring [D+1][6][BT] (RingOf<storage>) at ring_offset.
 template <class S, class C, int BT, int D, class IDX>
 __global__ void __launch_bounds__(BT)
     batch_vadv_kernel(const DevTable* __restrict__ tab, unsigned long long* __restrict__ counter, int bucket,
@@ -110,7 +110,7 @@ __global__ void __launch_bounds__(BT)
     if (total == 0) return;
     const int t = threadIdx.x;
     C* sc = reinterpret_cast<C*>(smem_raw) + t;
-    S* ring = reinterpret_cast<S*>(smem_raw + ring_offset) + t;
+    auto* ring = reinterpret_cast<typename RingOf<S>::T*>(smem_raw + ring_offset) + t;
     for (;;) {
         if (t == 0) {
             const int64_t item = (int64_t)atomicAdd(counter, 1ULL);
@@ -135,16 +135,9 @@ __global__ void __launch_bounds__(BT)
         const int i = group * BT + t;
         if (i < dm.ni) {
             const IDX col = (IDX)i * (IDX)dm.si + (IDX)j * (IDX)dm.sj;
-            if constexpr (sizeof(S) == 2) {
-                // 2-byte storage: cp.async copies 4+ bytes, so stage through registers
-                const SmemFactors<C> fac{sc, sc + dm.nk * BT, BT};
-                vadv_column<S, C, D>((const S*)dm.f[0], (const S*)dm.f[1], (const S*)dm.f[2], (const S*)dm.f[3],
-                                     (const S*)dm.f[4], (S*)dm.out, (int64_t)col, dm.nk, dm.sk, dm.wsh, fac);
-            } else {
-                vadv_async_column<S, C, BT, D, IDX>((const S*)dm.f[0], (const S*)dm.f[1], (const S*)dm.f[2],
-                                                    (const S*)dm.f[3], (const S*)dm.f[4], (S*)dm.out, col, dm.nk,
-                                                    (IDX)dm.sk, (IDX)dm.wsh, sc, sc + dm.nk * BT, ring);
-            }
+            vadv_async_column<S, C, BT, D, IDX>((const S*)dm.f[0], (const S*)dm.f[1], (const S*)dm.f[2],
+                                                (const S*)dm.f[3], (const S*)dm.f[4], (S*)dm.out, col, dm.nk,
+                                                (IDX)dm.sk, (IDX)dm.wsh, sc, sc + dm.nk * BT, ring);
         }
         __syncthreads();  // s_dom / s_local are rewritten by the next grab
     }
@@ -177,7 +170,7 @@ Kinds kinds_for() {
     k.vadv64 = &run_vadv<S, C, 64, IDX>;
     k.vadv32_fn = (const void*)&batch_vadv_kernel<S, C, 32, kVadvDepth, IDX>;
     k.vadv64_fn = (const void*)&batch_vadv_kernel<S, C, 64, kVadvDepth, IDX>;
-    k.storage_bytes = sizeof(S);
+    k.storage_bytes = sizeof(typename RingOf<S>::T);  // ring entry
     k.compute_bytes = sizeof(C);
     return k;
 }
@@ -189,6 +182,7 @@ bool pick_kinds(int storage, int compute, bool idx64, Kinds* out) {
         return true;                                                                      \
     }
     SB_PICK(SB_F64, SB_F64, double, double, 2)
+    SB_PICK(SB_F64, SB_F32X2, double, f32x2, 2)
     SB_PICK(SB_F32, SB_F32, float, float, 4)
     SB_PICK(SB_F32, SB_F64, float, double, 2)
     SB_PICK(SB_BF16, SB_F32, bf16, float, 4)

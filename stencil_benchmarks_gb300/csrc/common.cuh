@@ -10,6 +10,7 @@
 #include <cstdio>
 
 #include "../../include/sbgb300.h"
+#include "f32x2.cuh"
 
 namespace sb {
 
@@ -70,6 +71,10 @@ template <>
 __device__ __forceinline__ double ld<double, bf16>(const bf16* p) {
     return (double)__bfloat162float(__ldg(p));
 }
+template <>
+__device__ __forceinline__ f32x2 ld<f32x2, double>(const double* p) {
+    return f32x2_from_double(__ldg(p));
+}
 
 // load through the coherent path (for fields the same kernel also writes)
 template <class C, class S>
@@ -86,6 +91,10 @@ template <>
 __device__ __forceinline__ double ldc<double, bf16>(const bf16* p) {
     return (double)__bfloat162float(*p);
 }
+template <>
+__device__ __forceinline__ f32x2 ldc<f32x2, double>(const double* p) {
+    return f32x2_from_double(*p);
+}
 
 // store a compute value into storage type S with one rounding
 template <class S, class C>
@@ -98,6 +107,36 @@ template <>
 __device__ __forceinline__ void st<float, double>(float* p, double v) { *p = __double2float_rn(v); }
 template <>
 __device__ __forceinline__ void st<bf16, float>(bf16* p, float v) { *p = __float2bfloat16_rn(v); }
+template <>
+__device__ __forceinline__ void st<double, f32x2>(double* p, f32x2 v) { *p = f32x2_to_double(v); }
+
+// a compile-time constant in compute type C (the float pair of a double)
+template <class C>
+__device__ __forceinline__ C konst(double v) {
+    return (C)v;
+}
+template <>
+__device__ __forceinline__ f32x2 konst<f32x2>(double v) {
+    return f32x2_from_double(v);
+}
+
+// whole-warp shuffles of compute values
+template <class C>
+__device__ __forceinline__ C shfl_up(C v, unsigned d) {
+    return __shfl_up_sync(0xffffffffu, v, d);
+}
+template <class C>
+__device__ __forceinline__ C shfl_down(C v, unsigned d) {
+    return __shfl_down_sync(0xffffffffu, v, d);
+}
+template <>
+__device__ __forceinline__ f32x2 shfl_up<f32x2>(f32x2 v, unsigned d) {
+    return {__shfl_up_sync(0xffffffffu, v.hi, d), __shfl_up_sync(0xffffffffu, v.lo, d)};
+}
+template <>
+__device__ __forceinline__ f32x2 shfl_down<f32x2>(f32x2 v, unsigned d) {
+    return {__shfl_down_sync(0xffffffffu, v.hi, d), __shfl_down_sync(0xffffffffu, v.lo, d)};
+}
 
 // ---------------------------------------------------------------------------
 // arithmetic with exactly one IEEE rounding per operation (never contracted
@@ -185,6 +224,29 @@ struct Ar<float> {
     }
 };
 
+// Float-pair compute (f32x2.cuh): about 48 significant bits on the fp32 pipe,
+// within a few 2^-48 of the float64 result per operation instead of
+// bit-identical to it.  The limiter compares the pair values exactly.
+template <>
+struct Ar<f32x2> {
+    static __device__ __forceinline__ f32x2 add(f32x2 a, f32x2 b) { return sb::add(a, b); }
+    static __device__ __forceinline__ f32x2 sub(f32x2 a, f32x2 b) { return sb::sub(a, b); }
+    static __device__ __forceinline__ f32x2 mul(f32x2 a, f32x2 b) { return sb::mul(a, b); }
+    static __device__ __forceinline__ f32x2 div(f32x2 a, f32x2 b) { return sb::div(a, b); }
+    static __device__ __forceinline__ f32x2 rcp(f32x2 a) { return sb::rcp(a); }
+    template <int E>
+    static __device__ __forceinline__ f32x2 scale2(f32x2 x) {
+        return sb::scale2<E>(x);
+    }
+    // (f * (a1 - a0) > 0) ? 0 : f, with the sign of a1 - a0 from an exact comparison
+    static __device__ __forceinline__ f32x2 limit(f32x2 f, f32x2 a1, f32x2 a0) {
+        const int c = cmp(a1, a0);
+        const int fs = (f.hi > 0.0f) - (f.hi < 0.0f);
+        return (fs != 0 && fs == c) ? f32x2(0) : f;
+    }
+    static __device__ __forceinline__ f32x2 neg_diff(f32x2 x, f32x2, f32x2) { return sb::neg(x); }
+};
+
 // ---------------------------------------------------------------------------
 // asynchronous global -> shared copies (cp.async, per thread, 4/8/16 bytes).
 // Completion is tracked per thread in commit groups, so a thread can keep
@@ -219,6 +281,8 @@ template <>
 __device__ __forceinline__ double cvt<double, float>(float v) { return (double)v; }
 template <>
 __device__ __forceinline__ float cvt<float, bf16>(bf16 v) { return __bfloat162float(v); }
+template <>
+__device__ __forceinline__ f32x2 cvt<f32x2, double>(double v) { return f32x2_from_double(v); }
 
 // ---------------------------------------------------------------------------
 // launch helpers

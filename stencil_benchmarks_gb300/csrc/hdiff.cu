@@ -21,6 +21,7 @@
 // Caller contract: inp is readable on [-2, ni+1] x [-2, nj+1] x [0, nk)
 // relative to the interior pointer (a halo of at least 2 in i and j).
 #include <cstdlib>
+#include <type_traits>
 
 #include "stencil_core.cuh"
 
@@ -191,9 +192,9 @@ int launch_typed(const void* inp, const void* coeff, void* out, int64_t ni, int6
     if (rc) return rc;
     int variant = tune ? tune->variant : SB_VARIANT_AUTO;
     // fp64 compute is bound by the fp64 pipe: TILE computes every lap/flx/fly
-    // once per tile (fewest fp64 operations); fp32 compute is bound by memory
-    // and instruction issue: JSCAN (shuffles, no block barriers) is faster.
-    const bool auto_tile = variant == SB_VARIANT_AUTO && sizeof(C) == 8;
+    // once per tile (fewest fp64 operations); fp32 and float-pair compute are
+    // bound by instruction issue: JSCAN (shuffles, no block barriers) is faster.
+    const bool auto_tile = variant == SB_VARIANT_AUTO && std::is_same<C, double>::value;
     if (variant == SB_VARIANT_AUTO) variant = auto_tile ? SB_HDIFF_TILE : SB_HDIFF_JSCAN;
     SB_CHECK(variant == SB_HDIFF_TILE || variant == SB_HDIFF_JSCAN, SB_ERR_UNSUPPORTED,
              "hdiff variant %d is not available", variant);
@@ -246,6 +247,8 @@ extern "C" int sb_hdiff(int storage, int compute, const void* inp, const void* c
     return timed(s, time_s, [&]() {
         if (storage == SB_F64 && compute == SB_F64)
             return launch_typed<double, double>(inp, coeff, out, ni, nj, nk, si, sj, sk, tune, s);
+        if (storage == SB_F64 && compute == SB_F32X2)
+            return launch_typed<double, f32x2>(inp, coeff, out, ni, nj, nk, si, sj, sk, tune, s);
         if (storage == SB_F32 && compute == SB_F32)
             return launch_typed<float, float>(inp, coeff, out, ni, nj, nk, si, sj, sk, tune, s);
         if (storage == SB_F32 && compute == SB_F64)

@@ -88,6 +88,47 @@ __global__ void arith_probe_kernel(double* out, int iters, double x) {
         float s = 0.f;
         for (int u = 0; u < 8; ++u) s += a[u];
         if (s == 12345.678f) out[0] = s;
+    } else if (KIND == 3) {  // f64 -> f32 conversion (the way back is an integer move)
+        double a[8];
+        for (int u = 0; u < 8; ++u) a[u] = x + (double)(threadIdx.x + u);
+        for (int it = 0; it < iters; ++it) {
+#pragma unroll
+            for (int u = 0; u < 8; ++u)
+                a[u] = __hiloint2double(__float_as_int(__double2float_rn(a[u])) ^ 0x40000000, it);
+        }
+        double s = 0.0;
+        for (int u = 0; u < 8; ++u) s += a[u];
+        if (s == 12345.678) out[0] = s;
+    } else if (KIND == 4) {  // f32 -> f64 conversion (the way back is an integer move)
+        float a[8];
+        for (int u = 0; u < 8; ++u) a[u] = (float)x + (float)(threadIdx.x + u);
+        for (int it = 0; it < iters; ++it) {
+#pragma unroll
+            for (int u = 0; u < 8; ++u) a[u] = __int_as_float(__double2hiint((double)a[u]) ^ it);
+        }
+        float s = 0.f;
+        for (int u = 0; u < 8; ++u) s += a[u];
+        if (s == 12345.678f) out[0] = s;
+    } else if (KIND == 5) {  // 32-bit integer shift, xor, multiply (3 operations a step, not foldable)
+        unsigned a[8];
+        for (int u = 0; u < 8; ++u) a[u] = (unsigned)x + threadIdx.x + u;
+        for (int it = 0; it < iters; ++it) {
+#pragma unroll
+            for (int u = 0; u < 8; ++u) a[u] = (a[u] ^ (a[u] >> 15)) * 0x2C1B3C6Du;
+        }
+        unsigned s = 0;
+        for (int u = 0; u < 8; ++u) s += a[u];
+        if (s == 12345u) out[0] = s;
+    } else if (KIND == 6) {  // u32 -> f32 conversion (the way back is an integer move)
+        float a[8];
+        for (int u = 0; u < 8; ++u) a[u] = (float)x + (float)(threadIdx.x + u);
+        for (int it = 0; it < iters; ++it) {
+#pragma unroll
+            for (int u = 0; u < 8; ++u) a[u] = __uint2float_rn(__float_as_uint(a[u]) ^ (unsigned)it);
+        }
+        float s = 0.f;
+        for (int u = 0; u < 8; ++u) s += a[u];
+        if (s == 12345.678f) out[0] = s;
     } else {
         double a[8];
         for (int u = 0; u < 8; ++u) a[u] = x + (double)(threadIdx.x + u);
@@ -297,17 +338,21 @@ int sb_l2_flush(void* stream) {
 }
 
 int sb_probe_arith_rate(int kind, double* ops_per_s) {
-    SB_CHECK(kind >= 0 && kind <= 2 && ops_per_s, SB_ERR_INVALID, "bad probe arguments");
+    SB_CHECK(kind >= 0 && kind <= 6 && ops_per_s, SB_ERR_INVALID, "bad probe arguments");
     const DeviceProps* p;
     int rc = device_props(&p);
     if (rc) return rc;
     double* out = nullptr;
     SB_CUDA(cudaMalloc(&out, sizeof(double)));
-    const int blocks = p->sm_count * 8, threads = 256, iters = kind == 2 ? 8192 : 512;
+    const int blocks = p->sm_count * 8, threads = 256, iters = (kind == 2 || kind >= 5) ? 8192 : 512;
     auto launch = [&]() {
         if (kind == 0) arith_probe_kernel<0><<<blocks, threads>>>(out, iters, 0.5);
         if (kind == 1) arith_probe_kernel<1><<<blocks, threads>>>(out, iters, 0.5);
         if (kind == 2) arith_probe_kernel<2><<<blocks, threads>>>(out, iters, 0.5);
+        if (kind == 3) arith_probe_kernel<3><<<blocks, threads>>>(out, iters, 0.5);
+        if (kind == 4) arith_probe_kernel<4><<<blocks, threads>>>(out, iters, 0.5);
+        if (kind == 5) arith_probe_kernel<5><<<blocks, threads>>>(out, iters, 0.5);
+        if (kind == 6) arith_probe_kernel<6><<<blocks, threads>>>(out, iters, 0.5);
         return SB_OK;
     };
     double t = 0.0;
@@ -315,7 +360,7 @@ int sb_probe_arith_rate(int kind, double* ops_per_s) {
     if (rc == SB_OK) rc = timed(nullptr, &t, launch);
     cudaFree(out);
     if (rc) return rc;
-    *ops_per_s = (double)blocks * threads * iters * 8.0 / t;
+    *ops_per_s = (double)blocks * threads * iters * 8.0 * (kind == 5 ? 3.0 : 1.0) / t;
     return SB_OK;
 }
 

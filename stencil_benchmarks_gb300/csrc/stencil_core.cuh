@@ -29,8 +29,8 @@ __device__ __forceinline__ void hdiff_jscan_strip(const S* __restrict__ inp, con
         return (col_in && r <= rmax) ? ld<C, S>(inp + (obase + (IDX)r * sj)) : C(0);
     };
     auto lap_of = [&](C below, C center, C above) -> C {
-        const C left = __shfl_up_sync(0xffffffffu, center, 1);
-        const C right = __shfl_down_sync(0xffffffffu, center, 1);
+        const C left = shfl_up(center, 1);
+        const C right = shfl_down(center, 1);
         return A::sub(A::template scale2<2>(center), A::add(A::add(A::add(right, left), above), below));
     };
     // preamble: rows j0-2 .. j0+1
@@ -41,7 +41,7 @@ __device__ __forceinline__ void hdiff_jscan_strip(const S* __restrict__ inp, con
     const C lap_m1 = lap_of(am2, a0, a1);               // lap(j0-1)
     C lap0 = lap_of(a0, a1, a2);                        // lap(j0)
     C fly_m1 = A::limit(A::sub(lap0, lap_m1), a1, a0);  // fly(j0-1)
-    C right0 = __shfl_down_sync(0xffffffffu, a1, 1);    // inp(i+1, j0)
+    C right0 = shfl_down(a1, 1);    // inp(i+1, j0)
     // state for output row j: a0 = inp(j), a1 = inp(j+1), lap0 = lap(j)
     a0 = a1;
     a1 = a2;
@@ -58,13 +58,13 @@ __device__ __forceinline__ void hdiff_jscan_strip(const S* __restrict__ inp, con
             const int j = jb + u;
             if (j >= j1) break;  // warp-uniform
             const C a2n = nxt[u];
-            const C left1 = __shfl_up_sync(0xffffffffu, a1, 1);
-            const C right1 = __shfl_down_sync(0xffffffffu, a1, 1);
+            const C left1 = shfl_up(a1, 1);
+            const C right1 = shfl_down(a1, 1);
             const C lap1 = A::sub(A::template scale2<2>(a1), A::add(A::add(A::add(right1, left1), a2n), a0));
             const C fly0 = A::limit(A::sub(lap1, lap0), a1, a0);      // fly(i, j)
-            const C lapR = __shfl_down_sync(0xffffffffu, lap0, 1);    // lap(i+1, j)
+            const C lapR = shfl_down(lap0, 1);    // lap(i+1, j)
             const C flx0 = A::limit(A::sub(lapR, lap0), right0, a0);  // flx(i, j)
-            const C flxL = __shfl_up_sync(0xffffffffu, flx0, 1);      // flx(i-1, j)
+            const C flxL = shfl_up(flx0, 1);      // flx(i-1, j)
             if (writer) {
                 const C d = A::sub(A::add(A::sub(flx0, flxL), fly0), fly_m1);
                 st<S, C>(out + (obase + (IDX)j * sj), A::sub(a0, A::mul(cf[u], d)));
@@ -123,7 +123,7 @@ __device__ __forceinline__ void vadv_column(const S* __restrict__ stage, const S
                                             const S* __restrict__ wcon, S* out, int64_t col, int nk, int64_t sk,
                                             int64_t wsh, const F& fac) {
     using A = Ar<C>;
-    const C dtr = (C)(3.0 / 20.0);
+    const C dtr = konst<C>(3.0 / 20.0);
     // ---- forward sweep, k = 0
     int64_t o = col;
     C gcv = A::template scale2<-2>(A::add(ld<C, S>(wcon + o + sk + wsh), ld<C, S>(wcon + o + sk)));
@@ -220,29 +220,85 @@ __device__ __forceinline__ void vadv_column(const S* __restrict__ stage, const S
     }
 }
 
+// Ring entries of the SMEM-async solve.  Storage of 4 or 8 bytes is staged
+// as is.  cp.async copies at least 4 bytes, so 2-byte storage is staged as
+// the aligned 4-byte word that holds the element (its neighbour comes along;
+// the word never leaves the allocation's aligned 4-byte granule), and the
+// element's half is picked with a byte permutation when it is used.  Which
+// half holds level k of a field is bit 1 of its address: the level-0 value
+// flipped when k * sk is odd.
+template <class S>
+struct RingOf {
+    using T = S;
+};
+template <>
+struct RingOf<bf16> {
+    using T = uint32_t;
+};
+
+template <class S>
+__device__ __forceinline__ const void* ring_src(const S* p) {
+    if constexpr (sizeof(S) == 2) return (const void*)((uintptr_t)p & ~(uintptr_t)3);
+    else return (const void*)p;
+}
+
+// __byte_perm selector moving the addressed half of the staged word to the
+// high half (a bfloat16 there is the float32 of the same value)
+template <class S>
+__device__ __forceinline__ uint32_t half_sel(const S* p) {
+    return (((uintptr_t)p >> 1) & 1) ? 0x3244u : 0x1044u;
+}
+
+template <class C, class S, class T>
+__device__ __forceinline__ C from_ring(T w, uint32_t sel) {
+    if constexpr (sizeof(S) == 2) {
+        static_assert(sizeof(C) == 4, "2-byte storage is computed in float32");
+        return __uint_as_float(__byte_perm(w, 0u, sel));
+    } else {
+        return cvt<C, S>(w);
+    }
+}
+
 // SMEM-async column solve (one thread): inputs staged global -> shared with
-// cp.async into a ring of R = D+1 slots ([R][6][BT] storage elements, this
-// thread's entries at stride BT), factors in sc/sd ([nk][BT], stride BT).
-// Every address below is a per-thread base plus a compile-time offset.
-template <class S, class C, int BT, int D, class IDX>
+// cp.async into a ring of R = D+1 slots ([R][6][BT] ring entries, this
+// thread's entries at stride BT).  Factors (ccol, dcol of each level):
+//   SLAB = false: in shared memory sc/sd ([nk][BT], level stride BT);
+//   SLAB = true:  in global memory sc/sd with level stride fs (a compact
+//                 per-thread slab, small enough to stay in L2), read back in
+//                 the backward sweep through the same cp.async ring (fields
+//                 0 and 1 of a slot; needs ring entries of the compute size).
+// Every shared-memory address below is a per-thread base plus a
+// compile-time offset.
+template <class S, class C, int BT, int D, class IDX, bool SLAB = false>
 __device__ __forceinline__ void vadv_async_column(const S* __restrict__ stage, const S* __restrict__ pos,
                                                   const S* __restrict__ tens, const S* tensstage,
                                                   const S* __restrict__ wcon, S* out, IDX col, int nk, IDX sk,
-                                                  IDX wsh, C* sc, C* sd, S* ring) {
+                                                  IDX wsh, C* sc, C* sd, typename RingOf<S>::T* ring,
+                                                  int fs = 0) {
     using A = Ar<C>;
+    using T = typename RingOf<S>::T;
     constexpr int R = D + 1;
-    const C dtr = (C)(3.0 / 20.0);
+    constexpr int B = sizeof(T);
+    static_assert(!SLAB || sizeof(T) == sizeof(C), "slab factors are staged in ring entries");
+    const int64_t FS = SLAB ? (int64_t)fs : (int64_t)BT;  // level stride of the factors
+    const C dtr = konst<C>(3.0 / 20.0);
+    // half selectors of level 0 (2-byte storage only; unused otherwise)
+    const uint32_t sel_w1 = half_sel(wcon + col + sk + wsh), sel_w0 = half_sel(wcon + col + sk);
+    const uint32_t sel_st = half_sel(stage + col + sk), sel_po = half_sel(pos + col);
+    const uint32_t sel_te = half_sel(tens + col), sel_ts = half_sel(tensstage + col);
+    const uint32_t sk_odd = (uint32_t)sk & 1u;
+    auto flip = [&](int k) -> uint32_t { return ((uint32_t)k & sk_odd) ? 0x2200u : 0u; };
 
     auto issue = [&](int slot, int k) {
         if (k < nk - 1) {
             const IDX q = col + (IDX)k * sk;
-            S* d = ring + slot * 6 * BT;
-            cp_async<sizeof(S)>(d, wcon + q + sk + wsh);
-            cp_async<sizeof(S)>(d + BT, wcon + q + sk);
-            cp_async<sizeof(S)>(d + 2 * BT, stage + q + sk);
-            cp_async<sizeof(S)>(d + 3 * BT, pos + q);
-            cp_async<sizeof(S)>(d + 4 * BT, tens + q);
-            cp_async<sizeof(S)>(d + 5 * BT, tensstage + q);
+            T* d = ring + slot * 6 * BT;
+            cp_async<B>(d, ring_src(wcon + q + sk + wsh));
+            cp_async<B>(d + BT, ring_src(wcon + q + sk));
+            cp_async<B>(d + 2 * BT, ring_src(stage + q + sk));
+            cp_async<B>(d + 3 * BT, ring_src(pos + q));
+            cp_async<B>(d + 4 * BT, ring_src(tens + q));
+            cp_async<B>(d + 5 * BT, ring_src(tensstage + q));
         }
         cp_async_commit();
     };
@@ -271,9 +327,11 @@ __device__ __forceinline__ void vadv_async_column(const S* __restrict__ stage, c
             const int k = kb + u;
             if (k >= nk - 1) break;  // uniform
             cp_async_wait<D - 1>();
-            const S* sl = ring + u * 6 * BT;
-            const C w1 = cvt<C, S>(sl[0]), w0 = cvt<C, S>(sl[BT]), snext = cvt<C, S>(sl[2 * BT]);
-            const C p0 = cvt<C, S>(sl[3 * BT]), t0 = cvt<C, S>(sl[4 * BT]), ts0 = cvt<C, S>(sl[5 * BT]);
+            const T* sl = ring + u * 6 * BT;
+            const uint32_t f = flip(k);
+            const C w1 = from_ring<C, S>(sl[0], sel_w1 ^ f), w0 = from_ring<C, S>(sl[BT], sel_w0 ^ f);
+            const C snext = from_ring<C, S>(sl[2 * BT], sel_st ^ f), p0 = from_ring<C, S>(sl[3 * BT], sel_po ^ f);
+            const C t0 = from_ring<C, S>(sl[4 * BT], sel_te ^ f), ts0 = from_ring<C, S>(sl[5 * BT], sel_ts ^ f);
             issue((u + D) % R, k + D);  // the slot of level k-1, already consumed
             const C as_ = A::template scale2<-1>(-gcv);
             gcv = A::template scale2<-2>(A::add(w1, w0));
@@ -286,8 +344,8 @@ __device__ __forceinline__ void vadv_async_column(const S* __restrict__ stage, c
             const C divided = A::rcp(A::sub(bcol, A::mul(cp, as_)));
             cp = A::mul(cs, divided);
             dp = A::mul(A::sub(dv, A::mul(dp, as_)), divided);
-            sc[k * BT] = cp;
-            sd[k * BT] = dp;
+            sc[k * FS] = cp;
+            sd[k * FS] = dp;
             sprev = scur;
             scur = snext;
         }
@@ -306,8 +364,15 @@ __device__ __forceinline__ void vadv_async_column(const S* __restrict__ stage, c
     }
 
     // ---- backward sweep; pos of level L staged in slot (nk-2-L) % R, field 3
+    // (slab factors in fields 0 and 1)
     auto issue_b = [&](int slot, int k) {
-        if (k >= 0) cp_async<sizeof(S)>(ring + slot * 6 * BT + 3 * BT, pos + (col + (IDX)k * sk));
+        if (k >= 0) {
+            cp_async<B>(ring + slot * 6 * BT + 3 * BT, ring_src(pos + (col + (IDX)k * sk)));
+            if constexpr (SLAB) {
+                cp_async<sizeof(C)>(ring + slot * 6 * BT, sc + k * FS);
+                cp_async<sizeof(C)>(ring + slot * 6 * BT + BT, sd + k * FS);
+            }
+        }
         cp_async_commit();
     };
 #pragma unroll
@@ -323,9 +388,17 @@ __device__ __forceinline__ void vadv_async_column(const S* __restrict__ stage, c
             const int k = kb - u;
             if (k < 0) break;
             cp_async_wait<D - 1>();
-            const C p0 = cvt<C, S>(ring[u * 6 * BT + 3 * BT]);
+            const C p0 = from_ring<C, S>(ring[u * 6 * BT + 3 * BT], sel_po ^ flip(k));
+            C cv, dv_k;
+            if constexpr (SLAB) {
+                cv = *reinterpret_cast<const C*>(ring + u * 6 * BT);
+                dv_k = *reinterpret_cast<const C*>(ring + u * 6 * BT + BT);
+            } else {
+                cv = sc[k * BT];
+                dv_k = sd[k * BT];
+            }
             issue_b((u + D) % R, k - D);
-            data = A::sub(sd[k * BT], A::mul(sc[k * BT], data));
+            data = A::sub(dv_k, A::mul(cv, data));
             st<S, C>(out + (col + (IDX)k * sk), A::mul(dtr, A::sub(data, p0)));
         }
     }

@@ -28,6 +28,8 @@
 //   GLOBAL : the caller's ccol/dcol fields (the reference's arguments of the
 //            same names), for columns too tall for shared memory.
 // The backward sweep reads them back in reverse order.
+#include <algorithm>
+
 #include "stencil_core.cuh"
 
 namespace sb {
@@ -56,7 +58,7 @@ __global__ void __launch_bounds__(256)
     }
 }
 
-// SMEM variant with asynchronous staging (storage of 4 or 8 bytes): the six
+// SMEM variant with asynchronous staging: the six
 // per-level inputs of the forward sweep (wcon at k+1 in both columns, stage
 // at k+1, pos/tens/tensstage at k) are copied global -> shared with cp.async
 // into a ring of R = D+1 slots, D levels ahead of the recurrence; the
@@ -64,7 +66,7 @@ __global__ void __launch_bounds__(256)
 // (the level loops are unrolled by R) and BT threads per block is a template
 // parameter, so every shared-memory address is a register + immediate.
 // Layout of dynamic shared memory: ccol[nk][BT], dcol[nk][BT] (compute type),
-// then ring[R][6][BT] (storage type), 16-byte aligned.
+// then ring[R][6][BT] (RingOf<storage>), 16-byte aligned.
 template <class S, class C, int BT, int D>
 __global__ void __launch_bounds__(BT)
     vadv_async_kernel(const S* __restrict__ stage, const S* __restrict__ pos, const S* __restrict__ tens,
@@ -73,12 +75,41 @@ __global__ void __launch_bounds__(BT)
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int t = threadIdx.x;
     C* sc = reinterpret_cast<C*>(smem_raw) + t;
-    S* ring = reinterpret_cast<S*>(smem_raw + ring_offset) + t;
+    auto* ring = reinterpret_cast<typename RingOf<S>::T*>(smem_raw + ring_offset) + t;
     const int i = blockIdx.x * BT + t;
     const int j = blockIdx.y;
     if (i >= ni) return;  // no block-wide barrier below
     vadv_async_column<S, C, BT, D, int>(stage, pos, tens, tensstage, wcon, out, i * si + j * sj, nk, sk, wsh, sc,
                                         sc + nk * BT, ring);
+}
+
+// SLAB variant: a persistent grid of BT-thread blocks walks the (i-block, j)
+// column groups; each thread keeps its forward-sweep factors in a compact
+// slab of the caller's ccol/dcol memory (level k of slot q at [k * nslots +
+// q]) instead of at its column's own position, so the factor working set is
+// nslots * nk * 2 elements -- sized to stay in L2 -- rather than the whole
+// field.  Inputs and read-back factors are staged with cp.async
+// (vadv_async_column<..., SLAB = true>); the shared memory is the ring only.
+template <class S, class C, int BT, int D>
+__global__ void __launch_bounds__(BT)
+    vadv_slab_kernel(const S* __restrict__ stage, const S* __restrict__ pos, const S* __restrict__ tens,
+                     const S* tensstage, const S* __restrict__ wcon, S* out, C* __restrict__ slab_c,
+                     C* __restrict__ slab_d, int ni, int nj, int nk, int si, int sj, int sk, int wsh) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int t = threadIdx.x;
+    auto* ring = reinterpret_cast<typename RingOf<S>::T*>(smem_raw) + t;
+    const int nslots = gridDim.x * BT;
+    const int slot = blockIdx.x * BT + t;
+    const int gx = (ni + BT - 1) / BT;
+    const int64_t ngroups = (int64_t)gx * nj;
+    for (int64_t g = blockIdx.x; g < ngroups; g += gridDim.x) {
+        const int i = (int)(g % gx) * BT + t;
+        const int j = (int)(g / gx);
+        if (i < ni) {
+            vadv_async_column<S, C, BT, D, int, true>(stage, pos, tens, tensstage, wcon, out, i * si + j * sj, nk, sk,
+                                                      wsh, slab_c + slot, slab_d + slot, ring, nslots);
+        }
+    }
 }
 
 template <class S, class C, bool GLOBAL, int D>
@@ -112,7 +143,7 @@ template <class S, class C>
 size_t async_smem(int64_t nk, int bt, int depth, int* ring_offset) {
     const size_t scratch = ((2 * sizeof(C) * (size_t)nk * (size_t)bt) + 15) / 16 * 16;
     if (ring_offset) *ring_offset = (int)scratch;
-    return scratch + (size_t)(depth + 1) * 6 * (size_t)bt * sizeof(S);
+    return scratch + (size_t)(depth + 1) * 6 * (size_t)bt * sizeof(typename RingOf<S>::T);
 }
 
 template <class S, class C, int BT, int D>
@@ -127,14 +158,14 @@ int launch_async_one(dim3 grid, size_t smem, int ring_offset, cudaStream_t strea
     return SB_OK;
 }
 
-// Asynchronous SMEM kernel if this launch qualifies (4/8-byte storage, one
+// Asynchronous SMEM kernel if this launch qualifies (one
 // row of 32 or 64 columns per block, all offsets within 32 bits); returns
 // SB_ERR_UNSUPPORTED (without error text) when it does not.
 template <class S, class C>
 int launch_async(int bx, int by, int depth, const DeviceProps* p, cudaStream_t stream, const void* stage,
                  const void* pos, const void* tens, const void* tensstage, const void* wcon, void* out,
                  int64_t ni, int64_t nj, int64_t nk, int64_t si, int64_t sj, int64_t sk, int64_t wsh) {
-    if constexpr (sizeof(S) != 4 && sizeof(S) != 8) {
+    if constexpr (sizeof(S) == 2 && sizeof(C) != 4) {
         return SB_ERR_UNSUPPORTED;
     } else {
     if (by != 1 || (bx != 32 && bx != 64) || (depth != 4 && depth != 8)) return SB_ERR_UNSUPPORTED;
@@ -158,6 +189,67 @@ int launch_async(int bx, int by, int depth, const DeviceProps* p, cudaStream_t s
     }
 }
 
+template <class S, class C, int BT, int D>
+int launch_slab_one(int blocks_per_sm, const DeviceProps* p, cudaStream_t stream, const void* stage,
+                    const void* pos, const void* tens, const void* tensstage, const void* wcon, void* out,
+                    void* ccol, void* dcol, int64_t ni, int64_t nj, int64_t nk, int64_t si, int64_t sj, int64_t sk,
+                    int64_t wsh) {
+    auto kernel = vadv_slab_kernel<S, C, BT, D>;
+    const size_t smem = (size_t)(D + 1) * 6 * BT * sizeof(typename RingOf<S>::T);
+    if (smem > 48 * 1024) SB_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int fit = 0;
+    SB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fit, kernel, BT, smem));
+    int per_sm = std::max(1, fit);
+    if (blocks_per_sm > 0) {
+        per_sm = std::min(per_sm, blocks_per_sm);
+    } else {
+        // keep the factor slabs (2 * nk elements per thread) within half of L2
+        const int64_t per_block = 2 * nk * (int64_t)sizeof(C) * BT * p->sm_count;
+        const int64_t budget = (int64_t)(p->l2_bytes > 0 ? p->l2_bytes : (128 << 20)) / 2;
+        per_sm = (int)std::max<int64_t>(1, std::min<int64_t>(per_sm, budget / std::max<int64_t>(1, per_block)));
+    }
+    const int64_t ngroups = ceil_div(ni, BT) * nj;
+    // the slabs use ccol/dcol as raw memory: nslots * nk elements must lie
+    // inside the fields' interior span
+    const int64_t span = (ni - 1) * si + (nj - 1) * sj + (nk - 1) * sk + 1;
+    int64_t grid = std::min<int64_t>((int64_t)per_sm * p->sm_count, ngroups);
+    grid = std::min<int64_t>(grid, span / (nk * BT));
+    if (grid < 1) return SB_ERR_UNSUPPORTED;
+    kernel<<<(unsigned)grid, BT, smem, stream>>>((const S*)stage, (const S*)pos, (const S*)tens, (const S*)tensstage,
+                                                 (const S*)wcon, (S*)out, (C*)ccol, (C*)dcol, (int)ni, (int)nj,
+                                                 (int)nk, (int)si, (int)sj, (int)sk, (int)wsh);
+    return SB_OK;
+}
+
+// SLAB variant if this launch qualifies (ccol/dcol given, ring entries of the
+// compute size, positive strides, 32-bit offsets); SB_ERR_UNSUPPORTED (without
+// error text) otherwise.
+template <class S, class C>
+int launch_slab(int bx, int depth, int blocks_per_sm, const DeviceProps* p, cudaStream_t stream,
+                const void* stage, const void* pos, const void* tens, const void* tensstage, const void* wcon,
+                void* out, void* ccol, void* dcol, int64_t ni, int64_t nj, int64_t nk, int64_t si, int64_t sj,
+                int64_t sk, int64_t wsh) {
+    if constexpr (sizeof(typename RingOf<S>::T) != sizeof(C)) {
+        return SB_ERR_UNSUPPORTED;
+    } else {
+        if (!ccol || !dcol || si <= 0 || sj <= 0 || sk <= 0) return SB_ERR_UNSUPPORTED;
+        const int64_t span = (ni + 1) * si + nj * sj + (nk + 1) * sk;
+        if (span >= (1LL << 31) || (int64_t)ni * nj * nk >= (1LL << 31)) return SB_ERR_UNSUPPORTED;
+#define SB_VADV_SLAB_CASE(BTV, DV)                                                                              \
+    if (bx == BTV && depth == DV)                                                                               \
+        return launch_slab_one<S, C, BTV, DV>(blocks_per_sm, p, stream, stage, pos, tens, tensstage, wcon, out, \
+                                              ccol, dcol, ni, nj, nk, si, sj, sk, wsh);
+        SB_VADV_SLAB_CASE(32, 2)
+        SB_VADV_SLAB_CASE(32, 4)
+        SB_VADV_SLAB_CASE(32, 8)
+        SB_VADV_SLAB_CASE(64, 2)
+        SB_VADV_SLAB_CASE(64, 4)
+        SB_VADV_SLAB_CASE(64, 8)
+#undef SB_VADV_SLAB_CASE
+        return SB_ERR_UNSUPPORTED;
+    }
+}
+
 template <class S, class C>
 int launch_typed(const void* stage, const void* pos, const void* tens, const void* tensstage,
                  const void* wcon, void* out, void* ccol, void* dcol, int64_t ni, int64_t nj, int64_t nk,
@@ -173,7 +265,19 @@ int launch_typed(const void* stage, const void* pos, const void* tens, const voi
     const size_t smem = 2 * sizeof(C) * (size_t)nk * (size_t)(bx * by);
     const bool can_global = ccol && dcol && sizeof(S) == sizeof(C);
     if (variant == SB_VARIANT_AUTO) variant = ((int64_t)smem <= p->smem_optin) ? SB_VADV_SMEM : SB_VADV_GLOBAL;
-    SB_CHECK(variant == SB_VADV_SMEM || variant == SB_VADV_GLOBAL, SB_ERR_UNSUPPORTED, "vadv variant %d is not available", variant);
+    SB_CHECK(variant == SB_VADV_SMEM || variant == SB_VADV_GLOBAL || variant == SB_VADV_SLAB, SB_ERR_UNSUPPORTED,
+             "vadv variant %d is not available", variant);
+    if (variant == SB_VADV_SLAB) {
+        SB_CHECK(ccol && dcol, SB_ERR_INVALID, "vadv SLAB variant needs ccol/dcol scratch fields");
+        const int d = (tune && tune->unroll > 0) ? tune->unroll : 4;
+        const int bpsm = tune ? tune->k_per_cta : 0;
+        const int rc2 = launch_slab<S, C>(bx, d, bpsm, p, stream, stage, pos, tens, tensstage, wcon, out, ccol, dcol,
+                                          ni, nj, nk, si, sj, sk, wsh);
+        SB_CHECK(rc2 != SB_ERR_UNSUPPORTED, SB_ERR_UNSUPPORTED,
+                 "vadv SLAB variant: needs blocks of 32 or 64 threads, depth 2, 4 or 8, positive strides, "
+                 "32-bit offsets and a compute type as wide as the storage ring entries");
+        return rc2;
+    }
     const int64_t gx = ceil_div(ni, bx), gy = ceil_div(nj, by);
     SB_CHECK(gy <= p->max_grid_y, SB_ERR_INVALID, "vadv grid too large");
     const dim3 grid((unsigned)gx, (unsigned)gy), block(bx, by);
@@ -219,6 +323,8 @@ extern "C" int sb_vadv(int storage, int compute, const void* stage, const void* 
     return timed(s, time_s, [&]() {
         if (storage == SB_F64 && compute == SB_F64)
             return launch_typed<double, double>(stage, pos, tens, tensstage, wcon, out, ccol, dcol, ni, nj, nk, si, sj, sk, wsh, tune, s);
+        if (storage == SB_F64 && compute == SB_F32X2)
+            return launch_typed<double, f32x2>(stage, pos, tens, tensstage, wcon, out, ccol, dcol, ni, nj, nk, si, sj, sk, wsh, tune, s);
         if (storage == SB_F32 && compute == SB_F32)
             return launch_typed<float, float>(stage, pos, tens, tensstage, wcon, out, ccol, dcol, ni, nj, nk, si, sj, sk, wsh, tune, s);
         if (storage == SB_F32 && compute == SB_F64)

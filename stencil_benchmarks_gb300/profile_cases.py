@@ -2,15 +2,18 @@
 
     python -m stencil_benchmarks_gb300.profile_cases [--warmup W] [--launches L] CASE...
 
-CASE is ``<stencil>-<form>`` with stencil in hdiff, vadv, triad, copy, lap and
-form in f64, f32, bf16 (bf16 = bfloat16 storage, f32 compute); ``all`` runs
-every hdiff/vadv form plus triad-f64.  Stencil cases use the 512 x 512 x 80
+CASE is ``<stencil>-<form>[:<variant>]`` with stencil in hdiff, vadv, triad, copy, lap and
+form in f64, f32, bf16 (bf16 = bfloat16 storage, f32 compute) and f32x2
+(float64 storage, float-pair compute); ``all`` runs every hdiff/vadv form
+plus triad-f64.  Stencil cases use the 512 x 512 x 80
 interior with the reference's halos (2 for hdiff, 1 for vadv); triad uses
 2^27 elements.  Each case allocates its fields, runs W warm-up launches and L
 measured launches (CUDA events), prints one line per case, and frees its
 fields before the next case.  The kernel variants are the defaults of the
-library, except vadv-f64 which uses the caller-scratch (GLOBAL) variant as
-``bench.py`` does.
+library, except vadv-f64 and vadv-f32x2, which use the caller-scratch
+(GLOBAL) variant as ``bench.py`` does.  ``:<variant>`` picks another one
+(hdiff: tile, jscan; vadv: smem, global, slab -- global and slab with
+ccol/dcol scratch fields).
 """
 
 from __future__ import annotations
@@ -26,7 +29,8 @@ from . import array as sbarray
 from .device import DeviceBuffer, Field
 
 NI, NJ, NK = 512, 512, 80
-STORAGE = {"f64": ("float64", "float64"), "f32": ("float32", "float32"), "bf16": ("bfloat16", "float32")}
+STORAGE = {"f64": ("float64", "float64"), "f32": ("float32", "float32"), "bf16": ("bfloat16", "float32"),
+           "f32x2": ("float64", "float32x2")}
 
 
 def _field(rng, storage, halo, lo, hi):
@@ -43,7 +47,12 @@ def _field(rng, storage, halo, lo, hi):
     return dev
 
 
+VARIANTS = {"tile": _native.HDIFF_TILE, "jscan": _native.HDIFF_JSCAN, "smem": _native.VADV_SMEM,
+            "global": _native.VADV_GLOBAL, "slab": _native.VADV_SLAB}
+
+
 def run_case(name, warmup, launches, rng):
+    name, _, variant = name.partition(":")
     stencil, form = name.split("-")
     if stencil == "triad":
         n = 1 << 27
@@ -58,18 +67,28 @@ def run_case(name, warmup, launches, rng):
         if stencil == "hdiff":
             f = [_field(rng, storage, (2, 2, 0), 0.0, 1.0) for _ in range(3)]
 
+            htune = _native.tune(variant=VARIANTS[variant]) if variant else None
+
             def launch(timed):
-                return kernels.hdiff(*f, compute=compute, timed=timed)
+                return kernels.hdiff(*f, compute=compute, tune=htune, timed=timed)
         elif stencil == "vadv":
             f = [_field(rng, storage, (1, 1, 0), -1.0, 1.0) for _ in range(4)]
             f.append(_field(rng, storage, (1, 1, 0), -0.5, 0.5))
             out = _field(rng, storage, (1, 1, 0), 0.0, 0.0)
             scratch = {}
             tune = None
-            if form == "f64":
-                scratch = {"ccol": _field(rng, storage, (1, 1, 0), 0.0, 0.0),
-                           "dcol": _field(rng, storage, (1, 1, 0), 0.0, 0.0)}
-                tune = _native.tune(variant=_native.VADV_GLOBAL, block_x=64, unroll=2)
+            scratch_storage = "float64" if compute in ("float64", "float32x2") else "float32"
+            if variant in ("global", "slab") or (not variant and form in ("f64", "f32x2")):
+                scratch = {"ccol": _field(rng, scratch_storage, (1, 1, 0), 0.0, 0.0),
+                           "dcol": _field(rng, scratch_storage, (1, 1, 0), 0.0, 0.0)}
+            if variant == "slab":
+                tune = _native.tune(variant=_native.VADV_SLAB, block_x=64, unroll=2 if form == "f32x2" else 4,
+                                    k_per_cta=32 if form == "f32x2" else 16)
+            elif variant:
+                tune = _native.tune(variant=VARIANTS[variant])
+            elif form in ("f64", "f32x2"):
+                tune = _native.tune(variant=_native.VADV_GLOBAL, block_x=64 if form == "f64" else 32,
+                                    unroll=2 if form == "f64" else 1)
 
             def launch(timed):
                 return kernels.vadv(*f, out=out, compute=compute, tune=tune, timed=timed, **scratch)
@@ -97,7 +116,7 @@ def main(argv=None):
     cases = []
     for c in args.cases:
         if c == "all":
-            cases += [f"{s}-{f}" for s in ("hdiff", "vadv") for f in ("f64", "f32", "bf16")] + ["triad-f64"]
+            cases += [f"{s}-{f}" for s in ("hdiff", "vadv") for f in STORAGE] + ["triad-f64"]
         else:
             cases.append(c)
     _native.call("sb_set_device", 0)

@@ -1,0 +1,185 @@
+"""Float-pair compute (float64 storage, compute "float32x2") on the GPU
+against the float64 oracle, within the stated tolerances:
+
+    hdiff: max |got - oracle| <= 1e-12 * max |oracle|
+    vadv:  max |got - oracle| <= 1e-10 * max |oracle|
+
+(relative to the field's magnitude: the pair carries about 48 significant
+bits, so isolated results close to zero have large pointwise relative
+errors while their absolute error stays a few 2^-48 of the operands).
+"""
+
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from oracle import stencils as ora
+from stencil_benchmarks_gb300 import _native, kernels
+from stencil_benchmarks_gb300.batching import Batch, HdiffDomain, VadvDomain
+from tests.conftest import golden_cases, load_golden
+from tests.gpu_helpers import (
+    VADV_ARGS,
+    VADV_DISTS,
+    download_like,
+    host_field,
+    interior,
+    rng_fields,
+    to_device,
+)
+
+pytestmark = pytest.mark.gpu
+
+HDIFF_TOL = 1e-12
+VADV_TOL = 1e-10
+
+
+def _check(got, want, tol, what):
+    got, want = np.asarray(got, np.float64), np.asarray(want, np.float64)
+    assert got.shape == want.shape
+    scale = float(np.max(np.abs(want))) if want.size else 0.0
+    err = float(np.max(np.abs(got - want))) if want.size else 0.0
+    assert np.all(np.isfinite(got)), f"{what}: non-finite results"
+    assert err <= tol * max(scale, 1e-300), f"{what}: max abs error {err:.3e} > {tol:g} * {scale:.3e}"
+    return err / max(scale, 1e-300)
+
+
+def _hdiff(domain, halo, tune=None, seed=0, layout=(2, 1, 0)):
+    shape = tuple(d + 2 * h for d, h in zip(domain, halo))
+    vals = rng_fields(seed, shape, ("inp", "coeff", "out"), {})
+    hosts = {n: host_field(v, "float64", layout, 0, halo) for n, v in vals.items()}
+    dev = {n: to_device(h, "float64", halo) for n, h in hosts.items()}
+    kernels.hdiff(dev["inp"], dev["coeff"], dev["out"], compute="float32x2", tune=tune)
+    got = interior(download_like(dev["out"], hosts["out"]), domain, halo)
+    want = ora.hdiff(np.array(hosts["inp"]), np.array(hosts["coeff"]), domain, halo)
+    return got, want
+
+
+@pytest.mark.parametrize("variant", [_native.HDIFF_TILE, _native.HDIFF_JSCAN])
+@pytest.mark.parametrize("domain,halo,layout", [((150, 97, 6), (2, 2, 0), (2, 1, 0)),
+                                                ((33, 130, 2), (2, 4, 2), (0, 1, 2)),
+                                                ((1, 1, 1), (2, 2, 0), (2, 1, 0))])
+def test_hdiff_pair(variant, domain, halo, layout, lib):
+    got, want = _hdiff(domain, halo, tune=_native.tune(variant=variant), seed=21, layout=layout)
+    _check(got, want, HDIFF_TOL, f"hdiff pair variant {variant} {domain}")
+
+
+def _vadv(domain, halo, tune=None, seed=0, shift=(1, 0), use_scratch=False):
+    shape = tuple(d + 2 * h for d, h in zip(domain, halo))
+    vals = rng_fields(seed, shape, VADV_ARGS, VADV_DISTS)
+    hosts = {n: host_field(v, "float64", (2, 1, 0), 0, halo) for n, v in vals.items()}
+    dev = {n: to_device(h, "float64", halo) for n, h in hosts.items()}
+    scratch = {}
+    if use_scratch:  # pair factors fit in float64-sized scratch elements
+        for n in ("ccol", "dcol"):
+            scratch[n] = to_device(host_field(np.zeros(shape), "float64", (2, 1, 0), 0, halo), "float64", halo)
+    kernels.vadv(dev["ustage"], dev["upos"], dev["utens"], dev["utensstage"], dev["wcon"], shift,
+                 ccol=scratch.get("ccol"), dcol=scratch.get("dcol"), compute="float32x2", tune=tune)
+    got = interior(download_like(dev["utensstage"], hosts["utensstage"]), domain, halo)
+    f = {n: np.array(h) for n, h in hosts.items()}
+    want = ora._vadv_component(f["ustage"], f["upos"], f["utens"], f["utensstage"], f["wcon"], domain, halo,
+                               shift[0], shift[1])
+    return got, want
+
+
+@pytest.mark.parametrize("variant,bx,by,depth", [(0, 0, 0, 0), (1, 32, 1, 4), (1, 64, 1, 8), (1, 32, 2, 2),
+                                                 (2, 32, 1, 4), (2, 128, 2, 8), (3, 32, 1, 4), (3, 64, 1, 2)])
+def test_vadv_pair_variants(variant, bx, by, depth, lib):
+    t = _native.tune(variant=variant, block_x=bx, block_y=by, unroll=depth)
+    for nk in (2, 3, 9, 40):
+        got, want = _vadv((97, 19, nk), (1, 1, 0), tune=t, seed=30 + nk, use_scratch=(variant in (2, 3)))
+        _check(got, want, VADV_TOL, f"vadv pair variant {variant} {bx}x{by} depth {depth} nk {nk}")
+
+
+@pytest.mark.parametrize("shift", [(1, 0), (0, 1), (0, 0)])
+def test_vadv_pair_shifts(shift, lib):
+    """With wcon shift (0, 0) these random columns are ill-conditioned (results
+    up to ~4e4): float64 itself is then ~7e-12 of the scale away from the
+    exact solution, and the pair's error grows by the same conditioning.  The
+    bound is 1e-10 of the scale or 2^10 times float64's own error (measured
+    against the oracle in extended precision), whichever is larger."""
+    domain, halo = (45, 20, 17), (1, 1, 1)
+    got, want = _vadv(domain, halo, seed=41, shift=shift)
+    shape = tuple(d + 2 * h for d, h in zip(domain, halo))
+    vals = rng_fields(41, shape, VADV_ARGS, VADV_DISTS)
+    ext = ora._vadv_component(*[vals[n].astype(np.longdouble) for n in VADV_ARGS], domain, halo, *shift)
+    fp64_err = float(np.max(np.abs(np.asarray(want, np.longdouble) - ext)))
+    scale = float(np.max(np.abs(want)))
+    err = float(np.max(np.abs(np.asarray(got, np.float64) - want)))
+    assert err <= max(VADV_TOL * scale, 2.0**10 * fp64_err), (shift, err, scale, fp64_err)
+
+
+@pytest.mark.parametrize("name", [n for n, m in golden_cases().items()
+                                  if not n.startswith("_") and m["kind"] in ("hdiff", "vadv")
+                                  and m["dtype"] == "float64"])
+def test_golden_pair(name, lib):
+    """The reference's own golden vectors, computed in float pairs."""
+    meta = golden_cases()[name]
+    data = load_golden(name)
+    domain, halo = tuple(meta["domain"]), tuple(meta["halo"])
+    hosts = {n: host_field(data[f"in_{n}"], "float64", halo=halo) for n in meta["args"]}
+    dev = {n: to_device(h, "float64", halo) for n, h in hosts.items()}
+    if meta["kind"] == "hdiff":
+        kernels.hdiff(dev["inp"], dev["coeff"], dev["out"], compute="float32x2")
+        pairs, tol = {"out": "out"}, HDIFF_TOL
+    else:
+        kernels.vadv(dev["ustage"], dev["upos"], dev["utens"], dev["utensstage"], dev["wcon"], (1, 0),
+                     compute="float32x2")
+        pairs, tol = {"utensstage": "utensstage"}, VADV_TOL
+        if meta["params"].get("all_components"):
+            kernels.vadv(dev["vstage"], dev["vpos"], dev["vtens"], dev["vtensstage"], dev["wcon"], (0, 1),
+                         compute="float32x2")
+            kernels.vadv(dev["wstage"], dev["wpos"], dev["wtens"], dev["wtensstage"], dev["wcon"], (0, 0),
+                         compute="float32x2")
+            pairs.update(vtensstage="vtensstage", wtensstage="wtensstage")
+    _native.synchronize()
+    shifts = {"utensstage": (1, 0), "vtensstage": (0, 1), "wtensstage": (0, 0)}
+    for expected, field in pairs.items():
+        got = interior(download_like(dev[field], hosts[field]), domain, halo)
+        want = data[f"expected_{expected}"]
+        if meta["kind"] == "hdiff":
+            _check(got, want, tol, f"{name}:{expected}")
+            continue
+        c = expected[0]  # u, v or w
+        ins = [data[f"in_{c}{n}"].astype(np.longdouble) for n in ("stage", "pos", "tens", "tensstage")]
+        ext = ora._vadv_component(*ins, data["in_wcon"].astype(np.longdouble), domain, halo, *shifts[expected])
+        fp64_err = float(np.max(np.abs(np.asarray(want, np.longdouble) - ext)))
+        err = float(np.max(np.abs(np.asarray(got, np.float64) - want)))
+        scale = float(np.max(np.abs(want)))
+        assert err <= max(tol * scale, 2.0**10 * fp64_err), (name, expected, err, scale, fp64_err)
+
+
+def test_batch_pair(lib):
+    """Uneven hdiff and vadv domains in one batch launch, float pairs."""
+    rng = np.random.Generator(np.random.PCG64(51))
+    batch = Batch("float64", "float32x2", max_domains=8, max_nk=48)
+    doms, checks = [], []
+    for q in range(8):
+        ni, nj, nk = (int(v) for v in (rng.integers(20, 90), rng.integers(10, 60), rng.integers(2, 48)))
+        if q % 2 == 0:
+            halo = (2, 2, 0)
+            shape = (ni + 4, nj + 4, nk)
+            vals = rng_fields(60 + q, shape, ("inp", "coeff", "out"), {})
+            hosts = {n: host_field(v, "float64", halo=halo) for n, v in vals.items()}
+            dev = {n: to_device(h, "float64", halo) for n, h in hosts.items()}
+            doms.append(HdiffDomain(dev["inp"], dev["coeff"], dev["out"]))
+            want = ora.hdiff(np.array(hosts["inp"]), np.array(hosts["coeff"]), (ni, nj, nk), halo)
+            checks.append((dev["out"], hosts["out"], (ni, nj, nk), halo, want, HDIFF_TOL))
+        else:
+            halo = (1, 1, 0)
+            shape = (ni + 2, nj + 2, nk)
+            vals = rng_fields(60 + q, shape, VADV_ARGS + ("out",), VADV_DISTS)
+            hosts = {n: host_field(v, "float64", halo=halo) for n, v in vals.items()}
+            dev = {n: to_device(h, "float64", halo) for n, h in hosts.items()}
+            doms.append(VadvDomain(dev["ustage"], dev["upos"], dev["utens"], dev["utensstage"], dev["wcon"],
+                                   out=dev["out"]))
+            f = {n: np.array(h) for n, h in hosts.items()}
+            want = ora._vadv_component(f["ustage"], f["upos"], f["utens"], f["utensstage"], f["wcon"],
+                                       (ni, nj, nk), halo, 1, 0)
+            checks.append((dev["out"], hosts["out"], (ni, nj, nk), halo, want, VADV_TOL))
+    batch.set(doms)
+    batch.launch()
+    _native.synchronize()
+    for q, (field, host, domain, halo, want, tol) in enumerate(checks):
+        got = interior(download_like(field, host), domain, halo)
+        _check(got, want, tol, f"batch domain {q}")
