@@ -52,6 +52,9 @@ extern "C" {
                     * ~48-bit significand on the fp32 pipe; results within a few
                     * 2^-48 (relative to the operands) of the f64 ones, not
                     * bit-identical */
+#define SB_FIX64 4 /* compute only, hdiff with f64 storage: lap/flx/fly sums exact
+                    * in 64-bit fixed point on a per-strip scale, one f64 FMA per
+                    * point; errors at f64 rounding level, not bit-identical */
 
 /* ---- memcpy kinds (same values as cudaMemcpyKind) ------------------------ */
 #define SB_H2H 0

@@ -30,6 +30,7 @@ SB_NOT_READY = 7
 
 SB_F64, SB_F32, SB_BF16 = 0, 1, 2
 SB_F32X2 = 3  # compute only: float pair ("double-float") with float64 storage
+SB_FIX64 = 4  # compute only (hdiff): 64-bit fixed-point sums with float64 storage
 H2H, H2D, D2H, D2D = 0, 1, 2, 3
 
 STREAM_INIT, STREAM_COPY, STREAM_SCALE, STREAM_ADD, STREAM_TRIAD = range(5)
@@ -38,7 +39,8 @@ VARIANT_AUTO = 0
 HDIFF_TILE, HDIFF_JSCAN = 1, 2
 VADV_SMEM, VADV_GLOBAL, VADV_SLAB = 1, 2, 3
 
-DTYPE_CODES = {"float64": SB_F64, "float32": SB_F32, "bfloat16": SB_BF16, "float32x2": SB_F32X2}
+DTYPE_CODES = {"float64": SB_F64, "float32": SB_F32, "bfloat16": SB_BF16, "float32x2": SB_F32X2,
+               "fixed64": SB_FIX64}
 
 
 class NativeLibraryError(RuntimeError):

@@ -90,7 +90,7 @@ __global__ void __launch_bounds__(256)
         const int j0 = jb * rows;
         const int j1 = min(dm.nj, j0 + rows);
         for (int k = k0; k < k1; ++k) {
-            hdiff_jscan_strip<S, C, U, IDX>((const S*)dm.f[0], (const S*)dm.f[1], (S*)dm.out, dm.ni, dm.nj,
+            hdiff_strip<S, C, U, IDX>((const S*)dm.f[0], (const S*)dm.f[1], (S*)dm.out, dm.ni, dm.nj,
                                             (IDX)dm.si, (IDX)dm.sj, (IDX)dm.sk, i, lane, j0, j1, k);
         }
     }

@@ -129,7 +129,7 @@ __global__ void __launch_bounds__(256)
     const int j1 = min(nj, j0 + TY);  // output rows [j0, j1)
     const int k0 = blockIdx.z * kper;
     const int k1 = min(nk, k0 + kper);
-    for (int k = k0; k < k1; ++k) hdiff_jscan_strip<S, C, U, IDX>(inp, coeff, out, ni, nj, si, sj, sk, i, lane, j0, j1, k);
+    for (int k = k0; k < k1; ++k) hdiff_strip<S, C, U, IDX>(inp, coeff, out, ni, nj, si, sj, sk, i, lane, j0, j1, k);
 }
 
 template <class S, class C, class IDX>
@@ -196,6 +196,9 @@ int launch_typed(const void* inp, const void* coeff, void* out, int64_t ni, int6
     // bound by instruction issue: JSCAN (shuffles, no block barriers) is faster.
     const bool auto_tile = variant == SB_VARIANT_AUTO && std::is_same<C, double>::value;
     if (variant == SB_VARIANT_AUTO) variant = auto_tile ? SB_HDIFF_TILE : SB_HDIFF_JSCAN;
+    if constexpr (std::is_same<C, fix64>::value) {
+        SB_CHECK(variant == SB_HDIFF_JSCAN, SB_ERR_UNSUPPORTED, "fixed-point hdiff runs as JSCAN strips only");
+    }
     SB_CHECK(variant == SB_HDIFF_TILE || variant == SB_HDIFF_JSCAN, SB_ERR_UNSUPPORTED,
              "hdiff variant %d is not available", variant);
     if (variant == SB_HDIFF_JSCAN) {
@@ -207,6 +210,9 @@ int launch_typed(const void* inp, const void* coeff, void* out, int64_t ni, int6
                  "hdiff jscan uses one warp (block_x = 32) per strip");
         return launch_jscan<S, C>(inp, coeff, out, ni, nj, nk, si, sj, sk, nw, ty, kper, unroll, stream, p);
     }
+    if constexpr (std::is_same<C, fix64>::value) {
+        return SB_ERR_UNSUPPORTED;
+    } else {
     const int bx = (tune && tune->block_x > 0) ? tune->block_x : (auto_tile ? 128 : 64);
     const int by = (tune && tune->block_y > 0) ? tune->block_y : 4;
     int ty = (tune && tune->tile_y > 0) ? tune->tile_y : 16;
@@ -225,6 +231,7 @@ int launch_typed(const void* inp, const void* coeff, void* out, int64_t ni, int6
 #undef SB_HDIFF_CASE
     return fail(SB_ERR_UNSUPPORTED,
                 "hdiff block (%d, %d) not instantiated; use 32x{4,8}, 64x{2,4,8} or 128x{2,4}", bx, by);
+    }
 }
 
 }  // namespace
@@ -249,6 +256,8 @@ extern "C" int sb_hdiff(int storage, int compute, const void* inp, const void* c
             return launch_typed<double, double>(inp, coeff, out, ni, nj, nk, si, sj, sk, tune, s);
         if (storage == SB_F64 && compute == SB_F32X2)
             return launch_typed<double, f32x2>(inp, coeff, out, ni, nj, nk, si, sj, sk, tune, s);
+        if (storage == SB_F64 && compute == SB_FIX64)
+            return launch_typed<double, fix64>(inp, coeff, out, ni, nj, nk, si, sj, sk, tune, s);
         if (storage == SB_F32 && compute == SB_F32)
             return launch_typed<float, float>(inp, coeff, out, ni, nj, nk, si, sj, sk, tune, s);
         if (storage == SB_F32 && compute == SB_F64)

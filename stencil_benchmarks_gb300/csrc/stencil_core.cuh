@@ -2,6 +2,8 @@
 // (hdiff.cu, vadv.cu) and the persistent batched kernel (batch.cu).
 #pragma once
 
+#include <type_traits>
+
 #include "common.cuh"
 
 namespace sb {
@@ -75,6 +77,157 @@ __device__ __forceinline__ void hdiff_jscan_strip(const S* __restrict__ inp, con
             fly_m1 = fly0;
             right0 = right1;
         }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// horizontal diffusion in 64-bit fixed point (float64 storage), one warp strip
+// ---------------------------------------------------------------------------
+// lap, flx, fly and their sum S are additions only, so they are exact in
+// two's-complement integers once the inputs share a scale.  Per warp strip
+// (32 columns x rows j0-2 .. j1+1 of one k-plane) the largest biased
+// exponent E of the inputs sets the unit u = 2^(E-1078): |inp| / u < 2^56,
+// |lap| < 2^59, |flx| < 2^60, |S| < 2^62.  Inputs below 1/8 of the strip's
+// largest binade lose the bits under u (at most 2^-56 of the largest value).
+// The limiter's sign of inp(+1) - inp is taken exactly from the float64 bit
+// patterns; flx and fly are exact integers.  The result is
+//     out = fma(-coeff, S * u, inp)
+// with S * u rounded once to float64: one fp64 operation per point, errors
+// at float64 rounding level relative to the strip's largest value.  Strips
+// with inf/nan, |inp| >= 2^1017, all |inp| < 2^-500 (where fp64 products of
+// differences could underflow) or nonzero values spanning more than 2^40
+// are computed by the float64 strip instead.
+struct fix64 {};  // compute tag: 64-bit fixed point
+
+__device__ __forceinline__ int dsign_diff(unsigned long long b1, unsigned long long b0) {
+    if (((b1 | b0) << 1) == 0) return 0;  // +-0 and +-0
+    const unsigned long long k1 = (b1 >> 63) ? ~b1 : (b1 | (1ull << 63));
+    const unsigned long long k0 = (b0 >> 63) ? ~b0 : (b0 | (1ull << 63));
+    return (k1 > k0) - (k1 < k0);
+}
+
+// (f * (inp1 - inp0) > 0) ? 0 : f for fixed-point f.  Truncation toward zero
+// is monotone, so a nonzero a1 - a0 has the sign of inp1 - inp0; equal fixed
+// values (rare) compare the float64 bit patterns.
+__device__ __forceinline__ long long fix_limit(long long f, long long a1, long long a0, unsigned long long b1,
+                                               unsigned long long b0) {
+    const long long d = a1 - a0;
+    if (d == 0) {
+        const int s = dsign_diff(b1, b0);
+        return ((f > 0 && s > 0) || (f < 0 && s < 0)) ? 0 : f;
+    }
+    return (f != 0 && (f ^ d) >= 0) ? 0 : f;
+}
+
+// float64 bit pattern -> integer multiple of 2^(E-1078), truncated toward
+// zero (E >= 523: subnormals and zeros shift out entirely)
+__device__ __forceinline__ long long fix_of(unsigned long long b, int E) {
+    const unsigned hi = (unsigned)(b >> 32);
+    const int e = (int)((hi >> 20) & 0x7ffu);
+    const unsigned long long m = ((unsigned long long)((hi & 0xfffffu) | 0x100000u) << 32) | (unsigned)b;
+    const int rs = E - e;  // >= 0: |inp| / u = m * 2^3 / 2^rs
+    const unsigned long long mag = rs < 3 ? (m << (3 - rs)) : (rs < 67 ? (m >> (rs - 3)) : 0ull);
+    const long long sgn = (long long)b >> 63;  // 0 or -1
+    return ((long long)mag ^ sgn) - sgn;
+}
+
+// S * 2^Ue rounded to float64 (|S| < 2^62; the scaling is an exponent add)
+__device__ __forceinline__ double fix_to_double(long long S, int Ue) {
+    const double d = __ll2double_rn(S);
+    if (S == 0) return 0.0;
+    return __longlong_as_double(__double_as_longlong(d) + ((long long)Ue << 52));
+}
+
+template <int U, class IDX>
+__device__ __forceinline__ void hdiff_fixed_strip(const double* __restrict__ inp, const double* __restrict__ coeff,
+                                                  double* __restrict__ out, int ni, int nj, IDX si, IDX sj, IDX sk,
+                                                  int i, int lane, int j0, int j1, int k) {
+    const bool col_in = i <= ni + 1;
+    const bool writer = lane >= 2 && lane < 2 + kJscanOut && i < ni;
+    const int rmax = nj + 1;
+    const IDX obase = (IDX)k * sk + (IDX)i * si;
+    auto load_bits = [&](int r) -> unsigned long long {
+        return (col_in && r <= rmax) ? (unsigned long long)__double_as_longlong(__ldg(inp + (obase + (IDX)r * sj)))
+                                     : 0ull;
+    };
+    // scale of the strip: largest and smallest biased exponent of the values
+    // (exponent field 0, i.e. zeros and subnormals, does not count as smallest)
+    unsigned emax = 0, emin = 0x7ff00000u;
+    for (int r = j0 - 2; r <= j1 + 1; ++r) {
+        const unsigned ef = (unsigned)(load_bits(r) >> 32) & 0x7ff00000u;
+        emax = max(emax, ef);
+        emin = min(emin, ef ? ef : 0x7ff00000u);
+    }
+    emax = __reduce_max_sync(0xffffffffu, emax) >> 20;
+    emin = __reduce_min_sync(0xffffffffu, emin) >> 20;
+    if (emax >= 2040u || emax < 523u || emax - emin > 40u) {
+        hdiff_jscan_strip<double, double, U, IDX>(inp, coeff, out, ni, nj, si, sj, sk, i, lane, j0, j1, k);
+        return;
+    }
+    const int E = (int)emax, Ue = E - 1078;
+
+    const long long am2 = fix_of(load_bits(j0 - 2), E);
+    unsigned long long b0 = load_bits(j0 - 1), b1 = load_bits(j0), b2 = load_bits(j0 + 1);
+    long long a0 = fix_of(b0, E), a1 = fix_of(b1, E), a2 = fix_of(b2, E);
+    auto lap_of = [&](long long below, long long center, long long above) -> long long {
+        return 4 * center - (shfl_down(center, 1) + shfl_up(center, 1) + above + below);
+    };
+    const long long lap_m1 = lap_of(am2, a0, a1);
+    long long lap0 = lap_of(a0, a1, a2);
+    long long fly_m1 = fix_limit(lap0 - lap_m1, a1, a0, b1, b0);
+    unsigned long long right0 = shfl_down(b1, 1);  // bits of inp(i+1, j0)
+    long long rightf0 = shfl_down(a1, 1);          // fixed inp(i+1, j0)
+    a0 = a1;
+    a1 = a2;
+    b0 = b1;
+    b1 = b2;
+    for (int jb = j0; jb < j1; jb += U) {
+        unsigned long long nxt[U];
+        double cf[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int j = jb + u;
+            nxt[u] = load_bits(j + 2);
+            cf[u] = (writer && j < j1) ? __ldg(coeff + (obase + (IDX)j * sj)) : 0.0;
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int j = jb + u;
+            if (j >= j1) break;  // warp-uniform
+            const unsigned long long b2n = nxt[u];
+            const long long a2n = fix_of(b2n, E);
+            const long long rightf1 = shfl_down(a1, 1);
+            const long long lap1 = 4 * a1 - (rightf1 + shfl_up(a1, 1) + a2n + a0);
+            const long long fly0 = fix_limit(lap1 - lap0, a1, a0, b1, b0);           // fly(i, j)
+            const long long lapR = shfl_down(lap0, 1);                                // lap(i+1, j)
+            const long long flx0 = fix_limit(lapR - lap0, rightf0, a0, right0, b0);   // flx(i, j)
+            const long long flxL = shfl_up(flx0, 1);                                  // flx(i-1, j)
+            const unsigned long long right1 = shfl_down(b1, 1);
+            if (writer) {
+                const long long sum = ((flx0 - flxL) + fly0) - fly_m1;
+                out[obase + (IDX)j * sj] = __fma_rn(-cf[u], fix_to_double(sum, Ue), __longlong_as_double((long long)b0));
+            }
+            a0 = a1;
+            a1 = a2n;
+            b0 = b1;
+            b1 = b2n;
+            lap0 = lap1;
+            fly_m1 = fly0;
+            right0 = right1;
+            rightf0 = rightf1;
+        }
+    }
+}
+
+// one strip in compute type C (fix64: the fixed-point strip, float64 storage)
+template <class S, class C, int U, class IDX>
+__device__ __forceinline__ void hdiff_strip(const S* __restrict__ inp, const S* __restrict__ coeff,
+                                            S* __restrict__ out, int ni, int nj, IDX si, IDX sj, IDX sk, int i,
+                                            int lane, int j0, int j1, int k) {
+    if constexpr (std::is_same<C, fix64>::value) {
+        hdiff_fixed_strip<U, IDX>(inp, coeff, out, ni, nj, si, sj, sk, i, lane, j0, j1, k);
+    } else {
+        hdiff_jscan_strip<S, C, U, IDX>(inp, coeff, out, ni, nj, si, sj, sk, i, lane, j0, j1, k);
     }
 }
 

@@ -3,9 +3,9 @@
     python -m stencil_benchmarks_gb300.profile_cases [--warmup W] [--launches L] CASE...
 
 CASE is ``<stencil>-<form>[:<variant>]`` with stencil in hdiff, vadv, triad, copy, lap and
-form in f64, f32, bf16 (bf16 = bfloat16 storage, f32 compute) and f32x2
-(float64 storage, float-pair compute); ``all`` runs every hdiff/vadv form
-plus triad-f64.  Stencil cases use the 512 x 512 x 80
+form in f64, f32, bf16 (bf16 = bfloat16 storage, f32 compute), f32x2
+(float64 storage, float-pair compute) and fix64 (float64 storage, hdiff only,
+fixed-point sums); ``all`` runs every hdiff/vadv form plus triad-f64.  Stencil cases use the 512 x 512 x 80
 interior with the reference's halos (2 for hdiff, 1 for vadv); triad uses
 2^27 elements.  Each case allocates its fields, runs W warm-up launches and L
 measured launches (CUDA events), prints one line per case, and frees its
@@ -30,7 +30,7 @@ from .device import DeviceBuffer, Field
 
 NI, NJ, NK = 512, 512, 80
 STORAGE = {"f64": ("float64", "float64"), "f32": ("float32", "float32"), "bf16": ("bfloat16", "float32"),
-           "f32x2": ("float64", "float32x2")}
+           "f32x2": ("float64", "float32x2"), "fix64": ("float64", "fixed64")}
 
 
 def _field(rng, storage, halo, lo, hi):
@@ -116,7 +116,8 @@ def main(argv=None):
     cases = []
     for c in args.cases:
         if c == "all":
-            cases += [f"{s}-{f}" for s in ("hdiff", "vadv") for f in STORAGE] + ["triad-f64"]
+            cases += [f"{s}-{f}" for s in ("hdiff", "vadv") for f in STORAGE if (s, f) != ("vadv", "fix64")]
+            cases.append("triad-f64")
         else:
             cases.append(c)
     _native.call("sb_set_device", 0)

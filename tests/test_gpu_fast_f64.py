@@ -1,12 +1,15 @@
-"""Float-pair compute (float64 storage, compute "float32x2") on the GPU
-against the float64 oracle, within the stated tolerances:
+"""The fast float64 forms on the GPU against the float64 oracle, within the
+stated tolerances:
 
     hdiff: max |got - oracle| <= 1e-12 * max |oracle|
     vadv:  max |got - oracle| <= 1e-10 * max |oracle|
 
-(relative to the field's magnitude: the pair carries about 48 significant
-bits, so isolated results close to zero have large pointwise relative
-errors while their absolute error stays a few 2^-48 of the operands).
+(relative to the field's magnitude).  Float-pair compute ("float32x2")
+carries about 48 significant bits, so isolated results close to zero have
+large pointwise relative errors while their absolute error stays a few 2^-48
+of the operands.  Fixed-point hdiff ("fixed64") sums exactly in 64-bit
+integers on a per-strip scale and rounds once through a float64 FMA: its
+errors are at float64 rounding level, which the tests check as well.
 """
 
 from __future__ import annotations
@@ -183,3 +186,88 @@ def test_batch_pair(lib):
     for q, (field, host, domain, halo, want, tol) in enumerate(checks):
         got = interior(download_like(field, host), domain, halo)
         _check(got, want, tol, f"batch domain {q}")
+
+
+# ---------------------------------------------------------------------------
+# fixed-point hdiff
+# ---------------------------------------------------------------------------
+
+
+def _hdiff_values(domain, halo, inp, coeff, tune=None, compute="fixed64"):
+    hosts = {"inp": host_field(inp, "float64", halo=halo), "coeff": host_field(coeff, "float64", halo=halo),
+             "out": host_field(np.zeros_like(inp), "float64", halo=halo)}
+    dev = {n: to_device(h, "float64", halo) for n, h in hosts.items()}
+    kernels.hdiff(dev["inp"], dev["coeff"], dev["out"], compute=compute, tune=tune)
+    got = interior(download_like(dev["out"], hosts["out"]), domain, halo)
+    want = ora.hdiff(np.array(hosts["inp"]), np.array(hosts["coeff"]), domain, halo)
+    return got, want
+
+
+@pytest.mark.parametrize("domain,halo,layout", [((150, 97, 6), (2, 2, 0), (2, 1, 0)),
+                                                ((33, 130, 2), (2, 4, 2), (0, 1, 2)),
+                                                ((1, 1, 1), (2, 2, 0), (2, 1, 0)),
+                                                ((512, 64, 3), (2, 2, 0), (2, 1, 0))])
+@pytest.mark.parametrize("tune", [None, dict(block_y=2, tile_y=8, unroll=1), dict(block_y=8, tile_y=64, unroll=8)])
+def test_hdiff_fixed(domain, halo, layout, tune, lib):
+    t = _native.tune(variant=_native.HDIFF_JSCAN, **tune) if tune else None
+    shape = tuple(d + 2 * h for d, h in zip(domain, halo))
+    vals = rng_fields(23, shape, ("inp", "coeff", "out"), {})
+    hosts = {n: host_field(v, "float64", layout, 0, halo) for n, v in vals.items()}
+    dev = {n: to_device(h, "float64", halo) for n, h in hosts.items()}
+    kernels.hdiff(dev["inp"], dev["coeff"], dev["out"], compute="fixed64", tune=t)
+    got = interior(download_like(dev["out"], hosts["out"]), domain, halo)
+    want = ora.hdiff(np.array(hosts["inp"]), np.array(hosts["coeff"]), domain, halo)
+    rel = _check(got, want, HDIFF_TOL, f"hdiff fixed {domain} {tune}")
+    assert rel <= 2.0**-50, rel  # float64 rounding level
+
+
+def test_hdiff_fixed_wide_magnitudes(lib):
+    """Inputs spanning 8 decades lose bits under the strip's unit: the error
+    stays at float64 rounding level of the field scale.  Strips spanning more
+    than 2^40 (here 20 decades) run the float64 strip: bit-identical."""
+    domain, halo = (96, 70, 4), (2, 2, 0)
+    shape = tuple(d + 2 * h for d, h in zip(domain, halo))
+    rng = np.random.Generator(np.random.PCG64(24))
+    sign = rng.choice([-1.0, 1.0], size=shape)
+    coeff = rng.uniform(0, 1, size=shape)
+    got, want = _hdiff_values(domain, halo, 10.0 ** rng.uniform(-8, 0, size=shape) * sign, coeff)
+    rel = _check(got, want, HDIFF_TOL, "hdiff fixed 8 decades")
+    assert rel <= 2.0**-50, rel
+    got, want = _hdiff_values(domain, halo, 10.0 ** rng.uniform(-20, 0, size=shape) * sign, coeff)
+    assert np.array_equal(got.view(np.uint64), np.asarray(want).view(np.uint64))
+
+
+def test_hdiff_fixed_fallback_strips(lib):
+    """Strips holding nan/inf, huge (>= 2^1017) or only tiny (< 2^-500)
+    values, or only zeros, run the float64 strip: bit-identical to the
+    oracle there; every other strip stays within the tolerance."""
+    domain, halo = (200, 120, 3), (2, 2, 0)
+    shape = tuple(d + 2 * h for d, h in zip(domain, halo))
+    rng = np.random.Generator(np.random.PCG64(25))
+    inp = rng.uniform(0, 1, size=shape)
+    coeff = rng.uniform(0, 1, size=shape)
+    inp[10, 5, 0] = np.nan
+    inp[40, 60, 1] = np.inf
+    inp[100:130, 0:40, 2] = rng.uniform(-1, 1, size=(30, 40)) * 2.0**1020
+    inp[0:60, 80:124, 0] = rng.uniform(-1, 1, size=(60, 44)) * 2.0**-700
+    inp[150:204, 50:124, 1] = 0.0
+    got, want = _hdiff_values(domain, halo, inp, coeff)
+    nan_got, nan_want = np.isnan(got), np.isnan(want)
+    assert np.array_equal(nan_got, nan_want)
+    fin = np.isfinite(want)
+    assert np.array_equal(np.isfinite(got), fin)
+    g, w = got[fin], want[fin]
+    big = np.abs(w) > 1e300
+    assert np.all(np.abs(g[big] - w[big]) <= 1e-12 * np.abs(w[big]).max())
+    small = ~big
+    assert np.max(np.abs(g[small] - w[small])) <= 1e-12 * np.abs(w[small]).max()
+
+
+def test_golden_fixed(lib):
+    for name, meta in golden_cases().items():
+        if name.startswith("_") or meta["kind"] != "hdiff" or meta["dtype"] != "float64":
+            continue
+        data = load_golden(name)
+        domain, halo = tuple(meta["domain"]), tuple(meta["halo"])
+        got, _ = _hdiff_values(domain, halo, data["in_inp"], data["in_coeff"])
+        _check(got, data["expected_out"], HDIFF_TOL, f"{name} fixed")
