@@ -18,6 +18,9 @@ Printed JSON line (rank 0):
   cpu_baseline the C restatement of the reference arithmetic (OpenMP, all
                host cores) on the same workload
   stream_triad STREAM triad on 2^29 fp64 (the bandwidth calibration kernel)
+  fast_f64     the same step with fixed-point hdiff and float-pair vadv
+               (within the stated tolerances, not bit-identical), with its
+               error against the exact step's outputs
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 
@@ -52,10 +55,19 @@ METRIC = "hdiff+vadv GPoints/s (fp64, 512x512x80)"
 UNIT = "GPoints/s"
 
 
-# fp64 vadv on GB300 is bound by the fp64 pipe; the GLOBAL variant (factors in
-# the ccol/dcol scratch fields) keeps more columns in flight than shared memory
-# allows and is the faster fp64 form (1.37 ms vs 1.49 ms at 512x512x80).
-VADV_TUNE = {"variant": 2, "block_x": 64, "block_y": 1, "unroll": 2}
+# fp64 vadv on GB300 is bound by the fp64 pipe; the SLAB variant (persistent
+# threads, factors in compact L2-resident slabs of the ccol/dcol scratch
+# fields) keeps the most columns in flight and is the fastest exact form
+# (1.33 ms vs 1.37 ms GLOBAL and 1.49 ms SMEM at 512x512x80).
+VADV_TUNE = {"variant": 3, "block_x": 32, "unroll": 4, "k_per_cta": 8}
+
+# The fast float64 step: hdiff with exact 64-bit fixed-point sums and one
+# float64 FMA per point (float64 rounding level), vadv in float-pair
+# arithmetic on the fp32 pipe (~48-bit significand; within 1e-10 of the
+# field scale).  Neither is bit-identical to the reference's numpy.
+FAST_HDIFF_COMPUTE = "fixed64"
+FAST_VADV_COMPUTE = "float32x2"
+FAST_VADV_TUNE = {"variant": 3, "block_x": 64, "unroll": 2, "k_per_cta": 32}
 
 
 def compulsory_bytes(kind, s=8):
@@ -210,10 +222,12 @@ def make_inputs(seed=2024):
         return a
 
     hd = {n: field(HDIFF_HALO, 0.0, 1.0) for n in ("inp", "coeff", "out")}
+    hd["out_fast"] = field(HDIFF_HALO, 0.0, 0.0)
     va = {n: field(VADV_HALO, -1.0, 1.0) for n in ("ustage", "upos", "utens", "utensstage")}
     va["wcon"] = field(VADV_HALO, -0.5, 0.5)
     # the new utensstage goes to a separate field, so every step solves the same system
     va["out"] = field(VADV_HALO, 0.0, 0.0)
+    va["out_fast"] = field(VADV_HALO, 0.0, 0.0)
     # the reference's ccol/dcol fields: scratch for the forward-elimination factors
     va["ccol"] = field(VADV_HALO, 0.0, 0.0)
     va["dcol"] = field(VADV_HALO, 0.0, 0.0)
@@ -312,6 +326,49 @@ def run_gpu(args, dist):
     e1.synchronize()
     e2e_time = dist.max(e0.elapsed(e1))
 
+    # ---- the fast float64 step (same inputs, separate outputs), timed the same way
+    def fast_step(ev=None):
+        if ev is not None:
+            ev[0].record(stream)
+        kernels.hdiff(dev_hd["inp"], dev_hd["coeff"], dev_hd["out_fast"], compute=FAST_HDIFF_COMPUTE,
+                      stream=stream)
+        if ev is not None:
+            ev[1].record(stream)
+        kernels.vadv(dev_va["ustage"], dev_va["upos"], dev_va["utens"], dev_va["utensstage"], dev_va["wcon"],
+                     out=dev_va["out_fast"], ccol=dev_va["ccol"], dcol=dev_va["dcol"], compute=FAST_VADV_COMPUTE,
+                     tune=FAST_VADV_TUNE, stream=stream)
+        if ev is not None:
+            ev[2].record(stream)
+
+    for _ in range(args.warmup):
+        fast_step()
+    stream.synchronize()
+    fev = [[Event(), Event(), Event()] for _ in range(args.steps)]
+    dist.barrier()
+    f0, f1 = Event(), Event()
+    f0.record(stream)
+    for s in range(args.steps):
+        fast_step(fev[s])
+    f1.record(stream)
+    f1.synchronize()
+    fast_elapsed = dist.max(f0.elapsed(f1))
+    fast = {"elapsed": fast_elapsed, "t_hdiff": [e[0].elapsed(e[1]) for e in fev],
+            "t_vadv": [e[1].elapsed(e[2]) for e in fev]}
+    # accuracy against the exact step's outputs (bit-identical to the reference's numpy)
+    for name, exact, approx, halo in (("hdiff", "out", "out_fast", HDIFF_HALO),
+                                      ("vadv", "out", "out_fast", VADV_HALO)):
+        src = dev_hd if name == "hdiff" else dev_va
+        host = hd if name == "hdiff" else va
+        a = np.empty_like(host[exact])
+        b = np.empty_like(host[approx])
+        src[exact].download(a)
+        src[approx].download(b)
+        sl = tuple(slice(h, h + n) for h, n in zip(halo, (NI, NJ, NK)))
+        a, b = a[sl], b[sl]
+        scale = float(np.max(np.abs(a)))
+        fast["err_" + name] = {"max_abs_over_scale": float(np.max(np.abs(a - b))) / scale,
+                               "rms_rel": float(np.sqrt(np.mean((a - b) ** 2)) / np.sqrt(np.mean(a * a)))}
+
     # ---- STREAM triad calibration (outside the timed region)
     triad = None
     if not args.no_triad:
@@ -328,7 +385,7 @@ def run_gpu(args, dist):
     return {
         "info": info, "elapsed": elapsed_max, "t_hdiff": t_hdiff, "t_vadv": t_vadv, "clocks": clk,
         "gpu_launches": gpu_launches, "e2e_time": e2e_time, "e2e_steps": e2e_steps, "h2d": h2d, "d2h": d2h,
-        "triad": triad,
+        "triad": triad, "fast": fast,
     }
 
 
@@ -510,7 +567,9 @@ def main(argv=None):
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": res["h2d"],
                     "d2h_bytes_per_step": res["d2h"], "steps": res["e2e_steps"],
                     "path": "C ABI: pinned host -> sb_memcpy_async -> sb_hdiff + sb_vadv -> pinned host"},
-            "roofline": {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peak,
+            "roofline": {"bound": "hbm", "limiter": "fp64 pipe: exact fp64 arithmetic runs at 1/73 of the fp32 "
+                                                   "rate on GB300 (0.52 Tops/s measured)",
+                         "kernel": dominant, "achieved": achieved, "peak": peak,
                          "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
                          "traffic": traffic, "algorithmic_bytes": compulsory_bytes(dominant)},
             "kernels": {
@@ -523,6 +582,23 @@ def main(argv=None):
             },
             "stream_triad": res["triad"],
             "clocks": res["clocks"],
+        }
+        fast = res["fast"]
+        fh, fv = statistics.mean(fast["t_hdiff"]), statistics.mean(fast["t_vadv"])
+        line["fast_f64"] = {
+            "what": "same step and inputs; hdiff fixed-point sums + one fp64 FMA (fp64 rounding level), vadv "
+                    "float-pair arithmetic (~48-bit significand); not bit-identical to the reference",
+            "value": 2 * POINTS * args.steps * dist.world / fast["elapsed"] / 1e9, "unit": UNIT,
+            "ms_per_step": fast["elapsed"] / args.steps * 1e3,
+            "hdiff": {"compute": FAST_HDIFF_COMPUTE, "ms": fh * 1e3, "gpoints_s": POINTS / fh / 1e9,
+                      "hbm_gbs": compulsory_bytes("hdiff") / fh / 1e9,
+                      "frac_of_" + peak_kind: compulsory_bytes("hdiff") / fh / 1e9 / peak,
+                      "error_vs_exact": fast["err_hdiff"]},
+            "vadv": {"compute": FAST_VADV_COMPUTE, "tune": FAST_VADV_TUNE, "ms": fv * 1e3,
+                     "gpoints_s": POINTS / fv / 1e9, "hbm_gbs": compulsory_bytes("vadv") / fv / 1e9,
+                     "frac_of_" + peak_kind: compulsory_bytes("vadv") / fv / 1e9 / peak,
+                     "error_vs_exact": fast["err_vadv"]},
+            "gpu_launches": 2 * args.steps,
         }
         if res["triad"]:
             line["stream_triad"]["frac_of_" + peak_kind] = res["triad"]["gbs"] / peak

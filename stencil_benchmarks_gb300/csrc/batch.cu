@@ -98,7 +98,7 @@ __global__ void __launch_bounds__(256)
 
 // Dynamic shared memory: ccol[cap][BT], dcol[cap][BT] (compute type), then the
 // staging ring [D+1][6][BT] (RingOf<storage>) at ring_offset.
-template <class S, class C, int BT, int D, class IDX>
+template <class S, class C, int BT, int D, class IDX, class P = C>
 __global__ void __launch_bounds__(BT)
     batch_vadv_kernel(const DevTable* __restrict__ tab, unsigned long long* __restrict__ counter, int bucket,
                       int cap, int ring_offset) {
@@ -109,7 +109,7 @@ __global__ void __launch_bounds__(BT)
     const int64_t total = tab->bucket_items[bucket];
     if (total == 0) return;
     const int t = threadIdx.x;
-    C* sc = reinterpret_cast<C*>(smem_raw) + t;
+    P* sc = reinterpret_cast<P*>(smem_raw) + t;
     auto* ring = reinterpret_cast<typename RingOf<S>::T*>(smem_raw + ring_offset) + t;
     for (;;) {
         if (t == 0) {
@@ -135,9 +135,10 @@ __global__ void __launch_bounds__(BT)
         const int i = group * BT + t;
         if (i < dm.ni) {
             const IDX col = (IDX)i * (IDX)dm.si + (IDX)j * (IDX)dm.sj;
-            vadv_async_column<S, C, BT, D, IDX>((const S*)dm.f[0], (const S*)dm.f[1], (const S*)dm.f[2],
-                                                (const S*)dm.f[3], (const S*)dm.f[4], (S*)dm.out, col, dm.nk,
-                                                (IDX)dm.sk, (IDX)dm.wsh, sc, sc + dm.nk * BT, ring);
+            vadv_async_column<S, C, BT, D, IDX, false, P>((const S*)dm.f[0], (const S*)dm.f[1],
+                                                          (const S*)dm.f[2], (const S*)dm.f[3], (const S*)dm.f[4],
+                                                          (S*)dm.out, col, dm.nk, (IDX)dm.sk, (IDX)dm.wsh, sc,
+                                                          sc + dm.nk * BT, ring);
         }
         __syncthreads();  // s_dom / s_local are rewritten by the next grab
     }
@@ -156,36 +157,38 @@ template <class S, class C, int U, class IDX>
 void run_hdiff(dim3 g, dim3 b, cudaStream_t s, const DevTable* t, unsigned long long* c) {
     batch_hdiff_kernel<S, C, U, IDX><<<g, b, 0, s>>>(t, c);
 }
-template <class S, class C, int BT, class IDX>
+template <class S, class C, int BT, class IDX, class P>
 void run_vadv(dim3 g, dim3 b, size_t smem, cudaStream_t s, const DevTable* t, unsigned long long* c, int bucket,
               int cap, int ring_offset) {
-    batch_vadv_kernel<S, C, BT, kVadvDepth, IDX><<<g, b, smem, s>>>(t, c, bucket, cap, ring_offset);
+    batch_vadv_kernel<S, C, BT, kVadvDepth, IDX, P><<<g, b, smem, s>>>(t, c, bucket, cap, ring_offset);
 }
 
-template <class S, class C, int U, class IDX>
+// hdiff computes in HC, vadv in VC with its recurrences in P
+template <class S, class HC, class VC, int U, class IDX, class P = VC>
 Kinds kinds_for() {
     Kinds k;
-    k.hdiff = &run_hdiff<S, C, U, IDX>;
-    k.vadv32 = &run_vadv<S, C, 32, IDX>;
-    k.vadv64 = &run_vadv<S, C, 64, IDX>;
-    k.vadv32_fn = (const void*)&batch_vadv_kernel<S, C, 32, kVadvDepth, IDX>;
-    k.vadv64_fn = (const void*)&batch_vadv_kernel<S, C, 64, kVadvDepth, IDX>;
+    k.hdiff = &run_hdiff<S, HC, U, IDX>;
+    k.vadv32 = &run_vadv<S, VC, 32, IDX, P>;
+    k.vadv64 = &run_vadv<S, VC, 64, IDX, P>;
+    k.vadv32_fn = (const void*)&batch_vadv_kernel<S, VC, 32, kVadvDepth, IDX, P>;
+    k.vadv64_fn = (const void*)&batch_vadv_kernel<S, VC, 64, kVadvDepth, IDX, P>;
     k.storage_bytes = sizeof(typename RingOf<S>::T);  // ring entry
-    k.compute_bytes = sizeof(C);
+    k.compute_bytes = sizeof(P);                      // factor entry
     return k;
 }
 
 bool pick_kinds(int storage, int compute, bool idx64, Kinds* out) {
-#define SB_PICK(SC, CC, S, C, U)                                                          \
-    if (storage == SC && compute == CC) {                                                 \
-        *out = idx64 ? kinds_for<S, C, U, int64_t>() : kinds_for<S, C, U, int>();         \
-        return true;                                                                      \
+#define SB_PICK(SC, CC, S, HC, VC, U, P)                                                            \
+    if (storage == SC && compute == CC) {                                                           \
+        *out = idx64 ? kinds_for<S, HC, VC, U, int64_t, P>() : kinds_for<S, HC, VC, U, int, P>();   \
+        return true;                                                                                \
     }
-    SB_PICK(SB_F64, SB_F64, double, double, 2)
-    SB_PICK(SB_F64, SB_F32X2, double, f32x2, 2)
-    SB_PICK(SB_F32, SB_F32, float, float, 4)
-    SB_PICK(SB_F32, SB_F64, float, double, 2)
-    SB_PICK(SB_BF16, SB_F32, bf16, float, 4)
+    SB_PICK(SB_F64, SB_F64, double, double, double, 2, double)
+    SB_PICK(SB_F64, SB_F32X2, double, f32x2, f32x2, 2, f32x2)
+    SB_PICK(SB_F64, SB_FIX64, double, fix64, f32x2, 2, f32x2)  // fixed-point hdiff, float-pair vadv
+    SB_PICK(SB_F32, SB_F32, float, float, float, 4, float)
+    SB_PICK(SB_F32, SB_F64, float, double, double, 2, double)
+    SB_PICK(SB_BF16, SB_F32, bf16, float, float, 4, float)
 #undef SB_PICK
     return false;
 }

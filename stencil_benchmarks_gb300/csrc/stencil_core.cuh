@@ -373,6 +373,20 @@ __device__ __forceinline__ void vadv_column(const S* __restrict__ stage, const S
     }
 }
 
+// Precision of the Thomas recurrences: the bulk arithmetic in C, the
+// forward-elimination divisor and factors and the back-substitution in P.
+// Every form uses P = C; the type split keeps the solve generic.
+template <class P, class C>
+__device__ __forceinline__ P to_p(C x) {
+    if constexpr (std::is_same<P, C>::value) return x;
+    else return P(x, 0.0f);
+}
+template <class C, class P>
+__device__ __forceinline__ C from_p(P x) {
+    if constexpr (std::is_same<P, C>::value) return x;
+    else return x.hi;  // a normalised pair's hi is its value rounded to float
+}
+
 // Ring entries of the SMEM-async solve.  Storage of 4 or 8 bytes is staged
 // as is.  cp.async copies at least 4 bytes, so 2-byte storage is staged as
 // the aligned 4-byte word that holds the element (its neighbour comes along;
@@ -422,17 +436,18 @@ __device__ __forceinline__ C from_ring(T w, uint32_t sel) {
 //                 0 and 1 of a slot; needs ring entries of the compute size).
 // Every shared-memory address below is a per-thread base plus a
 // compile-time offset.
-template <class S, class C, int BT, int D, class IDX, bool SLAB = false>
+template <class S, class C, int BT, int D, class IDX, bool SLAB = false, class P = C>
 __device__ __forceinline__ void vadv_async_column(const S* __restrict__ stage, const S* __restrict__ pos,
                                                   const S* __restrict__ tens, const S* tensstage,
                                                   const S* __restrict__ wcon, S* out, IDX col, int nk, IDX sk,
-                                                  IDX wsh, C* sc, C* sd, typename RingOf<S>::T* ring,
+                                                  IDX wsh, P* sc, P* sd, typename RingOf<S>::T* ring,
                                                   int fs = 0) {
     using A = Ar<C>;
+    using AP = Ar<P>;
     using T = typename RingOf<S>::T;
     constexpr int R = D + 1;
     constexpr int B = sizeof(T);
-    static_assert(!SLAB || sizeof(T) == sizeof(C), "slab factors are staged in ring entries");
+    static_assert(!SLAB || sizeof(T) == sizeof(P), "slab factors are staged in ring entries");
     const int64_t FS = SLAB ? (int64_t)fs : (int64_t)BT;  // level stride of the factors
     const C dtr = konst<C>(3.0 / 20.0);
     // half selectors of level 0 (2-byte storage only; unused otherwise)
@@ -468,8 +483,8 @@ __device__ __forceinline__ void vadv_async_column(const S* __restrict__ stage, c
     C bcol = A::sub(dtr, cs);
     C corr = A::mul(-cs, dup);
     C dv = A::add(A::add(A::add(A::mul(dtr, ld<C, S>(pos + col)), ld<C, S>(tens + col)), ldc<C, S>(tensstage + col)), corr);
-    C cp = A::div(cs, bcol);
-    C dp = A::div(dv, bcol);
+    P cp = AP::div(to_p<P>(cs), to_p<P>(bcol));
+    P dp = AP::div(to_p<P>(dv), to_p<P>(bcol));
     sc[0] = cp;
     sd[0] = dp;
 
@@ -494,9 +509,10 @@ __device__ __forceinline__ void vadv_async_column(const S* __restrict__ stage, c
             bcol = A::sub(A::sub(dtr, as_), cs);
             corr = A::sub(A::mul(-as_, ddown), A::mul(cs, dup));
             dv = A::add(A::add(A::add(A::mul(dtr, p0), t0), ts0), corr);
-            const C divided = A::rcp(A::sub(bcol, A::mul(cp, as_)));
-            cp = A::mul(cs, divided);
-            dp = A::mul(A::sub(dv, A::mul(dp, as_)), divided);
+            const P pas = to_p<P>(as_);
+            const P divided = AP::rcp(AP::sub(to_p<P>(bcol), AP::mul(cp, pas)));
+            cp = AP::mul(to_p<P>(cs), divided);
+            dp = AP::mul(AP::sub(to_p<P>(dv), AP::mul(dp, pas)), divided);
             sc[k * FS] = cp;
             sd[k * FS] = dp;
             sprev = scur;
@@ -513,7 +529,8 @@ __device__ __forceinline__ void vadv_async_column(const S* __restrict__ stage, c
         const C ddown = A::neg_diff(dup, scur, sprev);
         corr = A::mul(-as_, ddown);
         dv = A::add(A::add(A::add(A::mul(dtr, ld<C, S>(pos + o)), ld<C, S>(tens + o)), ldc<C, S>(tensstage + o)), corr);
-        dp = A::div(A::sub(dv, A::mul(dp, as_)), A::sub(bcol, A::mul(cp, as_)));
+        const P pas = to_p<P>(as_);
+        dp = AP::div(AP::sub(to_p<P>(dv), AP::mul(dp, pas)), AP::sub(to_p<P>(bcol), AP::mul(cp, pas)));
     }
 
     // ---- backward sweep; pos of level L staged in slot (nk-2-L) % R, field 3
@@ -522,18 +539,18 @@ __device__ __forceinline__ void vadv_async_column(const S* __restrict__ stage, c
         if (k >= 0) {
             cp_async<B>(ring + slot * 6 * BT + 3 * BT, ring_src(pos + (col + (IDX)k * sk)));
             if constexpr (SLAB) {
-                cp_async<sizeof(C)>(ring + slot * 6 * BT, sc + k * FS);
-                cp_async<sizeof(C)>(ring + slot * 6 * BT + BT, sd + k * FS);
+                cp_async<sizeof(P)>(ring + slot * 6 * BT, sc + k * FS);
+                cp_async<sizeof(P)>(ring + slot * 6 * BT + BT, sd + k * FS);
             }
         }
         cp_async_commit();
     };
 #pragma unroll
     for (int u = 0; u < D; ++u) issue_b(u, nk - 2 - u);
-    C data = dp;
+    P data = dp;
     {
         const IDX o = col + (IDX)(nk - 1) * sk;
-        st<S, C>(out + o, A::mul(dtr, A::sub(data, ld<C, S>(pos + o))));
+        st<S, C>(out + o, A::mul(dtr, from_p<C>(AP::sub(data, to_p<P>(ld<C, S>(pos + o))))));
     }
     for (int kb = nk - 2; kb >= 0; kb -= R) {
 #pragma unroll
@@ -542,17 +559,17 @@ __device__ __forceinline__ void vadv_async_column(const S* __restrict__ stage, c
             if (k < 0) break;
             cp_async_wait<D - 1>();
             const C p0 = from_ring<C, S>(ring[u * 6 * BT + 3 * BT], sel_po ^ flip(k));
-            C cv, dv_k;
+            P cv, dv_k;
             if constexpr (SLAB) {
-                cv = *reinterpret_cast<const C*>(ring + u * 6 * BT);
-                dv_k = *reinterpret_cast<const C*>(ring + u * 6 * BT + BT);
+                cv = *reinterpret_cast<const P*>(ring + u * 6 * BT);
+                dv_k = *reinterpret_cast<const P*>(ring + u * 6 * BT + BT);
             } else {
                 cv = sc[k * BT];
                 dv_k = sd[k * BT];
             }
             issue_b((u + D) % R, k - D);
-            data = A::sub(dv_k, A::mul(cv, data));
-            st<S, C>(out + (col + (IDX)k * sk), A::mul(dtr, A::sub(data, p0)));
+            data = AP::sub(dv_k, AP::mul(cv, data));
+            st<S, C>(out + (col + (IDX)k * sk), A::mul(dtr, from_p<C>(AP::sub(data, to_p<P>(p0)))));
         }
     }
     cp_async_wait<0>();

@@ -67,20 +67,20 @@ __global__ void __launch_bounds__(256)
 // parameter, so every shared-memory address is a register + immediate.
 // Layout of dynamic shared memory: ccol[nk][BT], dcol[nk][BT] (compute type),
 // then ring[R][6][BT] (RingOf<storage>), 16-byte aligned.
-template <class S, class C, int BT, int D>
+template <class S, class C, int BT, int D, class P = C>
 __global__ void __launch_bounds__(BT)
     vadv_async_kernel(const S* __restrict__ stage, const S* __restrict__ pos, const S* __restrict__ tens,
                       const S* tensstage, const S* __restrict__ wcon, S* out, int ni, int nj, int nk,
                       int si, int sj, int sk, int wsh, int ring_offset) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int t = threadIdx.x;
-    C* sc = reinterpret_cast<C*>(smem_raw) + t;
+    P* sc = reinterpret_cast<P*>(smem_raw) + t;
     auto* ring = reinterpret_cast<typename RingOf<S>::T*>(smem_raw + ring_offset) + t;
     const int i = blockIdx.x * BT + t;
     const int j = blockIdx.y;
     if (i >= ni) return;  // no block-wide barrier below
-    vadv_async_column<S, C, BT, D, int>(stage, pos, tens, tensstage, wcon, out, i * si + j * sj, nk, sk, wsh, sc,
-                                        sc + nk * BT, ring);
+    vadv_async_column<S, C, BT, D, int, false, P>(stage, pos, tens, tensstage, wcon, out, i * si + j * sj, nk, sk,
+                                                  wsh, sc, sc + nk * BT, ring);
 }
 
 // SLAB variant: a persistent grid of BT-thread blocks walks the (i-block, j)
@@ -138,19 +138,20 @@ int launch_depth(int depth, dim3 grid, dim3 block, size_t smem, cudaStream_t str
     return fail(SB_ERR_INVALID, "vadv prefetch depth (unroll) must be 1, 2, 4 or 8 (got %d)", depth);
 }
 
-// Shared memory of the asynchronous SMEM kernel for BT threads and depth D.
-template <class S, class C>
+// Shared memory of the asynchronous SMEM kernel for BT threads and depth D
+// (factors in the recurrence type P).
+template <class S, class P>
 size_t async_smem(int64_t nk, int bt, int depth, int* ring_offset) {
-    const size_t scratch = ((2 * sizeof(C) * (size_t)nk * (size_t)bt) + 15) / 16 * 16;
+    const size_t scratch = ((2 * sizeof(P) * (size_t)nk * (size_t)bt) + 15) / 16 * 16;
     if (ring_offset) *ring_offset = (int)scratch;
     return scratch + (size_t)(depth + 1) * 6 * (size_t)bt * sizeof(typename RingOf<S>::T);
 }
 
-template <class S, class C, int BT, int D>
+template <class S, class C, int BT, int D, class P>
 int launch_async_one(dim3 grid, size_t smem, int ring_offset, cudaStream_t stream, const void* stage,
                      const void* pos, const void* tens, const void* tensstage, const void* wcon, void* out,
                      int64_t ni, int64_t nj, int64_t nk, int64_t si, int64_t sj, int64_t sk, int64_t wsh) {
-    auto kernel = vadv_async_kernel<S, C, BT, D>;
+    auto kernel = vadv_async_kernel<S, C, BT, D, P>;
     if (smem > 48 * 1024) SB_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     kernel<<<grid, BT, smem, stream>>>((const S*)stage, (const S*)pos, (const S*)tens, (const S*)tensstage,
                                        (const S*)wcon, (S*)out, (int)ni, (int)nj, (int)nk, (int)si, (int)sj,
@@ -161,7 +162,7 @@ int launch_async_one(dim3 grid, size_t smem, int ring_offset, cudaStream_t strea
 // Asynchronous SMEM kernel if this launch qualifies (one
 // row of 32 or 64 columns per block, all offsets within 32 bits); returns
 // SB_ERR_UNSUPPORTED (without error text) when it does not.
-template <class S, class C>
+template <class S, class C, class P = C>
 int launch_async(int bx, int by, int depth, const DeviceProps* p, cudaStream_t stream, const void* stage,
                  const void* pos, const void* tens, const void* tensstage, const void* wcon, void* out,
                  int64_t ni, int64_t nj, int64_t nk, int64_t si, int64_t sj, int64_t sk, int64_t wsh) {
@@ -173,12 +174,12 @@ int launch_async(int bx, int by, int depth, const DeviceProps* p, cudaStream_t s
     const int64_t span = (ni + 1) * si + nj * sj + (nk + 1) * sk;
     if (span >= (1LL << 31)) return SB_ERR_UNSUPPORTED;
     int ring_offset = 0;
-    const size_t smem = async_smem<S, C>(nk, bx, depth, &ring_offset);
+    const size_t smem = async_smem<S, P>(nk, bx, depth, &ring_offset);
     if ((int64_t)smem > p->smem_optin) return SB_ERR_UNSUPPORTED;
     const dim3 grid((unsigned)ceil_div(ni, bx), (unsigned)nj);
 #define SB_VADV_ASYNC(BTV, DV)                                                                              \
     if (bx == BTV && depth == DV)                                                                           \
-        return launch_async_one<S, C, BTV, DV>(grid, smem, ring_offset, stream, stage, pos, tens, tensstage, \
+        return launch_async_one<S, C, BTV, DV, P>(grid, smem, ring_offset, stream, stage, pos, tens, tensstage, \
                                                wcon, out, ni, nj, nk, si, sj, sk, wsh);
     SB_VADV_ASYNC(32, 4)
     SB_VADV_ASYNC(32, 8)

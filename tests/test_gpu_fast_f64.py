@@ -193,6 +193,7 @@ def test_batch_pair(lib):
 # ---------------------------------------------------------------------------
 
 
+
 def _hdiff_values(domain, halo, inp, coeff, tune=None, compute="fixed64"):
     hosts = {"inp": host_field(inp, "float64", halo=halo), "coeff": host_field(coeff, "float64", halo=halo),
              "out": host_field(np.zeros_like(inp), "float64", halo=halo)}
@@ -271,3 +272,42 @@ def test_golden_fixed(lib):
         domain, halo = tuple(meta["domain"]), tuple(meta["halo"])
         got, _ = _hdiff_values(domain, halo, data["in_inp"], data["in_coeff"])
         _check(got, data["expected_out"], HDIFF_TOL, f"{name} fixed")
+
+
+@pytest.mark.parametrize("storage,compute", [("float64", "fixed64")])
+def test_batch_mixed_forms(storage, compute, lib):
+    """Batches of the mixed fast float64 form: fixed-point hdiff with
+    float-pair vadv on float64 storage."""
+    rng = np.random.Generator(np.random.PCG64(52))
+    batch = Batch(storage, compute, max_domains=6, max_nk=48)
+    doms, checks = [], []
+    for q in range(6):
+        ni, nj, nk = (int(v) for v in (rng.integers(20, 90), rng.integers(10, 60), rng.integers(2, 48)))
+        if q % 2 == 0:
+            halo = (2, 2, 0)
+            vals = rng_fields(80 + q, (ni + 4, nj + 4, nk), ("inp", "coeff", "out"), {})
+            hosts = {n: host_field(v, storage, halo=halo) for n, v in vals.items()}
+            dev = {n: to_device(h, storage, halo) for n, h in hosts.items()}
+            doms.append(HdiffDomain(dev["inp"], dev["coeff"], dev["out"]))
+            # float32 hdiff is plain float32: bit-identical to the oracle in float32
+            want = ora.hdiff(np.array(hosts["inp"]), np.array(hosts["coeff"]), (ni, nj, nk), halo)
+            tol = HDIFF_TOL if storage == "float64" else 0.0
+            checks.append((dev["out"], hosts["out"], (ni, nj, nk), halo, want, tol))
+        else:
+            halo = (1, 1, 0)
+            vals = rng_fields(80 + q, (ni + 2, nj + 2, nk), VADV_ARGS + ("out",), VADV_DISTS)
+            hosts = {n: host_field(v, storage, halo=halo) for n, v in vals.items()}
+            dev = {n: to_device(h, storage, halo) for n, h in hosts.items()}
+            doms.append(VadvDomain(dev["ustage"], dev["upos"], dev["utens"], dev["utensstage"], dev["wcon"],
+                                   out=dev["out"]))
+            f = {n: np.array(h, np.float64) for n, h in hosts.items()}
+            want = ora._vadv_component(f["ustage"], f["upos"], f["utens"], f["utensstage"], f["wcon"],
+                                       (ni, nj, nk), halo, 1, 0)
+            checks.append((dev["out"], hosts["out"], (ni, nj, nk), halo, want,
+                           VADV_TOL if storage == "float64" else 1e-5))
+    batch.set(doms)
+    batch.launch()
+    _native.synchronize()
+    for q, (field, host, domain, halo, want, tol) in enumerate(checks):
+        got = interior(download_like(field, host), domain, halo)
+        _check(got, want, tol, f"batch {storage}/{compute} domain {q}")
