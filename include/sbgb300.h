@@ -146,6 +146,9 @@ int sb_copy(int storage, const void* inp, void* out, int64_t ni, int64_t nj, int
 int sb_laplacian(int storage, int compute, const void* inp, void* out, int64_t ni, int64_t nj,
                  int64_t nk, int64_t si, int64_t sj, int64_t sk, int along_mask,
                  const sb_tune* tune, void* stream, double* time_s);
+/* Empty (reference: the generated kernel with an empty body, stencils/cuda_hip/
+ * basic.py:101-103): the basic stencils' grid over the domain, no memory access */
+int sb_empty(int64_t ni, int64_t nj, int64_t nk, const sb_tune* tune, void* stream, double* time_s);
 /* symmetric 0: (inp[+1] + inp) / 2; symmetric 1: (inp[+1] + inp[-1]) / 2 */
 int sb_average(int storage, int compute, const void* inp, void* out, int64_t ni, int64_t nj,
                int64_t nk, int64_t si, int64_t sj, int64_t sk, int axis, int symmetric,

@@ -114,6 +114,7 @@ SIGNATURES = {
     "sb_l2_flush": [_vp],
     "sb_stream_op": [_int, _int, _vp, _vp, _vp, _dbl, _i64, _tp, _vp, _dp],
     "sb_copy": [_int, _vp, _vp] + [_i64] * 6 + [_tp, _vp, _dp],
+    "sb_empty": [_i64] * 3 + [_tp, _vp, _dp],
     "sb_laplacian": [_int, _int, _vp, _vp] + [_i64] * 6 + [_int, _tp, _vp, _dp],
     "sb_average": [_int, _int, _vp, _vp] + [_i64] * 6 + [_int, _int, _tp, _vp, _dp],
     "sb_hdiff": [_int, _int, _vp, _vp, _vp] + [_i64] * 6 + [_tp, _vp, _dp],

@@ -176,6 +176,16 @@ class BasicStencil(Stencil):
         return 2 * int(np.prod(self.domain)) * self.dtype_size
 
 
+class EmptyStencil(BasicStencil):
+    """The reference's launch-overhead probe: no memory traffic, nothing to verify."""
+
+    stencil_kind = "empty"
+
+    @property
+    def compulsory_bytes(self):
+        return 0
+
+
 class CopyStencil(BasicStencil):
     stencil_kind = "copy"
 

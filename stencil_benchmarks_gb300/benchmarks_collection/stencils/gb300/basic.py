@@ -1,8 +1,8 @@
 """Basic stencils on GB300: ``sbench stencils gb300 basic <impl>``.
 
-Counterpart of stencil_benchmarks/benchmarks_collection/stencils/cuda_hip/basic.py:115-132
-(copy, one-sided / symmetric average, Laplacian), running ``sb_copy``,
-``sb_average`` and ``sb_laplacian``.
+Counterpart of stencil_benchmarks/benchmarks_collection/stencils/cuda_hip/basic.py:101-132
+(empty, copy, one-sided / symmetric average, Laplacian), running ``sb_empty``,
+``sb_copy``, ``sb_average`` and ``sb_laplacian``.
 """
 
 from __future__ import annotations
@@ -18,6 +18,11 @@ class BasicStencilMixin(StencilMixin):
 
     def tune(self):
         return _native.tune(block_x=self.block_size[0], block_y=self.block_size[1])
+
+
+class Empty(BasicStencilMixin, base.EmptyStencil):
+    def launch(self, fields, timed):
+        return kernels.empty(fields[0], tune=self.tune(), timed=timed)
 
 
 class Copy(BasicStencilMixin, base.CopyStencil):

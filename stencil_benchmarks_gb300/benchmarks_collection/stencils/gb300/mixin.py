@@ -26,8 +26,9 @@ class StencilMixin(Benchmark):
     dry_runs = Parameter("kernel dry-runs before the measurement", 0)
     timers = Parameter("timer type", "gpu", choices=["gpu", "wall"])
     compute_dtype = Parameter(
-        "compute type: auto (float64 for float64 storage, else float32), float32 or float64", "auto",
-        choices=["auto", "float32", "float64"],
+        "compute type: auto (float64 for float64 storage, else float32), float32, float64, float32x2 "
+        "(float-pair arithmetic, float64 storage) or fixed64 (hdiff: fixed-point sums, float64 storage)", "auto",
+        choices=["auto", "float32", "float64", "float32x2", "fixed64"],
     )
     device = Parameter("CUDA device index", 0)
 
@@ -44,6 +45,10 @@ class StencilMixin(Benchmark):
         _native.call("sb_set_device", self.device)
         if self.compute_dtype == "float32" and self.dtype == "float64":
             raise ParameterError("float64 storage with float32 compute is not provided")
+        if self.compute_dtype in ("float32x2", "fixed64") and self.dtype != "float64":
+            raise ParameterError(f"{self.compute_dtype} compute needs float64 storage")
+        if self.compute_dtype == "fixed64" and self.stencil_kind != "horizontal_diffusion":
+            raise ParameterError("fixed64 compute is provided for horizontal diffusion only")
         self._device_fields = [Field.like_host(host, self.dtype, self.halo) for host in self._data[0]]
 
     @property

@@ -8,7 +8,11 @@ at the column shifted by (1, 0), (0, 1) and (0, 0) for u, v and w
 (stencils/base.py:475-483).
 
 * ``SharedMem``     -- factors in shared memory, inputs staged with cp.async;
-* ``GlobalScratch`` -- factors in the ``ccol``/``dcol`` fields (fastest fp64 form);
+* ``GlobalScratch`` -- factors in the ``ccol``/``dcol`` fields at each
+  column's own position;
+* ``Slab``          -- persistent threads with their factors in compact,
+  L2-resident slabs of ``ccol``/``dcol`` (fastest float64 and float-pair
+  form);
 * ``NoAlloc``       -- factors in the library's static scratch array
   (``sb_vadv_noalloc``), for callers that cannot allocate device memory.
 """
@@ -69,11 +73,31 @@ class GlobalScratch(VerticalAdvectionMixin, base.VerticalAdvectionStencil):
 
     def setup(self):
         super().setup()
-        if self.dtype_size != {"float64": 8, "float32": 4}[self.compute]:
+        if self.dtype_size != {"float64": 8, "float32": 4, "float32x2": 8}[self.compute]:
             raise ParameterError("GlobalScratch keeps the factors in ccol/dcol: storage and compute types must match")
 
     def launch_component(self, f, named, shift, timed):
         tune = _native.tune(variant=_native.VADV_GLOBAL, block_x=self.block_size[0], block_y=self.block_size[1],
+                            unroll=self.unroll_factor)
+        return kernels.vadv(*f, named["wcon"], shift, ccol=named["ccol"], dcol=named["dcol"], compute=self.compute,
+                            tune=tune, timed=timed)
+
+
+class Slab(VerticalAdvectionMixin, base.VerticalAdvectionStencil):
+    block_size = Parameter("threads per block along i (32 or 64), persistent blocks per SM (0: fill L2/2)",
+                           (32, 8))
+    unroll_factor = Parameter("levels of inputs kept in flight (2, 4 or 8)", 4, choices=[2, 4, 8])
+
+    def setup(self):
+        super().setup()
+        if self.dtype_size != {"float64": 8, "float32": 4, "float32x2": 8}.get(self.compute, 0) and not (
+                self.dtype == "bfloat16" and self.compute == "float32"):
+            raise ParameterError("Slab stages its ccol/dcol factors in ring entries: compute type as wide as storage")
+        if self.block_size[0] not in (32, 64):
+            raise ParameterError("Slab blocks have 32 or 64 threads")
+
+    def launch_component(self, f, named, shift, timed):
+        tune = _native.tune(variant=_native.VADV_SLAB, block_x=self.block_size[0], k_per_cta=self.block_size[1],
                             unroll=self.unroll_factor)
         return kernels.vadv(*f, named["wcon"], shift, ccol=named["ccol"], dcol=named["dcol"], compute=self.compute,
                             tune=tune, timed=timed)

@@ -133,12 +133,40 @@ int basic_entry(int op, int storage, int compute, const void* inp, void* out, in
     });
 }
 
+// Empty: the reference's launch-overhead probe (its generated kernel body is
+// empty): the grid of the basic stencils over the domain, touching no memory.
+__global__ void __launch_bounds__(256) empty_kernel() {}
+
 }  // namespace
 }  // namespace sb
 
 using namespace sb;
 
 extern "C" {
+
+int sb_empty(int64_t ni, int64_t nj, int64_t nk, const sb_tune* tune, void* stream, double* time_s) {
+    clear_error();
+    SB_CHECK(ni >= 0 && nj >= 0 && nk >= 0, SB_ERR_INVALID, "negative domain size");
+    if (ni == 0 || nj == 0 || nk == 0) {
+        if (time_s) *time_s = 0.0;
+        return SB_OK;
+    }
+    const DeviceProps* p;
+    int rc = device_props(&p);
+    if (rc) return rc;
+    const int bx = (tune && tune->block_x > 0) ? tune->block_x : 128;
+    const int by = (tune && tune->block_y > 0) ? tune->block_y : 2;
+    SB_CHECK(bx * by <= 256 && bx % 32 == 0, SB_ERR_INVALID,
+             "block (%d, %d): need a multiple of 32 along i and at most 256 threads", bx, by);
+    const int64_t gx = ceil_div(ni, bx), gy = ceil_div(nj, by), gz = ceil_div(nk, kBasicPK);
+    SB_CHECK(gx < (1LL << 31) && gy <= p->max_grid_y && gz <= p->max_grid_z, SB_ERR_INVALID,
+             "domain too large for the launch grid");
+    return timed((cudaStream_t)stream, time_s, [&]() {
+        empty_kernel<<<dim3((unsigned)gx, (unsigned)gy, (unsigned)gz), dim3(bx, by), 0, (cudaStream_t)stream>>>();
+        SB_CUDA(cudaGetLastError());
+        return SB_OK;
+    });
+}
 
 int sb_copy(int storage, const void* inp, void* out, int64_t ni, int64_t nj, int64_t nk, int64_t si,
             int64_t sj, int64_t sk, const sb_tune* tune, void* stream, double* time_s) {

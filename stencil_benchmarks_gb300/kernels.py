@@ -95,6 +95,12 @@ def copy(inp: Field, out: Field, tune=None, stream=None, timed=False):
     return _launch("sb_copy", args, timed)
 
 
+def empty(field: Field, tune=None, stream=None, timed=False):
+    """The empty kernel over ``field``'s interior grid (launch overhead)."""
+    ni, nj, nk = _domain(field)
+    return _launch("sb_empty", [ni, nj, nk, _tune_arg(tune), _stream_arg(stream)], timed)
+
+
 def laplacian(inp: Field, out: Field, along=(True, True, False), compute=None, tune=None, stream=None,
               timed=False):
     _check_same_layout(inp, out)

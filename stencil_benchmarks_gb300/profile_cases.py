@@ -81,9 +81,9 @@ def run_case(name, warmup, launches, rng):
             if variant in ("global", "slab") or (not variant and form in ("f64", "f32x2")):
                 scratch = {"ccol": _field(rng, scratch_storage, (1, 1, 0), 0.0, 0.0),
                            "dcol": _field(rng, scratch_storage, (1, 1, 0), 0.0, 0.0)}
-            if variant == "slab":
-                tune = _native.tune(variant=_native.VADV_SLAB, block_x=64, unroll=2 if form == "f32x2" else 4,
-                                    k_per_cta=32 if form == "f32x2" else 16)
+            if variant == "slab":  # the bench's tunings for f64 and f32x2
+                slab = {"f64": (32, 4, 8), "f32x2": (64, 2, 32)}.get(form, (64, 4, 16))
+                tune = _native.tune(variant=_native.VADV_SLAB, block_x=slab[0], unroll=slab[1], k_per_cta=slab[2])
             elif variant:
                 tune = _native.tune(variant=VARIANTS[variant])
             elif form in ("f64", "f32x2"):

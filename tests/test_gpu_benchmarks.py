@@ -41,11 +41,29 @@ def test_hdiff_benchmark_forms(cls, dtype, lib):
 
 
 @pytest.mark.parametrize("cls", [vertical_advection.SharedMem, vertical_advection.GlobalScratch,
-                                 vertical_advection.NoAlloc])
+                                 vertical_advection.Slab, vertical_advection.NoAlloc])
 @pytest.mark.parametrize("all_components", [False, True])
 def test_vadv_benchmark_forms(cls, all_components, lib):
     b = cls(domain=(64, 40, 30), halo=(1, 1, 1), all_components=all_components)
     b.run()
+
+
+@pytest.mark.parametrize("cls,compute", [(horizontal_diffusion.JScan, "fixed64"),
+                                         (horizontal_diffusion.JScan, "float32x2"),
+                                         (horizontal_diffusion.Tile, "float32x2"),
+                                         (vertical_advection.SharedMem, "float32x2"),
+                                         (vertical_advection.Slab, "float32x2")])
+def test_fast_float64_forms_verify(cls, compute, lib):
+    """The fast float64 forms pass the reference's own float64 tolerance."""
+    halo = (2, 2, 0) if cls.__module__.endswith("horizontal_diffusion") else (1, 1, 0)
+    cls(domain=(90, 70, 12), halo=halo, compute_dtype=compute, data_sets=2).run()
+
+
+def test_fast_forms_parameter_checks(lib):
+    with pytest.raises(benchmark.ParameterError):
+        vertical_advection.SharedMem(domain=(16, 16, 8), halo=(1, 1, 0), compute_dtype="fixed64")
+    with pytest.raises(benchmark.ParameterError):
+        horizontal_diffusion.JScan(domain=(16, 16, 8), halo=(2, 2, 0), dtype="float32", compute_dtype="float32x2")
 
 
 def test_vadv_fp32_storage_with_fp64_solve(lib):
@@ -54,6 +72,7 @@ def test_vadv_fp32_storage_with_fp64_solve(lib):
 
 
 @pytest.mark.parametrize("cls,kw", [
+    (basic.Empty, {"halo": (1, 1, 1)}),
     (basic.Laplacian, {"along_z": True, "halo": (1, 1, 1)}),
     (basic.OnesidedAverage, {"axis": 2, "halo": (1, 1, 1)}),
     (basic.SymmetricAverage, {"axis": 1, "halo": (1, 1, 1)}),

@@ -23,7 +23,7 @@ def _compute_view(arr, stencil):
         vals = ora.bf16_bits_to_f32(np.ascontiguousarray(arr)).reshape(arr.shape)
     else:
         vals = np.array(arr)
-    return vals.astype(np.float64 if compute == "float64" else np.float32)
+    return vals.astype(np.float64 if compute in ("float64", "float32x2", "fixed64") else np.float32)
 
 
 def _to_storage(values, stencil):
