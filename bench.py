@@ -650,11 +650,11 @@ def main(argv=None):
             "hdiff": {"compute": FAST_HDIFF_COMPUTE, "ms": fh * 1e3, "gpoints_s": POINTS / fh / 1e9,
                       "hbm_gbs": compulsory_bytes("hdiff") / fh / 1e9,
                       "frac_of_" + peak_kind: compulsory_bytes("hdiff") / fh / 1e9 / peak,
-                      "error_vs_exact": fast["err_hdiff"]},
+                      "traffic": ncu_traffic().get("hdiff_fixed64"), "error_vs_exact": fast["err_hdiff"]},
             "vadv": {"compute": FAST_VADV_COMPUTE, "tune": FAST_VADV_TUNE, "ms": fv * 1e3,
                      "gpoints_s": POINTS / fv / 1e9, "hbm_gbs": compulsory_bytes("vadv") / fv / 1e9,
                      "frac_of_" + peak_kind: compulsory_bytes("vadv") / fv / 1e9 / peak,
-                     "error_vs_exact": fast["err_vadv"]},
+                     "traffic": ncu_traffic().get("vadv_f32x2"), "error_vs_exact": fast["err_vadv"]},
             "gpu_launches": 2 * args.steps,
         }
         if res["triad"]:

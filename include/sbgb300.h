@@ -286,7 +286,7 @@ int sb_vadv_noalloc(int storage, int compute, const void* stage, const void* pos
 /* Throughput of dependent-free arithmetic on this device, in operations per
  * second (kind 0: f64 add, 1: f64 fma, 2: f32 fma, 3: f64->f32 conversion,
  * 4: f32->f64 conversion, 5: 32-bit integer shift/xor/multiply, 6: u32->f32
- * conversion). */
+ * conversion, 7: s32->f32 conversion). */
 int sb_probe_arith_rate(int kind, double* ops_per_s);
 
 #ifdef __cplusplus

@@ -28,8 +28,12 @@
 
 #if defined(__CUDACC__)
 #define SB_HD __host__ __device__ __forceinline__
+// rare paths that run on the fp64 pipe: out of line, so the compiler cannot
+// evaluate them speculatively on every element of the common path
+#define SB_HD_COLD static __host__ __device__ __noinline__
 #else
 #define SB_HD inline
+#define SB_HD_COLD static inline
 #endif
 
 namespace sb {
@@ -152,6 +156,9 @@ SB_HD f32x2 two_prod(float a, float b) {
 
 // ---- conversions --------------------------------------------------------------
 
+SB_HD_COLD f32x2 f32x2_from_double_rare(double x) { return {fx::narrow(x), 0.0f}; }
+SB_HD_COLD double f32x2_to_double_rare(float hi, float lo) { return fx::widen(hi) + fx::widen(lo); }
+
 // float64 -> pair, integer operations only on the common path.  With the
 // 53-bit significand M (implicit bit included) of |x| = M * 2^(E-1075):
 // hi = round(M / 2^29) * 2^(E-1046) (the rounding carry moves into the
@@ -176,7 +183,7 @@ SB_HD f32x2 f32x2_from_double(double x) {
         }
         return {hi, fx::u2f(fx::f2u(lo) ^ sign)};
     }
-    return {fx::narrow(x), 0.0f};  // zero, subnormal, tiny, huge, inf, nan
+    return f32x2_from_double_rare(x);  // zero, subnormal, tiny, huge, inf, nan
 }
 
 // pair -> float64 (hi + lo, within one unit in the last place of float64),
@@ -215,7 +222,7 @@ SB_HD double f32x2_to_double(f32x2 a) {
                            ((uint64_t)H & ((1ull << 52) - 1)));
         }
     }
-    return fx::widen(a.hi) + fx::widen(a.lo);  // zero, subnormal, inf, nan
+    return f32x2_to_double_rare(a.hi, a.lo);  // zero, subnormal, inf, nan
 }
 
 SB_HD f32x2 f32x2_from_float(float x) { return {x, 0.0f}; }

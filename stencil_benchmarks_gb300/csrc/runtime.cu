@@ -119,6 +119,16 @@ __global__ void arith_probe_kernel(double* out, int iters, double x) {
         unsigned s = 0;
         for (int u = 0; u < 8; ++u) s += a[u];
         if (s == 12345u) out[0] = s;
+    } else if (KIND == 7) {  // s32 -> f32 conversion (the way back is an integer move)
+        float a[8];
+        for (int u = 0; u < 8; ++u) a[u] = (float)x + (float)(threadIdx.x + u);
+        for (int it = 0; it < iters; ++it) {
+#pragma unroll
+            for (int u = 0; u < 8; ++u) a[u] = __int2float_rn(__float_as_int(a[u]) ^ it);
+        }
+        float s = 0.f;
+        for (int u = 0; u < 8; ++u) s += a[u];
+        if (s == 12345.678f) out[0] = s;
     } else if (KIND == 6) {  // u32 -> f32 conversion (the way back is an integer move)
         float a[8];
         for (int u = 0; u < 8; ++u) a[u] = (float)x + (float)(threadIdx.x + u);
@@ -338,7 +348,7 @@ int sb_l2_flush(void* stream) {
 }
 
 int sb_probe_arith_rate(int kind, double* ops_per_s) {
-    SB_CHECK(kind >= 0 && kind <= 6 && ops_per_s, SB_ERR_INVALID, "bad probe arguments");
+    SB_CHECK(kind >= 0 && kind <= 7 && ops_per_s, SB_ERR_INVALID, "bad probe arguments");
     const DeviceProps* p;
     int rc = device_props(&p);
     if (rc) return rc;
@@ -353,6 +363,7 @@ int sb_probe_arith_rate(int kind, double* ops_per_s) {
         if (kind == 4) arith_probe_kernel<4><<<blocks, threads>>>(out, iters, 0.5);
         if (kind == 5) arith_probe_kernel<5><<<blocks, threads>>>(out, iters, 0.5);
         if (kind == 6) arith_probe_kernel<6><<<blocks, threads>>>(out, iters, 0.5);
+        if (kind == 7) arith_probe_kernel<7><<<blocks, threads>>>(out, iters, 0.5);
         return SB_OK;
     };
     double t = 0.0;
