@@ -503,14 +503,14 @@ def run_batched(seed=3, n_domains=64, storage="float32", reps=5):
     }
 
 
-def run_served(n_requests=2000, rates=(1000.0, 5000.0, 20000.0), seed=11):
+def run_served(n_requests=2000, rates=(1000.0, 5000.0, 20000.0), seed=11, float64_compute="float64"):
     """Continuous-batching server under Poisson arrivals (mixed hdiff/vadv,
     sizes log-uniform 32..1024, nk 40..137, fp64/fp32/bf16 at 20/60/20 %,
     150 GB budget).  The full 10,000-request sweep is
     ``python -m stencil_benchmarks_gb300.serving``."""
     from stencil_benchmarks_gb300 import serving
 
-    server = serving.Server(budget_bytes=150e9, max_batch=64, slots_per_form=3)
+    server = serving.Server(budget_bytes=150e9, max_batch=64, slots_per_form=3, float64_compute=float64_compute)
     serving.run_load(server, serving.request_specs(64, seed=seed + 1000), rate=1e6)  # warm-up
     out = []
     for rate in rates:
@@ -663,6 +663,10 @@ def main(argv=None):
             line["batched"] = run_batched()
         if not args.no_served:
             line["served"] = run_served()
+            line["served_fast_f64"] = {
+                "what": "float64 requests with fixed-point hdiff and float-pair vadv (within 1e-12 / 1e-10 of "
+                        "the field scale); float32 and bfloat16 requests unchanged",
+                "rates": run_served(rates=(5000.0, 20000.0), float64_compute="fixed64")}
         if not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline_sample()
         print(json.dumps(line), flush=True)

@@ -206,16 +206,25 @@ class _Slot:
 
 class Server:
     def __init__(self, budget_bytes: float = 150e9, max_batch: int = 64, max_nk: int = 137, slots_per_form: int = 3,
-                 keep_outputs: bool = False, batch_tune: Optional[dict] = None, fill_capacity: int = 4096):
+                 keep_outputs: bool = False, batch_tune: Optional[dict] = None, fill_capacity: int = 4096,
+                 float64_compute: str = "float64"):
+        """``float64_compute`` picks how float64 requests are computed: "float64"
+        (exact, bit-identical to the reference's numpy) or "fixed64" (fixed-point
+        hdiff and float-pair vadv: errors within 1e-12 / 1e-10 of the field scale,
+        about 3x less device time)."""
+        if float64_compute not in ("float64", "fixed64"):
+            raise ValueError("float64_compute must be 'float64' or 'fixed64'")
         _native.call("sb_set_device", 0)
         self.pool = DevicePool(int(budget_bytes))
         self.max_batch, self.max_nk = max_batch, max_nk
         self.keep_outputs = keep_outputs
+        self.float64_compute = float64_compute
         tune = dict(batch_tune or {})
+        forms = dict(FORMS, float64=("float64", float64_compute))
         self.slots = {
             form: [_Slot(Batch(s, c, max_domains=max_batch, max_nk=max_nk, **tune), Stream(), Event())
                    for _ in range(slots_per_form)]
-            for form, (s, c) in FORMS.items()
+            for form, (s, c) in forms.items()
         }
         self.waiting: collections.deque = collections.deque()
         self.ready = {form: collections.deque() for form in FORMS}
@@ -406,8 +415,11 @@ def main(argv=None):
     ap.add_argument("--max-batch", type=int, default=64)
     ap.add_argument("--slots", type=int, default=3)
     ap.add_argument("--seed", type=int, default=11)
+    ap.add_argument("--float64-compute", choices=["float64", "fixed64"], default="float64",
+                    help="float64 requests: exact (float64) or fixed-point hdiff / float-pair vadv (fixed64)")
     args = ap.parse_args(argv)
-    server = Server(budget_bytes=args.budget_gb * 1e9, max_batch=args.max_batch, slots_per_form=args.slots)
+    server = Server(budget_bytes=args.budget_gb * 1e9, max_batch=args.max_batch, slots_per_form=args.slots,
+                    float64_compute=args.float64_compute)
     warm = request_specs(64, seed=args.seed + 1000)
     run_load(server, warm, rate=1e6)
     for rate in (float(r) for r in args.rates.split(",")):

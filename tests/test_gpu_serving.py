@@ -115,3 +115,28 @@ def test_budget_bounded_load(lib):
     assert srv.pool.peak <= srv.pool.budget
     assert stats["p99_ms"] >= stats["p50_ms"] > 0
     assert srv.pool.in_use == 0
+
+
+def test_fast_float64_serving_within_tolerance(lib):
+    """float64 requests served with fixed-point hdiff and float-pair vadv:
+    within 1e-12 (hdiff) / 1e-10 (vadv) of the field scale of the oracle,
+    and the same bits alone and in a mix."""
+    reqs = [r for r in _small_mix(30, 10) if r.storage == "float64"]
+    assert reqs
+    srv = serving.Server(budget_bytes=8e9, max_batch=6, max_nk=48, slots_per_form=2, keep_outputs=True,
+                         float64_compute="fixed64")
+    for r in reqs:
+        srv.submit(r)
+    srv.drain()
+    for r in reqs:
+        got, want = download_output(r), expected_output(r)
+        scale = float(np.max(np.abs(want)))
+        tol = 1e-12 if r.op == "hdiff" else 1e-10
+        assert float(np.max(np.abs(got - want))) <= tol * scale, r
+    probe = reqs[0]
+    twin = serving.Request(999, probe.op, probe.ni, probe.nj, probe.nk, "float64", probe.seed)
+    alone = serving.Server(budget_bytes=4e9, max_batch=4, max_nk=48, slots_per_form=1, keep_outputs=True,
+                           float64_compute="fixed64")
+    alone.submit(twin)
+    alone.drain()
+    assert bits_equal(download_output(twin), download_output(probe))
