@@ -73,6 +73,11 @@ extern "C" {
                            * the caller's ccol/dcol (L2-resident), cp.async staging;
                            * tune: block_x 32/64, unroll = depth 2/4/8, k_per_cta =
                            * blocks per SM (0: as many as fit with slabs <= L2/2)  */
+#define SB_VADV_WSLAB 4   /* SLAB with each warp's 32-column rows staged together in
+                           * 16-byte copies (needs i unit-stride); same tune fields.
+                           * SB_VARIANT_AUTO with ccol/dcol given and no block/unroll
+                           * in the tune picks WSLAB for 2/4-byte storage and SLAB
+                           * for 8-byte storage when the layout qualifies */
 
 /*
  * Launch tuning.  Zero in any field means "choose the default".  The

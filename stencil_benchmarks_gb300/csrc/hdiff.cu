@@ -246,6 +246,10 @@ extern "C" int sb_hdiff(int storage, int compute, const void* inp, const void* c
     int rc = check_domain(ni, nj, nk, si, sj, sk);
     if (rc) return rc;
     SB_CHECK(inp && coeff && out, SB_ERR_INVALID, "NULL field pointer");
+    SB_CHECK((storage == SB_F64 && (compute == SB_F64 || compute == SB_F32X2 || compute == SB_FIX64)) ||
+                 (storage == SB_F32 && (compute == SB_F32 || compute == SB_F64)) ||
+                 (storage == SB_BF16 && compute == SB_F32),
+             SB_ERR_UNSUPPORTED, "unsupported storage/compute combination (%d, %d)", storage, compute);
     if (ni == 0 || nj == 0 || nk == 0) {
         if (time_s) *time_s = 0.0;
         return SB_OK;

@@ -575,4 +575,210 @@ __device__ __forceinline__ void vadv_async_column(const S* __restrict__ stage, c
     cp_async_wait<0>();
 }
 
+// ---------------------------------------------------------------------------
+// vertical advection, one warp, 32 consecutive columns, rows staged together
+// ---------------------------------------------------------------------------
+// With i unit-stride the level-k inputs of a warp's 32 columns are six
+// contiguous rows.  The warp copies each row's 16-byte-aligned span with
+// 16-byte cp.async chunks and spreads the chunks of all six rows over its
+// lanes, so a level costs ceil(6 * CPR / 32) copy instructions per lane
+// (2 for float32) instead of six; each lane then waits for its own copies and
+// __syncwarp makes the others' visible.  A chunk always contains a byte of
+// the row, so it never leaves the row's aligned 16-byte granules.  Factors go
+// to the thread's compact slab (level stride fs) and come back through the
+// same ring (rows pos, ccol, dcol) in the backward sweep.  All 32 lanes call
+// this; lanes at or past `nvalid` compute on stale ring bytes, load their
+// direct values from the last valid column and store nothing.
+template <class S, class C, int D>
+struct WarpRing {
+    static constexpr int ES = sizeof(S);
+    static constexpr int WB = ES > (int)sizeof(C) ? ES : (int)sizeof(C);
+    static constexpr int ROWB = (32 * WB + 16 + 15) / 16 * 16;  // one row's aligned span, at most
+    static constexpr int CPR = ROWB / 16;                        // 16-byte chunks per row, at most
+    static constexpr int R = D + 1;
+    static constexpr int SLOT = 6 * ROWB;
+    static constexpr int BYTES = R * SLOT;  // ring bytes per warp
+};
+
+template <class S, class C, int D, class IDX>
+__device__ __forceinline__ void vadv_warp_column(const S* __restrict__ stage, const S* __restrict__ pos,
+                                                 const S* __restrict__ tens, const S* tensstage,
+                                                 const S* __restrict__ wcon, S* out, IDX col0, int lane,
+                                                 int nvalid, int nk, IDX sk, IDX wsh, C* slab_c0, C* slab_d0,
+                                                 int64_t fs, unsigned char* ring) {
+    using A = Ar<C>;
+    using W = WarpRing<S, C, D>;
+    constexpr int R = W::R, ES = W::ES, CPR = W::CPR, ROWB = W::ROWB, SLOT = W::SLOT;
+    constexpr int MF = (6 * CPR + 31) / 32;  // forward chunks per lane
+    constexpr int MB = (3 * CPR + 31) / 32;  // backward chunks per lane
+    const C dtr = konst<C>(3.0 / 20.0);
+    const bool valid = lane < nvalid;
+    const IDX col = col0 + (IDX)(valid ? lane : nvalid - 1);
+    C* sc = slab_c0 + lane;
+    C* sd = slab_d0 + lane;
+    const int64_t kstep = (int64_t)sk * ES;  // bytes from level k to k+1 in a field
+    const int nbytes = nvalid * ES;
+
+    // forward rows at level k: wcon(k+1) shifted, wcon(k+1), stage(k+1), pos(k), tens(k), tensstage(k)
+    const unsigned char* const g0 = (const unsigned char*)(wcon + col0 + sk + wsh);
+    const unsigned char* const g1 = (const unsigned char*)(wcon + col0 + sk);
+    const unsigned char* const g2 = (const unsigned char*)(stage + col0 + sk);
+    const unsigned char* const g3 = (const unsigned char*)(pos + col0);
+    const unsigned char* const g4 = (const unsigned char*)(tens + col0);
+    const unsigned char* const g5 = (const unsigned char*)(tensstage + col0);
+    auto gsel = [&](int r) -> const unsigned char* {  // r is per lane: selects, not an indexed array
+        return r == 0 ? g0 : r == 1 ? g1 : r == 2 ? g2 : r == 3 ? g3 : r == 4 ? g4 : g5;
+    };
+    unsigned mis0[6];
+#pragma unroll
+    for (int f = 0; f < 6; ++f) mis0[f] = (unsigned)((uintptr_t)gsel(f) & 15u);
+    // this lane's chunks: slot s = lane + 32 m -> row s / CPR, chunk s % CPR
+    const unsigned char* cg[MF];
+    int cdst[MF], cidx[MF];
+#pragma unroll
+    for (int m = 0; m < MF; ++m) {
+        const int sidx = lane + 32 * m, r = sidx / CPR;
+        cidx[m] = r < 6 ? sidx % CPR : CPR;  // CPR = never issued
+        cdst[m] = (r < 6 ? r : 0) * ROWB + (sidx % CPR) * 16;
+        cg[m] = gsel(r < 6 ? r : 0);
+    }
+    auto issue = [&](int slot, int k) {
+        if (k < nk - 1) {  // uniform
+            const int64_t kb = (int64_t)k * kstep;
+#pragma unroll
+            for (int m = 0; m < MF; ++m) {
+                const uintptr_t a = (uintptr_t)(cg[m] + kb);
+                const int n = (int)(((a & 15u) + (unsigned)nbytes + 15u) >> 4);
+                if (cidx[m] < n)
+                    cp_async<16>(ring + slot * SLOT + cdst[m], (const void*)((a & ~(uintptr_t)15) + 16 * cidx[m]));
+            }
+        }
+        cp_async_commit();
+    };
+    auto row = [&](int slot, int f, unsigned kmis) -> const S* {
+        return (const S*)(ring + slot * SLOT + f * ROWB + ((mis0[f] + kmis) & 15u)) + lane;
+    };
+    // level L is staged in slot (L-1) % R
+#pragma unroll
+    for (int u = 0; u < D; ++u) issue(u, 1 + u);
+
+    // ---- forward sweep, k = 0 (direct loads)
+    C gcv = A::template scale2<-2>(A::add(ld<C, S>(wcon + col + sk + wsh), ld<C, S>(wcon + col + sk)));
+    C cs = A::template scale2<-1>(gcv);
+    C sprev = ld<C, S>(stage + col);
+    C scur = ld<C, S>(stage + col + sk);
+    C dup = A::sub(scur, sprev);
+    C bcol = A::sub(dtr, cs);
+    C corr = A::mul(-cs, dup);
+    C dv = A::add(A::add(A::add(A::mul(dtr, ld<C, S>(pos + col)), ld<C, S>(tens + col)), ldc<C, S>(tensstage + col)), corr);
+    C cp = A::div(cs, bcol);
+    C dp = A::div(dv, bcol);
+    sc[0] = cp;
+    sd[0] = dp;
+
+    // ---- forward sweep, 0 < k < nk-1
+    for (int kb = 1; kb < nk - 1; kb += R) {
+#pragma unroll
+        for (int u = 0; u < R; ++u) {
+            const int k = kb + u;
+            if (k >= nk - 1) break;  // uniform
+            cp_async_wait<D - 1>();
+            __syncwarp();
+            const unsigned kmis = (unsigned)(((int64_t)k * kstep) & 15);
+            const C w1 = cvt<C, S>(*row(u, 0, kmis)), w0 = cvt<C, S>(*row(u, 1, kmis));
+            const C snext = cvt<C, S>(*row(u, 2, kmis)), p0 = cvt<C, S>(*row(u, 3, kmis));
+            const C t0 = cvt<C, S>(*row(u, 4, kmis)), ts0 = cvt<C, S>(*row(u, 5, kmis));
+            issue((u + D) % R, k + D);  // the slot of level k-1: every lane has read it (__syncwarp above)
+            const C as_ = A::template scale2<-1>(-gcv);
+            gcv = A::template scale2<-2>(A::add(w1, w0));
+            cs = A::template scale2<-1>(gcv);
+            const C ddown = A::neg_diff(dup, scur, sprev);
+            dup = A::sub(snext, scur);
+            bcol = A::sub(A::sub(dtr, as_), cs);
+            corr = A::sub(A::mul(-as_, ddown), A::mul(cs, dup));
+            dv = A::add(A::add(A::add(A::mul(dtr, p0), t0), ts0), corr);
+            const C divided = A::rcp(A::sub(bcol, A::mul(cp, as_)));
+            cp = A::mul(cs, divided);
+            dp = A::mul(A::sub(dv, A::mul(dp, as_)), divided);
+            sc[k * fs] = cp;
+            sd[k * fs] = dp;
+            sprev = scur;
+            scur = snext;
+        }
+    }
+    cp_async_wait<0>();
+    // every lane's slab stores are read back by other lanes' copies
+    __threadfence_block();
+    __syncwarp();
+
+    // ---- forward sweep, k = nk-1
+    {
+        const IDX o = col + (IDX)(nk - 1) * sk;
+        const C as_ = A::template scale2<-1>(-gcv);
+        bcol = A::sub(dtr, as_);
+        const C ddown = A::neg_diff(dup, scur, sprev);
+        corr = A::mul(-as_, ddown);
+        dv = A::add(A::add(A::add(A::mul(dtr, ld<C, S>(pos + o)), ld<C, S>(tens + o)), ldc<C, S>(tensstage + o)), corr);
+        dp = A::div(A::sub(dv, A::mul(dp, as_)), A::sub(bcol, A::mul(cp, as_)));
+    }
+
+    // ---- backward sweep: rows pos(k), ccol(k), dcol(k) of level k in slot (nk-2-k) % R
+    const unsigned char* const gb0 = (const unsigned char*)(pos + col0);
+    const unsigned char* const gb1 = (const unsigned char*)slab_c0;
+    const unsigned char* const gb2 = (const unsigned char*)slab_d0;
+    const int64_t fstep = fs * (int64_t)sizeof(C);  // bytes from level k to k+1 in a slab
+    const int fbytes = nvalid * (int)sizeof(C);
+    const unsigned char* bg[MB];
+    int bdst[MB], bidx[MB], brow[MB];
+#pragma unroll
+    for (int m = 0; m < MB; ++m) {
+        const int sidx = lane + 32 * m, r = sidx / CPR;
+        bidx[m] = r < 3 ? sidx % CPR : CPR;
+        brow[m] = r < 3 ? r : 0;
+        bdst[m] = brow[m] * ROWB + (sidx % CPR) * 16;
+        bg[m] = brow[m] == 0 ? gb0 : brow[m] == 1 ? gb1 : gb2;
+    }
+    auto issue_b = [&](int slot, int k) {
+        if (k >= 0) {
+#pragma unroll
+            for (int m = 0; m < MB; ++m) {
+                const int64_t st_ = brow[m] == 0 ? kstep : fstep;
+                const int nb_ = brow[m] == 0 ? nbytes : fbytes;
+                const uintptr_t a = (uintptr_t)(bg[m] + (int64_t)k * st_);
+                const int n = (int)(((a & 15u) + (unsigned)nb_ + 15u) >> 4);
+                if (bidx[m] < n)
+                    cp_async<16>(ring + slot * SLOT + bdst[m], (const void*)((a & ~(uintptr_t)15) + 16 * bidx[m]));
+            }
+        }
+        cp_async_commit();
+    };
+#pragma unroll
+    for (int u = 0; u < D; ++u) issue_b(u, nk - 2 - u);
+    C data = dp;
+    if (valid) {
+        const IDX o = col + (IDX)(nk - 1) * sk;
+        st<S, C>(out + o, A::mul(dtr, A::sub(data, ld<C, S>(pos + o))));
+    }
+    const unsigned mis_p = (unsigned)((uintptr_t)gb0 & 15u);
+    const unsigned mis_c = (unsigned)((uintptr_t)gb1 & 15u), mis_d = (unsigned)((uintptr_t)gb2 & 15u);
+    for (int kb = nk - 2; kb >= 0; kb -= R) {
+#pragma unroll
+        for (int u = 0; u < R; ++u) {
+            const int k = kb - u;
+            if (k < 0) break;
+            cp_async_wait<D - 1>();
+            __syncwarp();
+            const unsigned char* sl = ring + u * SLOT;
+            const unsigned kp = (unsigned)(((int64_t)k * kstep) & 15), kf = (unsigned)(((int64_t)k * fstep) & 15);
+            const C p0 = cvt<C, S>(((const S*)(sl + ((mis_p + kp) & 15u)))[lane]);
+            const C cv = ((const C*)(sl + ROWB + ((mis_c + kf) & 15u)))[lane];
+            const C dvk = ((const C*)(sl + 2 * ROWB + ((mis_d + kf) & 15u)))[lane];
+            issue_b((u + D) % R, k - D);
+            data = A::sub(dvk, A::mul(cv, data));
+            if (valid) st<S, C>(out + (col + (IDX)k * sk), A::mul(dtr, A::sub(data, p0)));
+        }
+    }
+    cp_async_wait<0>();
+}
+
 }  // namespace sb

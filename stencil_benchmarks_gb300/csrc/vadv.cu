@@ -29,6 +29,7 @@
 //            same names), for columns too tall for shared memory.
 // The backward sweep reads them back in reverse order.
 #include <algorithm>
+#include <type_traits>
 
 #include "stencil_core.cuh"
 
@@ -109,6 +110,33 @@ __global__ void __launch_bounds__(BT)
             vadv_async_column<S, C, BT, D, int, true>(stage, pos, tens, tensstage, wcon, out, i * si + j * sj, nk, sk,
                                                       wsh, slab_c + slot, slab_d + slot, ring, nslots);
         }
+    }
+}
+
+// WSLAB variant: the SLAB scheme with the rows of each warp's 32 columns
+// staged together (vadv_warp_column): fewer, wider copies per level.  Needs
+// i unit-stride.  Each block's warps take 32-column pieces of one
+// BT-column group.
+template <class S, class C, int W, int D>
+__global__ void __launch_bounds__(32 * W)
+    vadv_wslab_kernel(const S* __restrict__ stage, const S* __restrict__ pos, const S* __restrict__ tens,
+                      const S* tensstage, const S* __restrict__ wcon, S* out, C* __restrict__ slab_c,
+                      C* __restrict__ slab_d, int ni, int nj, int nk, int sj, int sk, int wsh) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    constexpr int BT = 32 * W;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    unsigned char* ring = smem_raw + warp * WarpRing<S, C, D>::BYTES;
+    const int64_t nslots = (int64_t)gridDim.x * BT;
+    const int64_t slot0 = (int64_t)blockIdx.x * BT + warp * 32;
+    const int gx = (ni + BT - 1) / BT;
+    const int64_t ngroups = (int64_t)gx * nj;
+    for (int64_t g = blockIdx.x; g < ngroups; g += gridDim.x) {
+        const int i0 = (int)(g % gx) * BT + warp * 32;
+        const int j = (int)(g / gx);
+        const int nvalid = min(32, ni - i0);
+        if (nvalid <= 0) continue;  // warp-uniform
+        vadv_warp_column<S, C, D, int>(stage, pos, tens, tensstage, wcon, out, i0 + j * sj, lane, nvalid, nk, sk, wsh,
+                                       slab_c + slot0, slab_d + slot0, nslots, ring);
     }
 }
 
@@ -251,6 +279,60 @@ int launch_slab(int bx, int depth, int blocks_per_sm, const DeviceProps* p, cuda
     }
 }
 
+template <class S, class C, int W, int D>
+int launch_wslab_one(int blocks_per_sm, const DeviceProps* p, cudaStream_t stream, const void* stage,
+                     const void* pos, const void* tens, const void* tensstage, const void* wcon, void* out,
+                     void* ccol, void* dcol, int64_t ni, int64_t nj, int64_t nk, int64_t si, int64_t sj, int64_t sk,
+                     int64_t wsh) {
+    constexpr int BT = 32 * W;
+    auto kernel = vadv_wslab_kernel<S, C, W, D>;
+    const size_t smem = (size_t)W * WarpRing<S, C, D>::BYTES;
+    if (smem > 48 * 1024) SB_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int fit = 0;
+    SB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fit, kernel, BT, smem));
+    int per_sm = std::max(1, fit);
+    if (blocks_per_sm > 0) {
+        per_sm = std::min(per_sm, blocks_per_sm);
+    } else {
+        const int64_t per_block = 2 * nk * (int64_t)sizeof(C) * BT * p->sm_count;
+        const int64_t budget = (int64_t)(p->l2_bytes > 0 ? p->l2_bytes : (128 << 20)) / 2;
+        per_sm = (int)std::max<int64_t>(1, std::min<int64_t>(per_sm, budget / std::max<int64_t>(1, per_block)));
+    }
+    const int64_t ngroups = ceil_div(ni, BT) * nj;
+    const int64_t span = (ni - 1) * si + (nj - 1) * sj + (nk - 1) * sk + 1;
+    int64_t grid = std::min<int64_t>((int64_t)per_sm * p->sm_count, ngroups);
+    grid = std::min<int64_t>(grid, span / (nk * BT));
+    if (grid < 1) return SB_ERR_UNSUPPORTED;
+    kernel<<<(unsigned)grid, BT, smem, stream>>>((const S*)stage, (const S*)pos, (const S*)tens, (const S*)tensstage,
+                                                 (const S*)wcon, (S*)out, (C*)ccol, (C*)dcol, (int)ni, (int)nj,
+                                                 (int)nk, (int)sj, (int)sk, (int)wsh);
+    return SB_OK;
+}
+
+// WSLAB variant if this launch qualifies (ccol/dcol given, i unit-stride,
+// positive strides, 32-bit offsets); SB_ERR_UNSUPPORTED otherwise.
+template <class S, class C>
+int launch_wslab(int bx, int depth, int blocks_per_sm, const DeviceProps* p, cudaStream_t stream,
+                 const void* stage, const void* pos, const void* tens, const void* tensstage, const void* wcon,
+                 void* out, void* ccol, void* dcol, int64_t ni, int64_t nj, int64_t nk, int64_t si, int64_t sj,
+                 int64_t sk, int64_t wsh) {
+    if (!ccol || !dcol || si != 1 || sj <= 0 || sk <= 0) return SB_ERR_UNSUPPORTED;
+    const int64_t span = (ni + 1) * si + nj * sj + (nk + 1) * sk;
+    if (span >= (1LL << 31) || (int64_t)ni * nj * nk >= (1LL << 31)) return SB_ERR_UNSUPPORTED;
+#define SB_VADV_WSLAB_CASE(WV, DV)                                                                               \
+    if (bx == 32 * WV && depth == DV)                                                                            \
+        return launch_wslab_one<S, C, WV, DV>(blocks_per_sm, p, stream, stage, pos, tens, tensstage, wcon, out, \
+                                              ccol, dcol, ni, nj, nk, si, sj, sk, wsh);
+    SB_VADV_WSLAB_CASE(1, 2)
+    SB_VADV_WSLAB_CASE(1, 4)
+    SB_VADV_WSLAB_CASE(1, 8)
+    SB_VADV_WSLAB_CASE(2, 2)
+    SB_VADV_WSLAB_CASE(2, 4)
+    SB_VADV_WSLAB_CASE(2, 8)
+#undef SB_VADV_WSLAB_CASE
+    return SB_ERR_UNSUPPORTED;
+}
+
 template <class S, class C>
 int launch_typed(const void* stage, const void* pos, const void* tens, const void* tensstage,
                  const void* wcon, void* out, void* ccol, void* dcol, int64_t ni, int64_t nj, int64_t nk,
@@ -265,9 +347,35 @@ int launch_typed(const void* stage, const void* pos, const void* tens, const voi
     SB_CHECK(bx * by <= 256 && bx >= 1 && by >= 1, SB_ERR_INVALID, "vadv block (%d, %d) exceeds 256 threads", bx, by);
     const size_t smem = 2 * sizeof(C) * (size_t)nk * (size_t)(bx * by);
     const bool can_global = ccol && dcol && sizeof(S) == sizeof(C);
+    if (variant == SB_VARIANT_AUTO && ccol && dcol && !(tune && (tune->block_x || tune->block_y || tune->unroll))) {
+        // scratch fields given and no explicit shape: the persistent slab forms
+        // (row-staged for 2- and 4-byte storage), falling back below if the
+        // layout does not qualify
+        const int arc = sizeof(S) <= 4
+                            ? launch_wslab<S, C>(32, 4, 0, p, stream, stage, pos, tens, tensstage, wcon, out, ccol,
+                                                 dcol, ni, nj, nk, si, sj, sk, wsh)
+                            : (std::is_same<C, double>::value
+                                   ? launch_slab<S, C>(32, 4, 8, p, stream, stage, pos, tens, tensstage, wcon, out,
+                                                       ccol, dcol, ni, nj, nk, si, sj, sk, wsh)
+                                   : launch_slab<S, C>(64, 2, 32, p, stream, stage, pos, tens, tensstage, wcon, out,
+                                                       ccol, dcol, ni, nj, nk, si, sj, sk, wsh));
+        if (arc != SB_ERR_UNSUPPORTED) return arc;
+    }
     if (variant == SB_VARIANT_AUTO) variant = ((int64_t)smem <= p->smem_optin) ? SB_VADV_SMEM : SB_VADV_GLOBAL;
-    SB_CHECK(variant == SB_VADV_SMEM || variant == SB_VADV_GLOBAL || variant == SB_VADV_SLAB, SB_ERR_UNSUPPORTED,
-             "vadv variant %d is not available", variant);
+    SB_CHECK(variant == SB_VADV_SMEM || variant == SB_VADV_GLOBAL || variant == SB_VADV_SLAB ||
+                 variant == SB_VADV_WSLAB,
+             SB_ERR_UNSUPPORTED, "vadv variant %d is not available", variant);
+    if (variant == SB_VADV_WSLAB) {
+        SB_CHECK(ccol && dcol, SB_ERR_INVALID, "vadv WSLAB variant needs ccol/dcol scratch fields");
+        const int d = (tune && tune->unroll > 0) ? tune->unroll : 4;
+        const int bpsm = tune ? tune->k_per_cta : 0;
+        const int rc2 = launch_wslab<S, C>(bx, d, bpsm, p, stream, stage, pos, tens, tensstage, wcon, out, ccol, dcol,
+                                           ni, nj, nk, si, sj, sk, wsh);
+        SB_CHECK(rc2 != SB_ERR_UNSUPPORTED, SB_ERR_UNSUPPORTED,
+                 "vadv WSLAB variant: needs blocks of 32 or 64 threads, depth 2, 4 or 8, i unit-stride, positive "
+                 "strides and 32-bit offsets");
+        return rc2;
+    }
     if (variant == SB_VADV_SLAB) {
         SB_CHECK(ccol && dcol, SB_ERR_INVALID, "vadv SLAB variant needs ccol/dcol scratch fields");
         const int d = (tune && tune->unroll > 0) ? tune->unroll : 4;
@@ -314,6 +422,10 @@ extern "C" int sb_vadv(int storage, int compute, const void* stage, const void* 
     SB_CHECK(stage && pos && tens && tensstage && wcon && out, SB_ERR_INVALID, "NULL field pointer");
     SB_CHECK(wshift_i >= 0 && wshift_i <= 1 && wshift_j >= 0 && wshift_j <= 1 && wshift_i + wshift_j <= 1,
              SB_ERR_INVALID, "wcon shift must be (1,0), (0,1) or (0,0)");
+    SB_CHECK((storage == SB_F64 && (compute == SB_F64 || compute == SB_F32X2)) ||
+                 (storage == SB_F32 && (compute == SB_F32 || compute == SB_F64)) ||
+                 (storage == SB_BF16 && compute == SB_F32),
+             SB_ERR_UNSUPPORTED, "unsupported storage/compute combination (%d, %d)", storage, compute);
     if (ni == 0 || nj == 0 || nk == 0) {
         if (time_s) *time_s = 0.0;
         return SB_OK;

@@ -212,16 +212,18 @@ def test_vadv_variants(variant, bx, by, depth, storage, compute, lib):
         _assert_bits(got, want, f"vadv variant {variant} {bx}x{by} depth {depth} nk {nk}")
 
 
+@pytest.mark.parametrize("variant", [_native.VADV_SLAB, _native.VADV_WSLAB])
 @pytest.mark.parametrize("bx,depth,per_sm", [(32, 4, 0), (64, 2, 0), (32, 8, 1), (64, 4, 3)])
 @pytest.mark.parametrize("storage,compute", [("float64", "float64"), ("float32", "float32"),
                                              ("bfloat16", "float32")])
-def test_vadv_slab(bx, depth, per_sm, storage, compute, lib):
-    """Persistent SLAB variant: factors in compact slabs of ccol/dcol; few
-    blocks per SM make every thread solve many columns in turn."""
-    t = _native.tune(variant=_native.VADV_SLAB, block_x=bx, unroll=depth, k_per_cta=per_sm)
+def test_vadv_slab(variant, bx, depth, per_sm, storage, compute, lib):
+    """Persistent SLAB / WSLAB variants: factors in compact slabs of
+    ccol/dcol; few blocks per SM make every thread solve many columns in
+    turn; row ends leave warps with 1 or 2 valid lanes (WSLAB)."""
+    t = _native.tune(variant=variant, block_x=bx, unroll=depth, k_per_cta=per_sm)
     for domain in ((97, 19, 2), (97, 19, 3), (33, 40, 9), (130, 7, 41)):
         got, want = _run_vadv(domain, (1, 1, 0), storage, compute, tune=t, seed=17 + domain[2], use_scratch=True)
-        _assert_bits(got, want, f"vadv slab {bx} depth {depth} per_sm {per_sm} {domain}")
+        _assert_bits(got, want, f"vadv slab {variant} {bx} depth {depth} per_sm {per_sm} {domain}")
 
 
 @pytest.mark.parametrize(
