@@ -222,13 +222,16 @@ int sb_batch_destroy(sb_batch* batch);
  * No counterpart in the reference (it runs one benchmark at a time).
  * sb_fill_batch: fill n device fields in one launch with seeded uniform values
  * in [lo, hi), generated without fp64 arithmetic on the device.  With H the
- * 32-bit lowbias32 hash, k0/k1 the low/high words of seed and e the element:
- *   h1 = H(H(lo32(e) ^ k0) ^ (k1 ^ hi32(e) * 0x9E3779B9))
- *   float32 / bfloat16:  v = lo_f + span_f * ((h1 >> 8) * 2^-24)  in float32
- *                        (lo_f = (float)lo, span_f = (float)(hi - lo)), then
- *                        rounded to bfloat16 for bfloat16 storage;
- *   float64:  h2 = H(h1 ^ (k0 + 0x632BE5AB)), k = h1 << 21 | h2 >> 11,
- *             v = lo + (hi - lo) * (k * 2^-53)  in double;
+ * 32-bit lowbias32 hash and, per field, k0 = H(lo32(seed) ^ 0xA511E9B3) | 1,
+ * k1 = H(hi32(seed) + 0x632BE5AB), k2 = H(k0 ^ k1),
+ * x(n) = lo32(n) * k0 + k1 + hi32(n) * 0x9E3779B9 (32-bit arithmetic):
+ *   float32:  v[e] = lo_f + span_f * ((H(x(e)) >> 8) * 2^-24)  in float32
+ *             (lo_f = (float)lo, span_f = (float)(hi - lo));
+ *   bfloat16: h = H(x(e / 2)); v[e] = lo_f + span_f * (b * 2^-16) in float32
+ *             with b = h & 0xFFFF for even e, h >> 16 for odd e, then
+ *             rounded to bfloat16;
+ *   float64:  h1 = H(x(e)), h2 = H(h1 ^ k2), k = h1 << 21 | h2 >> 11,
+ *             v[e] = lo + (hi - lo) * (k * 2^-53)  in double;
  * each operation rounded to nearest even, no fused multiply-add.  The
  * descriptors are copied (asynchronously on
  * `stream`, from the caller's host memory, which must stay valid until the

@@ -4,17 +4,21 @@
 // from a counter-based generator, so request fields are created where they
 // are used (no host->device copy) and are reproducible on the host.  The
 // generator avoids fp64 arithmetic (the fp64 pipe runs at 1/73 of the fp32
-// rate here): a 32-bit hash per element, float32 arithmetic for float32 and
-// bfloat16 fields, and for float64 fields an exact integer construction of
-// lo + (hi - lo) * u whenever hi - lo is a power of two and lo is 0 or
-// -(hi - lo)/2 (the fp64 formula otherwise; both give the same bits).  With
-// H the lowbias32 hash (C. Wellons, "Prospecting for hash functions", 2018),
-// k0/k1 the low/high words of the field's seed and e the element index:
-//     h1 = H(H(lo32(e) ^ k0) ^ (k1 ^ hi32(e) * 0x9E3779B9))
-//     float32/bfloat16: v = lo_f + span_f * ((h1 >> 8) * 2^-24)   (float32)
-//     float64:          h2 = H(h1 ^ (k0 + 0x632BE5AB)), k = h1 << 21 | h2 >> 11
-//                       v = lo + span * (k * 2^-53)                (double)
-// every operation rounded to nearest even, no fused multiply-add.
+// rate here) and spends one 32-bit hash per float32 element, one per two
+// bfloat16 elements and two per float64 element.  With H the lowbias32 hash
+// (C. Wellons, "Prospecting for hash functions", 2018) and, per field,
+//     k0 = H(lo32(seed) ^ 0xA511E9B3) | 1,  k1 = H(hi32(seed) + 0x632BE5AB),
+//     k2 = H(k0 ^ k1),  x(n) = lo32(n) * k0 + k1 + hi32(n) * 0x9E3779B9:
+//     float32:  v[e] = lo_f + span_f * ((H(x(e)) >> 8) * 2^-24)          (float32)
+//     bfloat16: h = H(x(m)) for the pair m = e / 2;  v[2m] from h & 0xFFFF,
+//               v[2m+1] from h >> 16, each lo_f + span_f * (bits * 2^-16)
+//               in float32, then rounded to bfloat16
+//     float64:  h1 = H(x(e)), h2 = H(h1 ^ k2), k = h1 << 21 | h2 >> 11,
+//               v[e] = lo + span * (k * 2^-53)                            (double)
+// (lo_f = (float)lo, span_f = (float)(hi - lo)); every operation rounded to
+// nearest even, no fused multiply-add.  The float64 value is built with
+// integer operations when hi - lo is a power of two and lo is 0 or
+// -(hi - lo)/2 (the fp64 formula otherwise; both give the same bits).
 #include <vector>
 
 #include "common.cuh"
@@ -46,17 +50,30 @@ __device__ __forceinline__ uint32_t lowbias32(uint32_t x) {
     return x;
 }
 
-__device__ __forceinline__ uint32_t fill_h1(uint64_t e, uint32_t k0, uint32_t k1) {
-    return lowbias32(lowbias32((uint32_t)e ^ k0) ^ (k1 ^ ((uint32_t)(e >> 32) * 0x9E3779B9u)));
+struct FillKeys {
+    uint32_t k0, k1, k2;
+};
+
+__device__ __forceinline__ FillKeys fill_keys(uint64_t seed) {
+    FillKeys k;
+    k.k0 = lowbias32((uint32_t)seed ^ 0xA511E9B3u) | 1u;
+    k.k1 = lowbias32((uint32_t)(seed >> 32) + 0x632BE5ABu);
+    k.k2 = lowbias32(k.k0 ^ k.k1);
+    return k;
 }
 
-__device__ __forceinline__ float fill_f32(uint32_t h1, float lo_f, float span_f) {
-    const float u = __fmul_rn(__uint2float_rn(h1 >> 8), 0x1p-24f);  // exact
-    return __fadd_rn(lo_f, __fmul_rn(span_f, u));
+__device__ __forceinline__ uint32_t fill_hash(uint64_t n, const FillKeys& k) {
+    return lowbias32((uint32_t)n * k.k0 + k.k1 + (uint32_t)(n >> 32) * 0x9E3779B9u);
 }
 
-__device__ __forceinline__ double fill_f64(uint32_t h1, uint32_t k0, double lo, double span, int mode, int e0) {
-    const uint32_t h2 = lowbias32(h1 ^ (k0 + 0x632BE5ABu));
+// lo_f + span_f * (bits * 2^-B) with bits < 2^B (B = 24 or 16): the product
+// bits * 2^-B is exact
+__device__ __forceinline__ float fill_f32(uint32_t bits, float scale, float lo_f, float span_f) {
+    return __fadd_rn(lo_f, __fmul_rn(span_f, __fmul_rn(__uint2float_rn(bits), scale)));
+}
+
+__device__ __forceinline__ double fill_f64(uint32_t h1, uint32_t k2, double lo, double span, int mode, int e0) {
+    const uint32_t h2 = lowbias32(h1 ^ k2);
     const uint64_t k = ((uint64_t)h1 << 21) | (h2 >> 11);  // 53 bits
     if (mode == kF64General) return __dadd_rn(lo, __dmul_rn(span, __dmul_rn(__ull2double_rn(k), 0x1p-53)));
     // exact: v = x * 2^e0 with x = k - c an integer below 2^53 in magnitude
@@ -105,16 +122,15 @@ __device__ __forceinline__ void fill_field(const FillPlan& f, int64_t gtid, int6
     const int64_t count = (int64_t)(f.meta & ((1ull << 48) - 1));
     const int mode = (int)((f.meta >> 50) & 3);
     const int e0 = (int)(f.meta >> 52) - 2048;
-    const uint32_t k0 = (uint32_t)f.seed, k1 = (uint32_t)(f.seed >> 32);
-    auto bits = [&](int64_t e) -> uint64_t {
-        const uint32_t h1 = fill_h1((uint64_t)e, k0, k1);
-        if constexpr (STORAGE == SB_F64) {
-            return (uint64_t)__double_as_longlong(fill_f64(h1, k0, f.lo, f.span, mode, e0));
-        } else if constexpr (STORAGE == SB_F32) {
-            return __float_as_uint(fill_f32(h1, f.lo_f, f.span_f));
-        } else {
-            return __bfloat16_as_ushort(__float2bfloat16_rn(fill_f32(h1, f.lo_f, f.span_f)));
-        }
+    const FillKeys keys = fill_keys(f.seed);
+    auto value64 = [&](int64_t e) -> uint64_t {
+        return (uint64_t)__double_as_longlong(fill_f64(fill_hash((uint64_t)e, keys), keys.k2, f.lo, f.span, mode, e0));
+    };
+    auto value32 = [&](int64_t e) -> uint32_t {
+        return __float_as_uint(fill_f32(fill_hash((uint64_t)e, keys) >> 8, 0x1p-24f, f.lo_f, f.span_f));
+    };
+    auto bf = [&](uint32_t bits16) -> uint32_t {  // one bfloat16 from 16 random bits
+        return __bfloat16_as_ushort(__float2bfloat16_rn(fill_f32(bits16, 0x1p-16f, f.lo_f, f.span_f)));
     };
     char* base = (char*)f.ptr;
     const int64_t chunks = ((uintptr_t)base & 15) == 0 ? count / V : 0;
@@ -122,25 +138,28 @@ __device__ __forceinline__ void fill_field(const FillPlan& f, int64_t gtid, int6
         uint32_t w[4];
         if constexpr (STORAGE == SB_F64) {
             for (int t = 0; t < 2; ++t) {
-                const uint64_t v = bits(c * V + t);
+                const uint64_t v = value64(c * V + t);
                 w[2 * t] = (uint32_t)v;
                 w[2 * t + 1] = (uint32_t)(v >> 32);
             }
         } else if constexpr (STORAGE == SB_F32) {
-            for (int t = 0; t < 4; ++t) w[t] = (uint32_t)bits(c * V + t);
+            for (int t = 0; t < 4; ++t) w[t] = value32(c * V + t);
         } else {
-            for (int t = 0; t < 4; ++t)
-                w[t] = (uint32_t)bits(c * V + 2 * t) | ((uint32_t)bits(c * V + 2 * t + 1) << 16);
+            for (int t = 0; t < 4; ++t) {  // elements 2m, 2m+1 with m = c * 4 + t
+                const uint32_t h = fill_hash((uint64_t)(c * 4 + t), keys);
+                w[t] = bf(h & 0xffffu) | (bf(h >> 16) << 16);
+            }
         }
         *(uint4*)(base + c * 16) = make_uint4(w[0], w[1], w[2], w[3]);
     }
     for (int64_t e = chunks * V + gtid; e < count; e += gsize) {
         if constexpr (STORAGE == SB_F64) {
-            ((uint64_t*)base)[e] = bits(e);
+            ((uint64_t*)base)[e] = value64(e);
         } else if constexpr (STORAGE == SB_F32) {
-            ((uint32_t*)base)[e] = (uint32_t)bits(e);
+            ((uint32_t*)base)[e] = value32(e);
         } else {
-            ((uint16_t*)base)[e] = (uint16_t)bits(e);
+            const uint32_t h = fill_hash((uint64_t)(e >> 1), keys);
+            ((uint16_t*)base)[e] = (uint16_t)bf((e & 1) ? (h >> 16) : (h & 0xffffu));
         }
     }
 }

@@ -17,27 +17,45 @@ def lowbias32(x):
     return x ^ (x >> np.uint32(16))
 
 
+def _keys(seed):
+    with np.errstate(over="ignore"):
+        k0 = lowbias32(np.uint32(seed & 0xFFFFFFFF) ^ np.uint32(0xA511E9B3)) | np.uint32(1)
+        k1 = lowbias32(np.uint32(seed >> 32) + np.uint32(0x632BE5AB))
+        k2 = lowbias32(k0 ^ k1)
+    return k0, k1, k2
+
+
+def _hash(n, k0, k1):
+    """H(x(n)) for an array of uint64 indices n."""
+    with np.errstate(over="ignore"):
+        lo32 = (n & np.uint64(0xFFFFFFFF)).astype(np.uint32)
+        hi32 = (n >> np.uint64(32)).astype(np.uint32)
+        return lowbias32(lo32 * k0 + k1 + hi32 * np.uint32(0x9E3779B9))
+
+
 def fill_values(seed, count, lo, hi, storage):
     """What sb_fill_batch writes: storage values (bf16 as uint16 bits)."""
-    k0, k1 = np.uint32(seed & 0xFFFFFFFF), np.uint32(seed >> 32)
+    k0, k1, k2 = _keys(seed)
+    lo_f = np.float32(lo)
+    span_f = np.float32(np.float64(hi) - np.float64(lo))
     with np.errstate(over="ignore"):
-        e = np.arange(count, dtype=np.uint64)
-        lo32 = (e & np.uint64(0xFFFFFFFF)).astype(np.uint32)
-        hi32 = (e >> np.uint64(32)).astype(np.uint32)
-        h1 = lowbias32(lowbias32(lo32 ^ k0) ^ (k1 ^ (hi32 * np.uint32(0x9E3779B9))))
         if storage == "float64":
-            h2 = lowbias32(h1 ^ np.uint32((int(k0) + 0x632BE5AB) & 0xFFFFFFFF))
+            h1 = _hash(np.arange(count, dtype=np.uint64), k0, k1)
+            h2 = lowbias32(h1 ^ k2)
             k = (h1.astype(np.uint64) << np.uint64(21)) | (h2 >> np.uint32(11)).astype(np.uint64)
             span = np.float64(hi) - np.float64(lo)
             return np.float64(lo) + span * (k.astype(np.float64) * 2.0**-53)
-    lo_f = np.float32(lo)
-    span_f = np.float32(np.float64(hi) - np.float64(lo))
-    u = (h1 >> np.uint32(8)).astype(np.float32) * np.float32(2.0**-24)
-    v = lo_f + span_f * u
-    assert v.dtype == np.float32
-    if storage == "float32":
-        return v
-    return ora.f32_to_bf16_bits(v)
+        if storage == "float32":
+            h = _hash(np.arange(count, dtype=np.uint64), k0, k1)
+            v = lo_f + span_f * ((h >> np.uint32(8)).astype(np.float32) * np.float32(2.0**-24))
+            assert v.dtype == np.float32
+            return v
+        e = np.arange(count, dtype=np.uint64)
+        h = _hash(e >> np.uint64(1), k0, k1)
+        bits = np.where((e & np.uint64(1)) == 1, h >> np.uint32(16), h & np.uint32(0xFFFF))
+        v = lo_f + span_f * (bits.astype(np.float32) * np.float32(2.0**-16))
+        assert v.dtype == np.float32
+        return ora.f32_to_bf16_bits(v)
 
 
 def request_inputs(req):
