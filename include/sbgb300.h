@@ -171,8 +171,9 @@ int sb_hdiff(int storage, int compute, const void* inp, const void* coeff, void*
  * reference's in-place update (any other overlap is not allowed).  wcon is
  * read at the column shifted by (wshift_i, wshift_j): (1,0) for u, (0,1)
  * for v, (0,0) for w.  ccol/dcol may be NULL; they are only used as scratch
- * by SB_VADV_GLOBAL (the reference's fields of the same names, compute
- * type).  Needs nk >= 2.                                                    */
+ * (the reference's fields of the same names, compute-type sized elements) by
+ * SB_VADV_GLOBAL, SB_VADV_SLAB, SB_VADV_WSLAB, and by SB_VARIANT_AUTO, which
+ * picks a slab form when they are given.  Needs nk >= 2.                      */
 int sb_vadv(int storage, int compute, const void* stage, const void* pos, const void* tens,
             const void* tensstage, const void* wcon, void* out, void* ccol, void* dcol, int64_t ni,
             int64_t nj, int64_t nk, int64_t si, int64_t sj, int64_t sk, int wshift_i, int wshift_j,
@@ -189,7 +190,9 @@ int sb_vadv(int storage, int compute, const void* stage, const void* pos, const 
  * are bit-identical to sb_hdiff / sb_vadv on the same domain.  The domain
  * table lives in pinned host memory and is copied by each launch: do not
  * call sb_batch_set while a launch of the same batch may still be pending
- * (synchronise its stream first).  Distinct batches are independent.        */
+ * (synchronise its stream first).  Distinct batches are independent.  Except
+ * for float32/float32 the vadv kernels keep their factors in a device
+ * workspace owned by the batch (sb_batch_info reports its size).            */
 #define SB_OP_HDIFF 0
 #define SB_OP_VADV 1
 typedef struct sb_domain {
@@ -207,7 +210,8 @@ typedef struct sb_batch_tune {
     int32_t hdiff_planes;  /* k-planes per hdiff item (0: 1)                       */
     int32_t order;         /* reserved (vadv domains always run tallest-first)         */
     int32_t vadv_block;    /* threads (= columns) per vadv block: 32 or 64 (0: 32)   */
-    int32_t vadv_blocks_per_sm; /* persistent vadv blocks per SM (0: as many as fit) */
+    int32_t vadv_blocks_per_sm; /* persistent vadv blocks per SM (0: as many as fit,
+                                 * at most 8 with a factor workspace)              */
     int32_t reserved;
 } sb_batch_tune;
 typedef struct sb_batch sb_batch;

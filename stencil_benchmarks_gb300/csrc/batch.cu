@@ -17,13 +17,16 @@
 //   shared memory.
 // vadv: persistent blocks of BT threads; an item is BT consecutive columns of
 //   one j-row of one domain, one column per thread (stencil_core.cuh:
-//   vadv_async_column: cp.async-staged inputs, factors in shared memory).
-//   Domains are grouped into 8 nk buckets (caps max_nk/8, 2*max_nk/8, ...) and
-//   each bucket's kernel is sized for its cap, so short columns do not pay for
-//   the shared memory of the tallest one.
+//   vadv_async_column: cp.async-staged inputs).  Factors live in shared memory
+//   for float32 storage and arithmetic, otherwise in a slab workspace per
+//   bucket (per thread slot, level stride = the bucket's thread count), which
+//   frees shared memory for more blocks per SM.  Domains are grouped into 8 nk
+//   buckets (caps max_nk/8, 2*max_nk/8, ...) and each bucket's kernel and slab
+//   are sized for its cap, so short columns do not pay for the tallest one.
 // No kernel waits on another warp or kernel: every queue is one atomic counter.
 #include <algorithm>
 #include <cstring>
+#include <type_traits>
 #include <vector>
 
 #include "stencil_core.cuh"
@@ -97,11 +100,14 @@ __global__ void __launch_bounds__(256)
 }
 
 // Dynamic shared memory: ccol[cap][BT], dcol[cap][BT] (compute type), then the
-// staging ring [D+1][6][BT] (RingOf<storage>) at ring_offset.
-template <class S, class C, int BT, int D, class IDX, class P = C>
+// staging ring [D+1][6][BT] (RingOf<storage>) at ring_offset.  With SLAB the
+// factors live in the bucket's slab workspace instead (level k of thread slot
+// q at slab[k * nslots + q], dcol after cap * nslots ccol entries) and the
+// shared memory is the ring only, so many more blocks fit per SM.
+template <class S, class C, int BT, int D, class IDX, class P = C, bool SLAB = false>
 __global__ void __launch_bounds__(BT)
     batch_vadv_kernel(const DevTable* __restrict__ tab, unsigned long long* __restrict__ counter, int bucket,
-                      int cap, int ring_offset) {
+                      int cap, int ring_offset, P* __restrict__ slab) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ int s_dom;
     __shared__ int64_t s_local;
@@ -109,7 +115,8 @@ __global__ void __launch_bounds__(BT)
     const int64_t total = tab->bucket_items[bucket];
     if (total == 0) return;
     const int t = threadIdx.x;
-    P* sc = reinterpret_cast<P*>(smem_raw) + t;
+    const int64_t nslots = (int64_t)gridDim.x * BT;
+    P* sc = SLAB ? slab + (int64_t)blockIdx.x * BT + t : reinterpret_cast<P*>(smem_raw) + t;
     auto* ring = reinterpret_cast<typename RingOf<S>::T*>(smem_raw + ring_offset) + t;
     for (;;) {
         if (t == 0) {
@@ -135,10 +142,18 @@ __global__ void __launch_bounds__(BT)
         const int i = group * BT + t;
         if (i < dm.ni) {
             const IDX col = (IDX)i * (IDX)dm.si + (IDX)j * (IDX)dm.sj;
-            vadv_async_column<S, C, BT, D, IDX, false, P>((const S*)dm.f[0], (const S*)dm.f[1],
-                                                          (const S*)dm.f[2], (const S*)dm.f[3], (const S*)dm.f[4],
-                                                          (S*)dm.out, col, dm.nk, (IDX)dm.sk, (IDX)dm.wsh, sc,
-                                                          sc + dm.nk * BT, ring);
+            if constexpr (SLAB) {
+                vadv_async_column<S, C, BT, D, IDX, true, P>((const S*)dm.f[0], (const S*)dm.f[1],
+                                                             (const S*)dm.f[2], (const S*)dm.f[3],
+                                                             (const S*)dm.f[4], (S*)dm.out, col, dm.nk,
+                                                             (IDX)dm.sk, (IDX)dm.wsh, sc, sc + (int64_t)cap * nslots,
+                                                             ring, (int)nslots);
+            } else {
+                vadv_async_column<S, C, BT, D, IDX, false, P>((const S*)dm.f[0], (const S*)dm.f[1],
+                                                              (const S*)dm.f[2], (const S*)dm.f[3],
+                                                              (const S*)dm.f[4], (S*)dm.out, col, dm.nk,
+                                                              (IDX)dm.sk, (IDX)dm.wsh, sc, sc + dm.nk * BT, ring);
+            }
         }
         __syncthreads();  // s_dom / s_local are rewritten by the next grab
     }
@@ -146,8 +161,9 @@ __global__ void __launch_bounds__(BT)
 
 struct Kinds {
     void (*hdiff)(dim3, dim3, cudaStream_t, const DevTable*, unsigned long long*);
-    void (*vadv32)(dim3, dim3, size_t, cudaStream_t, const DevTable*, unsigned long long*, int, int, int);
-    void (*vadv64)(dim3, dim3, size_t, cudaStream_t, const DevTable*, unsigned long long*, int, int, int);
+    void (*vadv32)(dim3, dim3, size_t, cudaStream_t, const DevTable*, unsigned long long*, int, int, int, void*);
+    void (*vadv64)(dim3, dim3, size_t, cudaStream_t, const DevTable*, unsigned long long*, int, int, int, void*);
+    bool slab;  // vadv keeps its factors in a slab workspace
     const void* vadv32_fn;
     const void* vadv64_fn;
     int storage_bytes, compute_bytes;
@@ -157,21 +173,27 @@ template <class S, class C, int U, class IDX>
 void run_hdiff(dim3 g, dim3 b, cudaStream_t s, const DevTable* t, unsigned long long* c) {
     batch_hdiff_kernel<S, C, U, IDX><<<g, b, 0, s>>>(t, c);
 }
-template <class S, class C, int BT, class IDX, class P>
+template <class S, class C, int BT, class IDX, class P, bool SLAB>
 void run_vadv(dim3 g, dim3 b, size_t smem, cudaStream_t s, const DevTable* t, unsigned long long* c, int bucket,
-              int cap, int ring_offset) {
-    batch_vadv_kernel<S, C, BT, kVadvDepth, IDX, P><<<g, b, smem, s>>>(t, c, bucket, cap, ring_offset);
+              int cap, int ring_offset, void* slab) {
+    batch_vadv_kernel<S, C, BT, kVadvDepth, IDX, P, SLAB><<<g, b, smem, s>>>(t, c, bucket, cap, ring_offset,
+                                                                             (P*)slab);
 }
 
 // hdiff computes in HC, vadv in VC with its recurrences in P
 template <class S, class HC, class VC, int U, class IDX, class P = VC>
 Kinds kinds_for() {
     Kinds k;
+    // slab factors need ring entries of the factor size; for float32 storage
+    // and arithmetic the shared-memory factors measured faster in batches
+    constexpr bool SLAB = sizeof(typename RingOf<S>::T) == sizeof(P) &&
+                          !(std::is_same<S, float>::value && std::is_same<P, float>::value);
+    k.slab = SLAB;
     k.hdiff = &run_hdiff<S, HC, U, IDX>;
-    k.vadv32 = &run_vadv<S, VC, 32, IDX, P>;
-    k.vadv64 = &run_vadv<S, VC, 64, IDX, P>;
-    k.vadv32_fn = (const void*)&batch_vadv_kernel<S, VC, 32, kVadvDepth, IDX, P>;
-    k.vadv64_fn = (const void*)&batch_vadv_kernel<S, VC, 64, kVadvDepth, IDX, P>;
+    k.vadv32 = &run_vadv<S, VC, 32, IDX, P, SLAB>;
+    k.vadv64 = &run_vadv<S, VC, 64, IDX, P, SLAB>;
+    k.vadv32_fn = (const void*)&batch_vadv_kernel<S, VC, 32, kVadvDepth, IDX, P, SLAB>;
+    k.vadv64_fn = (const void*)&batch_vadv_kernel<S, VC, 64, kVadvDepth, IDX, P, SLAB>;
     k.storage_bytes = sizeof(typename RingOf<S>::T);  // ring entry
     k.compute_bytes = sizeof(P);                      // factor entry
     return k;
@@ -210,6 +232,9 @@ struct sb_batch {
     int vadv_grid[kBuckets] = {};
     size_t vadv_smem[kBuckets] = {};
     int ring_offset[kBuckets] = {};
+    void* slab[kBuckets] = {};  // per-bucket factor slabs (inside slab_mem)
+    void* slab_mem = nullptr;
+    size_t slab_bytes = 0;
     bool idx64 = false;
     DevTable* host_table = nullptr;  // pinned
     DevTable* dev_table = nullptr;
@@ -235,6 +260,7 @@ void release(sb_batch* b) {
     for (auto& e : b->joins)
         if (e) cudaEventDestroy(e);
     if (b->counters) cudaFree(b->counters);
+    if (b->slab_mem) cudaFree(b->slab_mem);
     if (b->dev_table) cudaFree(b->dev_table);
     if (b->host_table) cudaFreeHost(b->host_table);
     delete b;
@@ -274,7 +300,7 @@ int capture_graph(sb_batch* b) {
     for (int q = 0; q < kBuckets; ++q) {
         cudaStreamWaitEvent(b->streams[2 + q], b->fork, 0);
         vadv_run(dim3(b->vadv_grid[q]), dim3(b->vadv_block), b->vadv_smem[q], b->streams[2 + q], b->dev_table,
-                 b->counters + 1 + q, q, b->cap[q], b->ring_offset[q]);
+                 b->counters + 1 + q, q, b->cap[q], b->ring_offset[q], b->slab[q]);
         cudaEventRecord(b->joins[1 + q], b->streams[2 + q]);
     }
     for (int q = 0; q < 1 + kBuckets; ++q) cudaStreamWaitEvent(s0, b->joins[q], 0);
@@ -328,7 +354,8 @@ int sb_batch_create(sb_batch** out, int storage, int compute, int max_domains, i
     b->hdiff_grid = p->sm_count * per_sm;
     for (int q = 0; q < kBuckets; ++q) {
         b->cap[q] = (int)std::max<int64_t>(2, ceil_div(max_nk * (q + 1), kBuckets));
-        b->vadv_smem[q] = vadv_smem_bytes(b->cap[q], b->vadv_block, k.compute_bytes, k.storage_bytes,
+        // slab mode: shared memory holds the ring only (cap 0 factor levels)
+        b->vadv_smem[q] = vadv_smem_bytes(k.slab ? 0 : b->cap[q], b->vadv_block, k.compute_bytes, k.storage_bytes,
                                           &b->ring_offset[q]);
         if ((int64_t)b->vadv_smem[q] > p->smem_optin) {
             const size_t need = b->vadv_smem[q];
@@ -339,12 +366,29 @@ int sb_batch_create(sb_batch** out, int storage, int compute, int max_domains, i
                         (long long)max_nk, need, p->smem_optin);
         }
         const int fit = (int)std::min<int64_t>(16, (p->smem_optin + 1024) / (int64_t)(b->vadv_smem[q] + 1024));
-        const int vper = b->tune.vadv_blocks_per_sm > 0 ? std::min(b->tune.vadv_blocks_per_sm, fit) : fit;
+        // slab mode: 8 blocks per SM by default (the slabs grow with the grid)
+        const int vdef = k.slab ? std::min(fit, 8) : fit;
+        const int vper = b->tune.vadv_blocks_per_sm > 0 ? std::min(b->tune.vadv_blocks_per_sm, fit) : vdef;
         b->vadv_grid[q] = p->sm_count * std::max(1, vper);
+    }
+    size_t slab_total = 0;
+    size_t slab_off[kBuckets] = {};
+    if (k.slab) {
+        for (int q = 0; q < kBuckets; ++q) {
+            slab_off[q] = slab_total;
+            slab_total += (2 * (size_t)b->cap[q] * b->vadv_grid[q] * b->vadv_block * k.compute_bytes + 255) / 256 * 256;
+        }
     }
     cudaError_t e = cudaMallocHost((void**)&b->host_table, table_bytes(max_domains));
     if (e == cudaSuccess) e = cudaMalloc((void**)&b->dev_table, table_bytes(max_domains));
     if (e == cudaSuccess) e = cudaMalloc((void**)&b->counters, sizeof(unsigned long long) * (1 + kBuckets));
+    if (e == cudaSuccess && slab_total) {
+        e = cudaMalloc(&b->slab_mem, slab_total);
+        if (e == cudaSuccess) {
+            b->slab_bytes = slab_total;
+            for (int q = 0; q < kBuckets; ++q) b->slab[q] = (char*)b->slab_mem + slab_off[q];
+        }
+    }
     for (auto& s : b->streams)
         if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming);
@@ -475,7 +519,7 @@ int sb_batch_launch(sb_batch* b, void* stream, double* time_s) {
 int sb_batch_info(sb_batch* b, int64_t* total_items, size_t* workspace_bytes, int* grid, int* block) {
     SB_CHECK(b, SB_ERR_INVALID, "batch is NULL");
     if (total_items) *total_items = b->total_items;
-    if (workspace_bytes) *workspace_bytes = 0;
+    if (workspace_bytes) *workspace_bytes = b->slab_bytes;
     if (grid) *grid = b->hdiff_grid;
     if (block) *block = b->hdiff_block;
     return SB_OK;
