@@ -511,7 +511,9 @@ def run_served(n_requests=2000, rates=(1000.0, 5000.0, 20000.0), seed=11, float6
     from stencil_benchmarks_gb300 import serving
 
     server = serving.Server(budget_bytes=150e9, max_batch=64, slots_per_form=3, float64_compute=float64_compute)
-    serving.run_load(server, serving.request_specs(64, seed=seed + 1000), rate=1e6)  # warm-up
+    # warm-up: enough requests that every slot of every form has launched (and
+    # captured its graph) before the measured rates
+    serving.run_load(server, serving.request_specs(1024, seed=seed + 1000), rate=1e6)
     out = []
     for rate in rates:
         stats = serving.run_load(server, serving.request_specs(n_requests, seed=seed), rate=rate)

@@ -420,7 +420,7 @@ def main(argv=None):
     args = ap.parse_args(argv)
     server = Server(budget_bytes=args.budget_gb * 1e9, max_batch=args.max_batch, slots_per_form=args.slots,
                     float64_compute=args.float64_compute)
-    warm = request_specs(64, seed=args.seed + 1000)
+    warm = request_specs(1024, seed=args.seed + 1000)  # every slot launches (and captures its graph) once
     run_load(server, warm, rate=1e6)
     for rate in (float(r) for r in args.rates.split(",")):
         reqs = request_specs(args.requests, seed=args.seed)
