@@ -67,6 +67,9 @@ extern "C" {
 #define SB_VARIANT_AUTO 0
 #define SB_HDIFF_TILE 1   /* smem-staged k-plane tiles, lap/flx/fly once per point */
 #define SB_HDIFF_JSCAN 2  /* register j-march, i-neighbours by warp shuffles       */
+#define SB_HDIFF_TMA 3    /* TILE with inp k-planes staged by TMA (cp.async.bulk.tensor)
+                           * into two shared-memory stages (i unit-stride, 16-byte
+                           * aligned j/k strides and halo corner)                   */
 #define SB_VADV_SMEM 1    /* one thread per column, ccol/dcol in shared memory     */
 #define SB_VADV_GLOBAL 2  /* one thread per column, ccol/dcol in caller scratch    */
 #define SB_VADV_SLAB 3    /* persistent threads, factors in compact per-thread slabs of

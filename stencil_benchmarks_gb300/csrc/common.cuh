@@ -283,6 +283,8 @@ template <>
 __device__ __forceinline__ float cvt<float, bf16>(bf16 v) { return __bfloat162float(v); }
 template <>
 __device__ __forceinline__ f32x2 cvt<f32x2, double>(double v) { return f32x2_from_double(v); }
+template <>
+__device__ __forceinline__ f32x2 cvt<f32x2, f32x2>(f32x2 v) { return v; }
 
 // ---------------------------------------------------------------------------
 // launch helpers

@@ -20,7 +20,11 @@
 //
 // Caller contract: inp is readable on [-2, ni+1] x [-2, nj+1] x [0, nk)
 // relative to the interior pointer (a halo of at least 2 in i and j).
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
 #include <cstdlib>
+#include <mutex>
 #include <type_traits>
 
 #include "stencil_core.cuh"
@@ -184,6 +188,241 @@ int launch_tile(const void* inp, const void* coeff, void* out, int64_t ni, int64
     return SB_OK;
 }
 
+// ---------------------------------------------------------------------------
+// TMA variant: the TILE computation with inp staged by the tensor memory
+// accelerator.  A CTA owns a TX x TY tile and walks KPER k-planes; plane k's
+// box of inp arrives by one cp.async.bulk.tensor into one of two
+// shared-memory stages, signalled by the stage's mbarrier, while the CTA
+// computes the previous plane.  The tensor map starts at the 16-byte boundary
+// at or below the halo corner inp(-2, -2, 0), `off` elements before it, so a
+// box for the tile at i0 starts at x = i0 (a multiple of TX elements, hence of
+// 16 bytes) and holds global i = i0 - 2 - off + c in column c; the box is
+// TX + PADX columns wide (PADX >= 4 + the largest off) and TY + 4 rows high.
+// Boxes reaching past the array are zero-filled by the hardware; those
+// columns and rows only feed points that are not stored.  Waits are bounded:
+// a wait that gives up sets g_tma_timeout, waits (bounded) for the other
+// stage's copy and the CTA returns; sb_hdiff reports SB_ERR_TIMEOUT.
+__device__ int g_tma_timeout = 0;
+thread_local bool t_tma_used = false;
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t phase) {
+    for (int it = 0; it < (1 << 20); ++it) {
+        uint32_t done;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(done)
+            : "r"(bar), "r"(phase)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+__device__ __forceinline__ void tma_load_plane(const CUtensorMap* map, uint32_t dst, uint32_t bar, int x, int y,
+                                               int z, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(bar), "r"(bytes) : "memory");
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+        "[%5];\n" ::"r"(dst),
+        "l"((uint64_t)map), "r"(x), "r"(y), "r"(z), "r"(bar)
+        : "memory");
+}
+
+template <class S, class C>
+struct TmaSmem {
+    static constexpr int PADX = sizeof(S) == 2 ? 16 : 8;
+    static __host__ __device__ size_t stage_bytes(int tx, int ty) {
+        return ((size_t)(tx + PADX) * (ty + 4) * sizeof(S) + 127) / 128 * 128;
+    }
+    // Narrower storage than compute: each landed plane is widened once into a
+    // compute-typed copy (a float -> double conversion per use would cost more
+    // than the extra shared-memory pass).
+    static constexpr bool CONV = !std::is_same<S, C>::value;
+    static __host__ __device__ size_t conv_bytes(int tx, int ty) {
+        return CONV ? ((size_t)(tx + PADX) * (ty + 4) * sizeof(C) + 127) / 128 * 128 : 0;
+    }
+    static size_t bytes(int tx, int ty) {
+        return 2 * stage_bytes(tx, ty) + conv_bytes(tx, ty) +
+               sizeof(C) * (size_t)((ty + 2) * (tx + 2) + ty * (tx + 1) + (ty + 1) * tx) + 16 + 16;
+    }
+};
+
+template <class S, class C, int TX, int NTY>
+__global__ void __launch_bounds__(TX* NTY)
+    hdiff_tma_kernel(const __grid_constant__ CUtensorMap tmap, const S* __restrict__ coeff, S* __restrict__ out,
+                     int ni, int nj, int nk, int64_t sj, int64_t sk, int TY, int kper, int off) {
+    using A = Ar<C>;
+    using M = TmaSmem<S, C>;
+    using T = typename std::conditional<M::CONV, C, S>::type;  // element type the stencil reads
+    constexpr int BX = TX + M::PADX, WL = TX + 2, WF = TX + 1, WY = TX;
+    extern __shared__ __align__(128) unsigned char smem_tma[];
+    const size_t stage = M::stage_bytes(TX, TY);
+    C* s_conv = reinterpret_cast<C*>(smem_tma + 2 * stage);  // (TY+4) x BX, CONV only
+    C* s_lap = reinterpret_cast<C*>(smem_tma + 2 * stage + M::conv_bytes(TX, TY));  // (TY+2) x WL
+    C* s_flx = s_lap + (TY + 2) * WL;                        // TY x WF
+    C* s_fly = s_flx + TY * WF;                              // (TY+1) x WY
+    uint64_t* bars = reinterpret_cast<uint64_t*>(
+        (reinterpret_cast<uintptr_t>(s_fly + (TY + 1) * WY) + 15) & ~(uintptr_t)15);
+    const uint32_t stage0 = smem_addr(smem_tma), bar0 = smem_addr(bars);
+    const uint32_t box_bytes = (uint32_t)(BX * (TY + 4) * sizeof(S));
+
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const bool leader = tx == 0 && ty == 0;
+    const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY;
+    const int k0 = blockIdx.z * kper;
+    const int k1 = min(nk, k0 + kper);
+    if (leader) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar0) : "memory");
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar0 + 8) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    __syncthreads();
+    if (leader) {
+        for (int q = 0; q < 2 && k0 + q < k1; ++q)
+            tma_load_plane(&tmap, stage0 + q * (uint32_t)stage, bar0 + 8 * q, i0, j0, k0 + q, box_bytes);
+    }
+    uint32_t phases = 0u;  // bit q: parity to wait for on stage q
+    for (int k = k0; k < k1; ++k) {
+        const int sidx = (k - k0) & 1;
+        if (!mbar_wait(bar0 + 8 * sidx, (phases >> sidx) & 1u)) {
+            atomicExch(&g_tma_timeout, 1);
+            if (k + 1 < k1) mbar_wait(bar0 + 8 * (sidx ^ 1), (phases >> (sidx ^ 1)) & 1u);
+            return;
+        }
+        phases ^= 1u << sidx;
+        // s_in(r, c) <-> global (i0 - 2 + c, j0 - 2 + r)
+        const S* s_land = reinterpret_cast<const S*>(smem_tma + sidx * stage) + off;
+        const T* s_in;
+        if constexpr (M::CONV) {
+            for (int r = ty; r < TY + 4; r += NTY)
+                for (int c = tx; c < TX + 4; c += TX) s_conv[r * BX + c] = cvt<C, S>(s_land[r * BX + c]);
+            __syncthreads();
+            s_in = s_conv;
+        } else {
+            s_in = s_land;
+        }
+
+        // lap at local (ii, jj) <-> global (i0-1+ii, j0-1+jj)
+        for (int jj = ty; jj < TY + 2; jj += NTY) {
+            for (int ii = tx; ii < WL; ii += TX) {
+                const T* c = s_in + (jj + 1) * BX + ii + 1;
+                const C sum = A::add(A::add(A::add(cvt<C, T>(c[1]), cvt<C, T>(c[-1])), cvt<C, T>(c[BX])),
+                                     cvt<C, T>(c[-BX]));
+                s_lap[jj * WL + ii] = A::sub(A::template scale2<2>(cvt<C, T>(c[0])), sum);
+            }
+        }
+        __syncthreads();
+        for (int jj = ty; jj < TY; jj += NTY) {
+            for (int ii = tx; ii < WF; ii += TX) {
+                const C* l = s_lap + (jj + 1) * WL + ii;
+                const T* x = s_in + (jj + 2) * BX + ii + 1;
+                s_flx[jj * WF + ii] = A::limit(A::sub(l[1], l[0]), cvt<C, T>(x[1]), cvt<C, T>(x[0]));
+            }
+        }
+        for (int jj = ty; jj < TY + 1; jj += NTY) {
+            for (int ii = tx; ii < WY; ii += TX) {
+                const C* l = s_lap + jj * WL + ii + 1;
+                const T* x = s_in + (jj + 1) * BX + ii + 2;
+                s_fly[jj * WY + ii] = A::limit(A::sub(l[WL], l[0]), cvt<C, T>(x[BX]), cvt<C, T>(x[0]));
+            }
+        }
+        __syncthreads();
+        const int gi = i0 + tx;
+        for (int jj = ty; jj < TY; jj += NTY) {
+            const int gj = j0 + jj;
+            if (gi < ni && gj < nj) {
+                const C fx1 = s_flx[jj * WF + tx + 1], fx0 = s_flx[jj * WF + tx];
+                const C fy1 = s_fly[(jj + 1) * WY + tx], fy0 = s_fly[jj * WY + tx];
+                const C x = cvt<C, T>(s_in[(jj + 2) * BX + tx + 2]);
+                const int64_t o = (int64_t)k * sk + (int64_t)gi + (int64_t)gj * sj;
+                const C cf = ld<C, S>(coeff + o);
+                st<S, C>(out + o, A::sub(x, A::mul(cf, A::sub(A::add(A::sub(fx1, fx0), fy1), fy0))));
+            }
+        }
+        __syncthreads();  // stage sidx and the lap/flux buffers are free again
+        if (leader && k + 2 < k1) {
+            asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+            tma_load_plane(&tmap, stage0 + sidx * (uint32_t)stage, bar0 + 8 * sidx, i0, j0, k + 2, box_bytes);
+        }
+    }
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
+        cudaGetLastError();
+    });
+    return fn;
+}
+
+template <class S>
+CUtensorMapDataType tma_type() {
+    if constexpr (sizeof(S) == 8) return CU_TENSOR_MAP_DATA_TYPE_FLOAT64;
+    else if constexpr (sizeof(S) == 4) return CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
+    else return CU_TENSOR_MAP_DATA_TYPE_BFLOAT16;
+}
+
+// TMA launch if the layout qualifies (i unit-stride, j/k strides multiples
+// of 16 bytes, tile rows within the 256-row box limit); SB_ERR_UNSUPPORTED
+// (no error text) if not.
+template <class S, class C, int TX, int NTY>
+int launch_tma(const void* inp, const void* coeff, void* out, int64_t ni, int64_t nj, int64_t nk, int64_t si,
+               int64_t sj, int64_t sk, int ty, int kper, cudaStream_t stream, const DeviceProps* p) {
+    constexpr int ES = (int)sizeof(S), PADX = TmaSmem<S, C>::PADX;
+    static_assert(((TX + PADX) * ES) % 16 == 0 && (TX * ES) % 16 == 0 && PADX >= 4 + 16 / ES - 1,
+                  "TMA box rows and x offsets must be 16-byte multiples covering the halo at any offset");
+    if (si != 1 || sj <= 0 || sk <= 0 || (sj * ES) % 16 || (sk * ES) % 16) return SB_ERR_UNSUPPORTED;
+    if (ty < NTY || ty + 4 > 256 || ni + 4 + 16 > (1LL << 31) || nj + 4 > (1LL << 31)) return SB_ERR_UNSUPPORTED;
+    // The 16-byte boundary at or below the halo corner: the bytes between it
+    // and the corner share the corner's 16-byte block, so reading them is safe.
+    const uintptr_t corner = (uintptr_t)((const S*)inp - 2 - 2 * sj);
+    if (corner % ES) return SB_ERR_UNSUPPORTED;
+    const int off = (int)((corner & 15) / ES);
+    const void* base = (const void*)(corner - (corner & 15));
+    auto encode = tensor_map_encoder();
+    if (!encode) return SB_ERR_UNSUPPORTED;
+    CUtensorMap tmap;
+    const cuuint64_t dims[3] = {(cuuint64_t)(ni + 4 + off), (cuuint64_t)(nj + 4), (cuuint64_t)nk};
+    const cuuint64_t strides[2] = {(cuuint64_t)(sj * ES), (cuuint64_t)(sk * ES)};
+    const cuuint32_t box[3] = {(cuuint32_t)(TX + PADX), (cuuint32_t)(ty + 4), 1};
+    const cuuint32_t estride[3] = {1, 1, 1};
+    const CUresult cr = encode(&tmap, tma_type<S>(), 3, const_cast<void*>(base), dims, strides, box, estride,
+                               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                               CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (cr != CUDA_SUCCESS) return SB_ERR_UNSUPPORTED;
+    const size_t smem = TmaSmem<S, C>::bytes(TX, ty);
+    SB_CHECK((int64_t)smem <= p->smem_optin, SB_ERR_INVALID, "hdiff TMA tile %dx%d needs %zu bytes of shared memory",
+             TX, ty, smem);
+    auto kernel = hdiff_tma_kernel<S, C, TX, NTY>;
+    if (smem > 48 * 1024) SB_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const int64_t gx = ceil_div(ni, TX), gy = ceil_div(nj, ty), gz = ceil_div(nk, kper);
+    SB_CHECK(gy <= p->max_grid_y && gz <= p->max_grid_z, SB_ERR_INVALID, "hdiff grid too large");
+    t_tma_used = true;
+    kernel<<<dim3((unsigned)gx, (unsigned)gy, (unsigned)gz), dim3(TX, NTY), smem, stream>>>(
+        tmap, (const S*)coeff, (S*)out, (int)ni, (int)nj, (int)nk, sj, sk, ty, kper, off);
+    return SB_OK;
+}
+
+// After a synchronous (timed) TMA launch: SB_ERR_TIMEOUT if a CTA gave up
+// waiting for its copies (the flag is cleared).
+int tma_timeout_status() {
+    int flag = 0;
+    SB_CUDA(cudaMemcpyFromSymbol(&flag, g_tma_timeout, sizeof(int)));
+    if (!flag) return SB_OK;
+    const int zero = 0;
+    SB_CUDA(cudaMemcpyToSymbol(g_tma_timeout, &zero, sizeof(int)));
+    return fail(SB_ERR_TIMEOUT, "hdiff TMA: a thread block timed out waiting for its tensor copies");
+}
+
 template <class S, class C>
 int launch_typed(const void* inp, const void* coeff, void* out, int64_t ni, int64_t nj, int64_t nk,
                  int64_t si, int64_t sj, int64_t sk, const sb_tune* tune, cudaStream_t stream) {
@@ -194,13 +433,46 @@ int launch_typed(const void* inp, const void* coeff, void* out, int64_t ni, int6
     // fp64 compute is bound by the fp64 pipe: TILE computes every lap/flx/fly
     // once per tile (fewest fp64 operations); fp32 and float-pair compute are
     // bound by instruction issue: JSCAN (shuffles, no block barriers) is faster.
+    // With float64 storage too, the TMA-staged tile is faster still (its
+    // loads leave the issue slots to the fp64 arithmetic and overlap the
+    // previous plane's compute); it needs TMA-describable strides, else TILE.
     const bool auto_tile = variant == SB_VARIANT_AUTO && std::is_same<C, double>::value;
+    if constexpr (std::is_same<S, double>::value && std::is_same<C, double>::value) {
+        if (variant == SB_VARIANT_AUTO) {
+            const int rc_tma = launch_tma<S, C, 128, 4>(inp, coeff, out, ni, nj, nk, si, sj, sk, 16, 4, stream, p);
+            if (rc_tma != SB_ERR_UNSUPPORTED) return rc_tma;
+        }
+    }
     if (variant == SB_VARIANT_AUTO) variant = auto_tile ? SB_HDIFF_TILE : SB_HDIFF_JSCAN;
     if constexpr (std::is_same<C, fix64>::value) {
         SB_CHECK(variant == SB_HDIFF_JSCAN, SB_ERR_UNSUPPORTED, "fixed-point hdiff runs as JSCAN strips only");
     }
-    SB_CHECK(variant == SB_HDIFF_TILE || variant == SB_HDIFF_JSCAN, SB_ERR_UNSUPPORTED,
+    SB_CHECK(variant == SB_HDIFF_TILE || variant == SB_HDIFF_JSCAN || variant == SB_HDIFF_TMA, SB_ERR_UNSUPPORTED,
              "hdiff variant %d is not available", variant);
+    if (variant == SB_HDIFF_TMA) {
+        if constexpr (std::is_same<C, fix64>::value) {
+            return fail(SB_ERR_UNSUPPORTED, "fixed-point hdiff runs as JSCAN strips only");
+        } else {
+            const int bx = (tune && tune->block_x > 0) ? tune->block_x : 64;
+            const int by = (tune && tune->block_y > 0) ? tune->block_y : 4;
+            const int ty = (tune && tune->tile_y > 0) ? tune->tile_y : 16;
+            const int kper = (tune && tune->k_per_cta > 0) ? tune->k_per_cta : 8;
+            int rc2 = SB_ERR_UNSUPPORTED;
+#define SB_TMA_CASE(TXV, NTYV)                                                                               \
+    if (bx == TXV && by == NTYV)                                                                              \
+        rc2 = launch_tma<S, C, TXV, NTYV>(inp, coeff, out, ni, nj, nk, si, sj, sk, ty, kper, stream, p);
+            SB_TMA_CASE(32, 8)
+            SB_TMA_CASE(64, 4)
+            SB_TMA_CASE(64, 8)
+            SB_TMA_CASE(128, 2)
+            SB_TMA_CASE(128, 4)
+#undef SB_TMA_CASE
+            SB_CHECK(rc2 != SB_ERR_UNSUPPORTED, SB_ERR_UNSUPPORTED,
+                     "hdiff TMA: needs blocks 32x8, 64x{4,8} or 128x{2,4}, i unit-stride, 16-byte aligned j/k "
+                     "strides and halo corner, tile rows in [block_y, 252]");
+            return rc2;
+        }
+    }
     if (variant == SB_HDIFF_JSCAN) {
         const int nw = (tune && tune->block_y > 0) ? tune->block_y : 4;
         const int ty = (tune && tune->tile_y > 0) ? tune->tile_y : 32;
@@ -255,7 +527,8 @@ extern "C" int sb_hdiff(int storage, int compute, const void* inp, const void* c
         return SB_OK;
     }
     cudaStream_t s = (cudaStream_t)stream;
-    return timed(s, time_s, [&]() {
+    t_tma_used = false;
+    rc = timed(s, time_s, [&]() {
         if (storage == SB_F64 && compute == SB_F64)
             return launch_typed<double, double>(inp, coeff, out, ni, nj, nk, si, sj, sk, tune, s);
         if (storage == SB_F64 && compute == SB_F32X2)
@@ -270,4 +543,6 @@ extern "C" int sb_hdiff(int storage, int compute, const void* inp, const void* c
             return launch_typed<bf16, float>(inp, coeff, out, ni, nj, nk, si, sj, sk, tune, s);
         return fail(SB_ERR_UNSUPPORTED, "unsupported storage/compute combination (%d, %d)", storage, compute);
     });
+    if (rc == SB_OK && time_s && t_tma_used) rc = tma_timeout_status();
+    return rc;
 }

@@ -12,8 +12,9 @@ measured launches (CUDA events), prints one line per case, and frees its
 fields before the next case.  The kernel variants are the defaults of the
 library, except vadv-f64 and vadv-f32x2, which use the caller-scratch
 (GLOBAL) variant as ``bench.py`` does.  ``:<variant>`` picks another one
-(hdiff: tile, jscan; vadv: smem, global, slab -- global and slab with
-ccol/dcol scratch fields).
+(hdiff: tile, jscan, tma -- tma with rows padded to 64 bytes so that the
+j/k strides suit the tensor copies; vadv: smem, global, slab -- global and
+slab with ccol/dcol scratch fields).
 """
 
 from __future__ import annotations
@@ -33,9 +34,9 @@ STORAGE = {"f64": ("float64", "float64"), "f32": ("float32", "float32"), "bf16":
            "f32x2": ("float64", "float32x2"), "fix64": ("float64", "fixed64")}
 
 
-def _field(rng, storage, halo, lo, hi):
+def _field(rng, storage, halo, lo, hi, alignment=0):
     shape = (NI + 2 * halo[0], NJ + 2 * halo[1], NK + 2 * halo[2])
-    host = sbarray.alloc_array(shape, storage, (2, 1, 0), 0, index_to_align=halo)
+    host = sbarray.alloc_array(shape, storage, (2, 1, 0), alignment, index_to_align=halo)
     vals = rng.uniform(lo, hi, size=shape)
     if storage == "bfloat16":
         bits = vals.astype(np.float32).view(np.uint32).astype(np.uint64)
@@ -47,7 +48,8 @@ def _field(rng, storage, halo, lo, hi):
     return dev
 
 
-VARIANTS = {"tile": _native.HDIFF_TILE, "jscan": _native.HDIFF_JSCAN, "smem": _native.VADV_SMEM,
+VARIANTS = {"tile": _native.HDIFF_TILE, "jscan": _native.HDIFF_JSCAN, "tma": _native.HDIFF_TMA,
+            "smem": _native.VADV_SMEM,
             "global": _native.VADV_GLOBAL, "slab": _native.VADV_SLAB}
 
 
@@ -65,7 +67,8 @@ def run_case(name, warmup, launches, rng):
     else:
         storage, compute = STORAGE[form]
         if stencil == "hdiff":
-            f = [_field(rng, storage, (2, 2, 0), 0.0, 1.0) for _ in range(3)]
+            align = 64 if variant == "tma" else 0
+            f = [_field(rng, storage, (2, 2, 0), 0.0, 1.0, align) for _ in range(3)]
 
             htune = _native.tune(variant=VARIANTS[variant]) if variant else None
 

@@ -47,10 +47,10 @@ def _check(got, want, tol, what):
     return err / max(scale, 1e-300)
 
 
-def _hdiff(domain, halo, tune=None, seed=0, layout=(2, 1, 0)):
+def _hdiff(domain, halo, tune=None, seed=0, layout=(2, 1, 0), alignment=0):
     shape = tuple(d + 2 * h for d, h in zip(domain, halo))
     vals = rng_fields(seed, shape, ("inp", "coeff", "out"), {})
-    hosts = {n: host_field(v, "float64", layout, 0, halo) for n, v in vals.items()}
+    hosts = {n: host_field(v, "float64", layout, alignment, halo) for n, v in vals.items()}
     dev = {n: to_device(h, "float64", halo) for n, h in hosts.items()}
     kernels.hdiff(dev["inp"], dev["coeff"], dev["out"], compute="float32x2", tune=tune)
     got = interior(download_like(dev["out"], hosts["out"]), domain, halo)
@@ -65,6 +65,16 @@ def _hdiff(domain, halo, tune=None, seed=0, layout=(2, 1, 0)):
 def test_hdiff_pair(variant, domain, halo, layout, lib):
     got, want = _hdiff(domain, halo, tune=_native.tune(variant=variant), seed=21, layout=layout)
     _check(got, want, HDIFF_TOL, f"hdiff pair variant {variant} {domain}")
+
+
+@pytest.mark.parametrize("domain,halo", [((150, 97, 6), (2, 2, 0)), ((77, 45, 3), (3, 3, 1))])
+def test_hdiff_pair_tma(domain, halo, lib):
+    """The TMA-staged tile computes the same pair arithmetic as TILE: same bits."""
+    got, want = _hdiff(domain, halo, tune=_native.tune(variant=_native.HDIFF_TMA), seed=22, alignment=64)
+    _check(got, want, HDIFF_TOL, f"hdiff pair tma {domain}")
+    tile, _ = _hdiff(domain, halo, tune=_native.tune(variant=_native.HDIFF_TILE, block_x=64, block_y=4,
+                                                     tile_y=16, k_per_cta=8), seed=22, alignment=64)
+    assert np.array_equal(got.view(np.uint64), tile.view(np.uint64))
 
 
 def _vadv(domain, halo, tune=None, seed=0, shift=(1, 0), use_scratch=False):

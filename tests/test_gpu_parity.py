@@ -137,6 +137,47 @@ def test_hdiff_jscan_tunings(storage, compute, nw, ty, kper, unroll, lib):
     _assert_bits(got, want, f"hdiff jscan {nw} {ty} {kper} {unroll} {storage}")
 
 
+# TMA staging needs i unit-stride and j/k strides that are multiples of 16
+# bytes (alignment=64 pads rows); the halo corner may sit at any element
+# offset from a 16-byte boundary (halo 3 and 9 move it).
+@pytest.mark.parametrize("storage,compute", FORMS)
+@pytest.mark.parametrize("bx,by,ty,kper", [(64, 4, 16, 8), (32, 8, 8, 3), (64, 8, 40, 2), (128, 2, 4, 1),
+                                           (128, 4, 12, 5)])
+def test_hdiff_tma(storage, compute, bx, by, ty, kper, lib):
+    t = _native.tune(variant=_native.HDIFF_TMA, block_x=bx, block_y=by, tile_y=ty, k_per_cta=kper)
+    got, want, _ = _run_hdiff((131, 70, 11), (2, 2, 0), storage, compute, alignment=64, tune=t, seed=31)
+    _assert_bits(got, want, f"hdiff tma {bx}x{by} ty{ty} k{kper} {storage}/{compute}")
+
+
+@pytest.mark.parametrize("storage", ["float64", "float32", "bfloat16"])
+@pytest.mark.parametrize("domain,halo", [((77, 45, 3), (3, 3, 1)), ((40, 21, 9), (9, 2, 0)),
+                                         ((33, 130, 2), (2, 4, 2)), ((1, 1, 1), (2, 2, 0)),
+                                         ((64, 16, 5), (5, 2, 3))])
+def test_hdiff_tma_corner_offsets(storage, domain, halo, lib):
+    compute = "float64" if storage == "float64" else "float32"
+    t = _native.tune(variant=_native.HDIFF_TMA)
+    got, want, _ = _run_hdiff(domain, halo, storage, compute, alignment=64, tune=t, seed=32)
+    _assert_bits(got, want, f"hdiff tma {domain} {halo} {storage}")
+
+
+@pytest.mark.parametrize("layout,alignment", [((2, 1, 0), 0), ((0, 1, 2), 64)])
+def test_hdiff_tma_rejects_unqualified_layouts(layout, alignment, lib):
+    """Rows of 135 float32 (540 bytes) or a strided i axis cannot be described
+    to the TMA unit: the call fails with SB_ERR_UNSUPPORTED, nothing runs."""
+    t = _native.tune(variant=_native.HDIFF_TMA)
+    with pytest.raises(_native.SbError) as err:
+        _run_hdiff((131, 70, 3), (2, 2, 0), "float32", "float32", layout=layout, alignment=alignment, tune=t)
+    assert err.value.code == _native.SB_ERR_UNSUPPORTED
+    assert "TMA" in err.value.message
+
+
+def test_hdiff_tma_full_size_fp32(lib):
+    """512x512x80 float32 through the TMA variant, against the oracle."""
+    t = _native.tune(variant=_native.HDIFF_TMA)
+    got, want, _ = _run_hdiff((512, 512, 80), (2, 2, 0), "float32", "float32", alignment=64, tune=t, seed=33)
+    _assert_bits(got, want, "hdiff tma 512x512x80 float32")
+
+
 def test_hdiff_special_values(lib):
     """Ties, zeros, signed zeros, tiny and huge values, inf and nan."""
     domain, halo = (40, 12, 3), (2, 2, 0)
