@@ -70,6 +70,11 @@ extern "C" {
 #define SB_HDIFF_TMA 3    /* TILE with inp k-planes staged by TMA (cp.async.bulk.tensor)
                            * into two shared-memory stages (i unit-stride, 16-byte
                            * aligned j/k strides and halo corner)                   */
+#define SB_HDIFF_VSCAN 4  /* JSCAN with V columns per lane moved as one aligned
+                           * vector (block_x = strip width 32*V: 64 for 8-byte,
+                           * 128 for 4-byte, 128 or 256 for 2-byte storage); i
+                           * unit-stride, j/k strides multiples of the vector,
+                           * inp/coeff/out at one offset from a vector boundary */
 #define SB_VADV_SMEM 1    /* one thread per column, ccol/dcol in shared memory     */
 #define SB_VADV_GLOBAL 2  /* one thread per column, ccol/dcol in caller scratch    */
 #define SB_VADV_SLAB 3    /* persistent threads, factors in compact per-thread slabs of

@@ -286,6 +286,44 @@ __device__ __forceinline__ f32x2 cvt<f32x2, double>(double v) { return f32x2_fro
 template <>
 __device__ __forceinline__ f32x2 cvt<f32x2, f32x2>(f32x2 v) { return v; }
 
+// V consecutive storage elements moved as one aligned vector of V*sizeof(S)
+// bytes (4, 8 or 16), converted to / rounded from compute type C per element.
+template <int B>
+struct RawVec;
+template <>
+struct RawVec<4> {
+    using T = unsigned;
+};
+template <>
+struct RawVec<8> {
+    using T = uint2;
+};
+template <>
+struct RawVec<16> {
+    using T = uint4;
+};
+
+template <class S, class C, int V>
+__device__ __forceinline__ void ld_vec(const S* p, C (&o)[V]) {
+    using R = typename RawVec<(int)sizeof(S) * V>::T;
+    const R r = __ldg(reinterpret_cast<const R*>(p));
+    S e[V];
+    memcpy(e, &r, sizeof(R));
+#pragma unroll
+    for (int q = 0; q < V; ++q) o[q] = cvt<C, S>(e[q]);
+}
+
+template <class S, class C, int V>
+__device__ __forceinline__ void st_vec(S* p, const C (&v)[V]) {
+    using R = typename RawVec<(int)sizeof(S) * V>::T;
+    S e[V];
+#pragma unroll
+    for (int q = 0; q < V; ++q) st<S, C>(&e[q], v[q]);
+    R r;
+    memcpy(&r, e, sizeof(R));
+    *reinterpret_cast<R*>(p) = r;
+}
+
 // ---------------------------------------------------------------------------
 // launch helpers
 // ---------------------------------------------------------------------------

@@ -171,6 +171,70 @@ int launch_jscan(const void* inp, const void* coeff, void* out, int64_t ni, int6
     return launch_jscan_idx<S, C, int64_t>(grid, block, stream, inp, coeff, out, ni, nj, nk, si, sj, sk, ty, kper, unroll);
 }
 
+// VSCAN: warp strips of 32*V columns (hdiff_vscan_strip), strip s = blockIdx.x
+// starting at column cs0 + s*step; the warps of a block take consecutive
+// TY-row tiles of that strip (few strips per domain, so no idle warps).
+template <class S, class C, int V, int U, class IDX>
+__global__ void __launch_bounds__(256)
+    hdiff_vscan_kernel(const S* __restrict__ inp, const S* __restrict__ coeff, S* __restrict__ out, int ni, int nj,
+                       int nk, IDX sj, IDX sk, int cs0, int step, int TY, int kper) {
+    const int strip = blockIdx.x;
+    const int j0 = (blockIdx.y * blockDim.y + threadIdx.y) * TY;
+    if (j0 >= nj) return;  // whole warp
+    const int j1 = min(nj, j0 + TY);
+    const int k0 = blockIdx.z * kper;
+    const int k1 = min(nk, k0 + kper);
+    for (int k = k0; k < k1; ++k)
+        hdiff_vscan_strip<S, C, V, U, IDX>(inp, coeff, out, ni, nj, sj, sk, cs0 + strip * step, step, threadIdx.x,
+                                           j0, j1, k);
+}
+
+// VSCAN launch if the layout qualifies: i unit-stride, j/k strides multiples
+// of the vector size, and inp / coeff / out at the same offset from a vector
+// boundary (then one column grid is vector-aligned in all three fields);
+// SB_ERR_UNSUPPORTED (no error text) if not.
+template <class S, class C, int V>
+int launch_vscan(const void* inp, const void* coeff, void* out, int64_t ni, int64_t nj, int64_t nk, int64_t si,
+                 int64_t sj, int64_t sk, int nw, int ty, int kper, int unroll, cudaStream_t stream,
+                 const DeviceProps* p) {
+    constexpr int ES = (int)sizeof(S), VB = V * ES;
+    if (si != 1 || sj <= 0 || sk <= 0 || (sj * ES) % VB || (sk * ES) % VB) return SB_ERR_UNSUPPORTED;
+    const uintptr_t a = (uintptr_t)inp;
+    if (a % ES || (uintptr_t)coeff % VB != a % VB || (uintptr_t)out % VB != a % VB) return SB_ERR_UNSUPPORTED;
+    SB_CHECK(nw >= 1 && nw <= 8, SB_ERR_INVALID, "vscan: 1..8 warps per block");
+    SB_CHECK(ty >= 1 && kper >= 1, SB_ERR_INVALID, "vscan: tile_y and k_per_cta must be positive");
+    const int off = (int)((a % VB) / ES);
+    const int cs0 = -2 - (((off - 2) % V) + V) % V;  // <= -2, (off + cs0) % V == 0
+    const int step = 32 * V - V * ((4 + V - 1) / V);
+    const int64_t nstrips = ceil_div(ni - (cs0 + 2), (int64_t)step);
+    const int64_t gx = nstrips, gy = ceil_div(ceil_div(nj, ty), (int64_t)nw), gz = ceil_div(nk, kper);
+    SB_CHECK(gy <= p->max_grid_y && gz <= p->max_grid_z, SB_ERR_INVALID, "hdiff grid too large");
+    const dim3 grid((unsigned)gx, (unsigned)gy, (unsigned)gz), block(32, nw);
+    const int64_t lo = -(2 + V) - 2 * sj;
+    const int64_t hi = ni + 2 + 32 * V + (nj + 2) * sj + nk * sk;
+    const bool small = lo > -(1LL << 31) && hi < (1LL << 31);
+#define SB_VSCAN(UV, IDXT)                                                                                   \
+    hdiff_vscan_kernel<S, C, V, UV, IDXT><<<grid, block, 0, stream>>>(                                        \
+        (const S*)inp, (const S*)coeff, (S*)out, (int)ni, (int)nj, (int)nk, (IDXT)sj, (IDXT)sk, cs0, step,    \
+        ty, kper)
+#define SB_VSCAN_U(IDXT)                                                                                     \
+    switch (unroll) {                                                                                         \
+        case 1: SB_VSCAN(1, IDXT); break;                                                                     \
+        case 2: SB_VSCAN(2, IDXT); break;                                                                     \
+        case 4: SB_VSCAN(4, IDXT); break;                                                                     \
+        case 8: SB_VSCAN(8, IDXT); break;                                                                     \
+        default: return fail(SB_ERR_INVALID, "vscan unroll must be 1, 2, 4 or 8 (got %d)", unroll);           \
+    }
+    if (small) {
+        SB_VSCAN_U(int)
+    } else {
+        SB_VSCAN_U(int64_t)
+    }
+#undef SB_VSCAN_U
+#undef SB_VSCAN
+    return SB_OK;
+}
+
 template <class S, class C, int TX, int NTY>
 int launch_tile(const void* inp, const void* coeff, void* out, int64_t ni, int64_t nj, int64_t nk,
                 int64_t si, int64_t sj, int64_t sk, int ty, int kper, cudaStream_t stream,
@@ -443,12 +507,23 @@ int launch_typed(const void* inp, const void* coeff, void* out, int64_t ni, int6
             if (rc_tma != SB_ERR_UNSUPPORTED) return rc_tma;
         }
     }
+    // bfloat16 storage and float-pair compute: vector strips (V columns per
+    // lane) issue fewer instructions per point than JSCAN (56 vs 62 us and
+    // 271 vs 313 us at 512x512x80); float32 stays on JSCAN (52 vs 59 us).
+    if constexpr (std::is_same<S, bf16>::value || std::is_same<C, f32x2>::value) {
+        if (variant == SB_VARIANT_AUTO) {
+            constexpr int V = sizeof(S) == 8 ? 2 : 4;
+            const int rc_v = launch_vscan<S, C, V>(inp, coeff, out, ni, nj, nk, si, sj, sk, 1, 16, 1, 1, stream, p);
+            if (rc_v != SB_ERR_UNSUPPORTED) return rc_v;
+        }
+    }
     if (variant == SB_VARIANT_AUTO) variant = auto_tile ? SB_HDIFF_TILE : SB_HDIFF_JSCAN;
     if constexpr (std::is_same<C, fix64>::value) {
         SB_CHECK(variant == SB_HDIFF_JSCAN, SB_ERR_UNSUPPORTED, "fixed-point hdiff runs as JSCAN strips only");
     }
-    SB_CHECK(variant == SB_HDIFF_TILE || variant == SB_HDIFF_JSCAN || variant == SB_HDIFF_TMA, SB_ERR_UNSUPPORTED,
-             "hdiff variant %d is not available", variant);
+    SB_CHECK(variant == SB_HDIFF_TILE || variant == SB_HDIFF_JSCAN || variant == SB_HDIFF_TMA ||
+                 variant == SB_HDIFF_VSCAN,
+             SB_ERR_UNSUPPORTED, "hdiff variant %d is not available", variant);
     if (variant == SB_HDIFF_TMA) {
         if constexpr (std::is_same<C, fix64>::value) {
             return fail(SB_ERR_UNSUPPORTED, "fixed-point hdiff runs as JSCAN strips only");
@@ -470,6 +545,44 @@ int launch_typed(const void* inp, const void* coeff, void* out, int64_t ni, int6
             SB_CHECK(rc2 != SB_ERR_UNSUPPORTED, SB_ERR_UNSUPPORTED,
                      "hdiff TMA: needs blocks 32x8, 64x{4,8} or 128x{2,4}, i unit-stride, 16-byte aligned j/k "
                      "strides and halo corner, tile rows in [block_y, 252]");
+            return rc2;
+        }
+    }
+    if (variant == SB_HDIFF_VSCAN) {
+        if constexpr (std::is_same<C, fix64>::value) {
+            return fail(SB_ERR_UNSUPPORTED, "fixed-point hdiff runs as JSCAN strips only");
+        } else {
+            const int nw = (tune && tune->block_y > 0) ? tune->block_y : 4;
+            const int ty = (tune && tune->tile_y > 0) ? tune->tile_y : 32;
+            const int kper = (tune && tune->k_per_cta > 0) ? tune->k_per_cta : 1;
+            const int unroll = (tune && tune->unroll > 0) ? tune->unroll : 4;
+            constexpr int VDEF = (int)(16 / sizeof(S)) > 4 ? 4 : (int)(16 / sizeof(S));
+            const int width = (tune && tune->block_x > 0) ? tune->block_x : 32 * VDEF;
+            int rc2 = SB_ERR_UNSUPPORTED;
+            bool shape_ok = false;
+            if constexpr (sizeof(S) == 8) {
+                if (width == 64) {
+                    shape_ok = true;
+                    rc2 = launch_vscan<S, C, 2>(inp, coeff, out, ni, nj, nk, si, sj, sk, nw, ty, kper, unroll, stream, p);
+                }
+            } else if constexpr (sizeof(S) == 4) {
+                if (width == 128) {
+                    shape_ok = true;
+                    rc2 = launch_vscan<S, C, 4>(inp, coeff, out, ni, nj, nk, si, sj, sk, nw, ty, kper, unroll, stream, p);
+                }
+            } else {
+                if (width == 128 || width == 256) shape_ok = true;
+                if (width == 128)
+                    rc2 = launch_vscan<S, C, 4>(inp, coeff, out, ni, nj, nk, si, sj, sk, nw, ty, kper, unroll, stream, p);
+                if (width == 256)
+                    rc2 = launch_vscan<S, C, 8>(inp, coeff, out, ni, nj, nk, si, sj, sk, nw, ty, kper, unroll, stream, p);
+            }
+            SB_CHECK(shape_ok, SB_ERR_INVALID,
+                     "hdiff vscan strip width (block_x) must be 64 for 8-byte, 128 for 4-byte and 128 or 256 for "
+                     "2-byte storage (got %d)", width);
+            SB_CHECK(rc2 != SB_ERR_UNSUPPORTED, SB_ERR_UNSUPPORTED,
+                     "hdiff VSCAN: needs i unit-stride, j/k strides that are multiples of the %d-column vector and "
+                     "inp/coeff/out at the same offset from a vector boundary", width / 32);
             return rc2;
         }
     }

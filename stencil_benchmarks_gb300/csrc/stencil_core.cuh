@@ -81,6 +81,119 @@ __device__ __forceinline__ void hdiff_jscan_strip(const S* __restrict__ inp, con
 }
 
 // ---------------------------------------------------------------------------
+// horizontal diffusion, one warp, one k-plane strip of 32*V columns
+// ---------------------------------------------------------------------------
+// The JSCAN march with V columns per lane: lane L holds columns
+// c = cs + V*L + q (q < V) of each row, moved as one aligned vector of
+// V*sizeof(S) bytes (the caller picks cs so that column cs starts a vector).
+// Neighbours inside a lane's group are registers; across lanes four shuffles
+// per row serve V points (inp left/right, lap right, flx left).  Outputs are
+// the columns [cs+2, cs+2+step) within [0, ni).  A vector is loaded when it
+// holds at least one column of the halo'd row [-2, ni+2); its other columns
+// lie in the same aligned V*sizeof(S)-byte block of the caller's memory and
+// only feed points that are not stored.  Same arithmetic and order as
+// hdiff_jscan_strip.  All 32 lanes must call this (full-mask shuffles).
+template <class S, class C, int V, int U, class IDX>
+__device__ __forceinline__ void hdiff_vscan_strip(const S* __restrict__ inp, const S* __restrict__ coeff,
+                                                  S* __restrict__ out, int ni, int nj, IDX sj, IDX sk, int cs,
+                                                  int step, int lane, int j0, int j1, int k) {
+    using A = Ar<C>;
+    const int c0 = cs + V * lane;
+    const bool grp_in = c0 + V > -2 && c0 < ni + 2;
+    const int wlo = max(cs + 2, 0), whi = min(cs + 2 + step, ni);
+    const bool any_w = c0 + V > wlo && c0 < whi;
+    const bool all_w = c0 >= wlo && c0 + V <= whi;
+    const int rmax = nj + 1;
+    const IDX obase = (IDX)k * sk + (IDX)c0;
+    auto load_row = [&](int r, C(&o)[V]) {
+        if (grp_in && r <= rmax) {
+            ld_vec<S, C, V>(inp + (obase + (IDX)r * sj), o);
+        } else {
+#pragma unroll
+            for (int q = 0; q < V; ++q) o[q] = C(0);
+        }
+    };
+    // lap of the centre row c given the rows below (b) and above (a)
+    auto lap_row = [&](const C(&b)[V], const C(&c)[V], const C(&a)[V], C(&o)[V], C& right) {
+        const C left = shfl_up(c[V - 1], 1);  // column c0 - 1
+        right = shfl_down(c[0], 1);           // column c0 + V
+#pragma unroll
+        for (int q = 0; q < V; ++q) {
+            const C l = q == 0 ? left : c[q - 1];
+            const C r = q == V - 1 ? right : c[q + 1];
+            o[q] = A::sub(A::template scale2<2>(c[q]), A::add(A::add(A::add(r, l), a[q]), b[q]));
+        }
+    };
+    C am2[V], a0[V], a1[V], a2[V], lap_m1[V], lap0[V], fly_m1[V];
+    load_row(j0 - 2, am2);
+    load_row(j0 - 1, a0);
+    load_row(j0, a1);
+    load_row(j0 + 1, a2);
+    C unused, rnb0;
+    lap_row(am2, a0, a1, lap_m1, unused);  // lap(j0-1)
+    lap_row(a0, a1, a2, lap0, rnb0);       // lap(j0); rnb0 = inp(c0+V, j0)
+#pragma unroll
+    for (int q = 0; q < V; ++q) {
+        fly_m1[q] = A::limit(A::sub(lap0[q], lap_m1[q]), a1[q], a0[q]);  // fly(j0-1)
+        a0[q] = a1[q];
+        a1[q] = a2[q];
+    }
+    // state for output row j: a0 = inp(j), a1 = inp(j+1), lap0 = lap(j), rnb0 = inp(c0+V, j)
+    for (int jb = j0; jb < j1; jb += U) {
+        C nxt[U][V], cf[U][V];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int j = jb + u;
+            load_row(j + 2, nxt[u]);
+            if (any_w && j < j1) {
+                ld_vec<S, C, V>(coeff + (obase + (IDX)j * sj), cf[u]);
+            } else {
+#pragma unroll
+                for (int q = 0; q < V; ++q) cf[u][q] = C(0);
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int j = jb + u;
+            if (j >= j1) break;  // warp-uniform
+            C lap1[V], fly0[V], flx0[V], res[V], rnb1;
+            lap_row(a0, a1, nxt[u], lap1, rnb1);
+            const C lapR = shfl_down(lap0[0], 1);  // lap(c0+V, j)
+#pragma unroll
+            for (int q = 0; q < V; ++q) {
+                fly0[q] = A::limit(A::sub(lap1[q], lap0[q]), a1[q], a0[q]);
+                const C lr = q == V - 1 ? lapR : lap0[q + 1];
+                const C ir = q == V - 1 ? rnb0 : a0[q + 1];
+                flx0[q] = A::limit(A::sub(lr, lap0[q]), ir, a0[q]);
+            }
+            const C flxL = shfl_up(flx0[V - 1], 1);  // flx(c0-1, j)
+#pragma unroll
+            for (int q = 0; q < V; ++q) {
+                const C fl = q == 0 ? flxL : flx0[q - 1];
+                const C d = A::sub(A::add(A::sub(flx0[q], fl), fly0[q]), fly_m1[q]);
+                res[q] = A::sub(a0[q], A::mul(cf[u][q], d));
+            }
+            S* orow = out + (obase + (IDX)j * sj);
+            if (all_w) {
+                st_vec<S, C, V>(orow, res);
+            } else if (any_w) {
+#pragma unroll
+                for (int q = 0; q < V; ++q)
+                    if (c0 + q >= wlo && c0 + q < whi) st<S, C>(orow + q, res[q]);
+            }
+#pragma unroll
+            for (int q = 0; q < V; ++q) {
+                a0[q] = a1[q];
+                a1[q] = nxt[u][q];
+                lap0[q] = lap1[q];
+                fly_m1[q] = fly0[q];
+            }
+            rnb0 = rnb1;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
 // horizontal diffusion in 64-bit fixed point (float64 storage), one warp strip
 // ---------------------------------------------------------------------------
 // lap, flx, fly and their sum S are additions only, so they are exact in

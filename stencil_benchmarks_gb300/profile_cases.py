@@ -12,7 +12,7 @@ measured launches (CUDA events), prints one line per case, and frees its
 fields before the next case.  The kernel variants are the defaults of the
 library, except vadv-f64 and vadv-f32x2, which use the caller-scratch
 (GLOBAL) variant as ``bench.py`` does.  ``:<variant>`` picks another one
-(hdiff: tile, jscan, tma -- tma with rows padded to 64 bytes so that the
+(hdiff: tile, jscan, tma, vscan -- tma with rows padded to 64 bytes so that the
 j/k strides suit the tensor copies; vadv: smem, global, slab -- global and
 slab with ccol/dcol scratch fields).
 """
@@ -49,6 +49,7 @@ def _field(rng, storage, halo, lo, hi, alignment=0):
 
 
 VARIANTS = {"tile": _native.HDIFF_TILE, "jscan": _native.HDIFF_JSCAN, "tma": _native.HDIFF_TMA,
+            "vscan": _native.HDIFF_VSCAN,
             "smem": _native.VADV_SMEM,
             "global": _native.VADV_GLOBAL, "slab": _native.VADV_SLAB}
 

@@ -68,6 +68,15 @@ def test_hdiff_pair(variant, domain, halo, layout, lib):
 
 
 @pytest.mark.parametrize("domain,halo", [((150, 97, 6), (2, 2, 0)), ((77, 45, 3), (3, 3, 1))])
+def test_hdiff_pair_vscan(domain, halo, lib):
+    """Vector strips compute the same pair arithmetic per point as JSCAN: same bits."""
+    got, want = _hdiff(domain, halo, tune=_native.tune(variant=_native.HDIFF_VSCAN), seed=23, alignment=64)
+    _check(got, want, HDIFF_TOL, f"hdiff pair vscan {domain}")
+    ref, _ = _hdiff(domain, halo, tune=_native.tune(variant=_native.HDIFF_JSCAN), seed=23, alignment=64)
+    assert np.array_equal(got.view(np.uint64), ref.view(np.uint64))
+
+
+@pytest.mark.parametrize("domain,halo", [((150, 97, 6), (2, 2, 0)), ((77, 45, 3), (3, 3, 1))])
 def test_hdiff_pair_tma(domain, halo, lib):
     """The TMA-staged tile computes the same pair arithmetic as TILE: same bits."""
     got, want = _hdiff(domain, halo, tune=_native.tune(variant=_native.HDIFF_TMA), seed=22, alignment=64)

@@ -178,6 +178,63 @@ def test_hdiff_tma_full_size_fp32(lib):
     _assert_bits(got, want, "hdiff tma 512x512x80 float32")
 
 
+VSCAN_WIDTHS = {"float64": (64,), "float32": (128,), "bfloat16": (128, 256)}
+
+
+@pytest.mark.parametrize("storage,compute", FORMS)
+@pytest.mark.parametrize("nw,ty,kper,unroll", [(1, 1, 1, 1), (2, 7, 3, 2), (4, 32, 1, 4), (8, 64, 2, 8),
+                                               (3, 5, 4, 4)])
+def test_hdiff_vscan(storage, compute, nw, ty, kper, unroll, lib):
+    """Vector strips (V columns per lane): same bits as the oracle for every
+    strip width, including strips that end inside a vector."""
+    for width in VSCAN_WIDTHS[storage]:
+        t = _native.tune(variant=_native.HDIFF_VSCAN, block_x=width, block_y=nw, tile_y=ty, k_per_cta=kper,
+                         unroll=unroll)
+        got, want, _ = _run_hdiff((261, 67, 5), (2, 2, 0), storage, compute, alignment=64, tune=t, seed=34)
+        _assert_bits(got, want, f"hdiff vscan {width} {nw} {ty} {kper} {unroll} {storage}/{compute}")
+
+
+@pytest.mark.parametrize("storage", ["float64", "float32", "bfloat16"])
+@pytest.mark.parametrize("domain,halo", [((77, 45, 3), (3, 3, 1)), ((40, 21, 9), (9, 2, 0)),
+                                         ((33, 130, 2), (2, 4, 2)), ((1, 1, 1), (2, 2, 0)),
+                                         ((64, 16, 5), (5, 2, 3)), ((124, 9, 2), (2, 2, 0)),
+                                         ((125, 9, 2), (7, 2, 0))])
+def test_hdiff_vscan_offsets(storage, domain, halo, lib):
+    """Every offset of the interior from a vector boundary (halo 2..9) and
+    domains one column either side of a strip boundary."""
+    compute = "float64" if storage == "float64" else "float32"
+    for width in VSCAN_WIDTHS[storage]:
+        t = _native.tune(variant=_native.HDIFF_VSCAN, block_x=width)
+        got, want, _ = _run_hdiff(domain, halo, storage, compute, alignment=64, tune=t, seed=35)
+        _assert_bits(got, want, f"hdiff vscan {width} {domain} {halo} {storage}")
+
+
+@pytest.mark.parametrize("layout,alignment", [((2, 1, 0), 0), ((0, 1, 2), 64)])
+def test_hdiff_vscan_rejects_unqualified_layouts(layout, alignment, lib):
+    t = _native.tune(variant=_native.HDIFF_VSCAN)
+    with pytest.raises(_native.SbError) as err:
+        _run_hdiff((131, 70, 3), (2, 2, 0), "float32", "float32", layout=layout, alignment=alignment, tune=t)
+    assert err.value.code == _native.SB_ERR_UNSUPPORTED
+    assert "VSCAN" in err.value.message
+
+
+def test_hdiff_vscan_rejects_bad_width(lib):
+    t = _native.tune(variant=_native.HDIFF_VSCAN, block_x=64)
+    with pytest.raises(_native.SbError) as err:
+        _run_hdiff((64, 8, 2), (2, 2, 0), "float32", "float32", alignment=64, tune=t)
+    assert err.value.code == _native.SB_ERR_INVALID
+
+
+def test_hdiff_vscan_full_size(lib):
+    """512x512x80 float32 and bfloat16 through vector strips, against the oracle
+    (unpadded rows of 516 elements: 16-byte vectors for float32, 8-byte for
+    bfloat16)."""
+    for storage, width in (("float32", 128), ("bfloat16", 128)):
+        t = _native.tune(variant=_native.HDIFF_VSCAN, block_x=width)
+        got, want, _ = _run_hdiff((512, 512, 80), (2, 2, 0), storage, "float32", tune=t, seed=36)
+        _assert_bits(got, want, f"hdiff vscan 512x512x80 {storage}")
+
+
 def test_hdiff_special_values(lib):
     """Ties, zeros, signed zeros, tiny and huge values, inf and nan."""
     domain, halo = (40, 12, 3), (2, 2, 0)
