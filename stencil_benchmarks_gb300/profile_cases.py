@@ -13,8 +13,8 @@ fields before the next case.  The kernel variants are the defaults of the
 library, except vadv-f64 and vadv-f32x2, which use the caller-scratch
 (GLOBAL) variant as ``bench.py`` does.  ``:<variant>`` picks another one
 (hdiff: tile, jscan, tma, vscan -- tma with rows padded to 64 bytes so that the
-j/k strides suit the tensor copies; vadv: smem, global, slab -- global and
-slab with ccol/dcol scratch fields).
+j/k strides suit the tensor copies; vadv: smem, global, slab, wslab -- global,
+slab and wslab with ccol/dcol scratch fields).
 """
 
 from __future__ import annotations
@@ -50,7 +50,7 @@ def _field(rng, storage, halo, lo, hi, alignment=0):
 
 VARIANTS = {"tile": _native.HDIFF_TILE, "jscan": _native.HDIFF_JSCAN, "tma": _native.HDIFF_TMA,
             "vscan": _native.HDIFF_VSCAN,
-            "smem": _native.VADV_SMEM,
+            "smem": _native.VADV_SMEM, "wslab": _native.VADV_WSLAB,
             "global": _native.VADV_GLOBAL, "slab": _native.VADV_SLAB}
 
 
@@ -82,7 +82,7 @@ def run_case(name, warmup, launches, rng):
             scratch = {}
             tune = None
             scratch_storage = "float64" if compute in ("float64", "float32x2") else "float32"
-            if variant in ("global", "slab") or (not variant and form in ("f64", "f32x2")):
+            if variant in ("global", "slab", "wslab") or (not variant and form in ("f64", "f32x2")):
                 scratch = {"ccol": _field(rng, scratch_storage, (1, 1, 0), 0.0, 0.0),
                            "dcol": _field(rng, scratch_storage, (1, 1, 0), 0.0, 0.0)}
             if variant == "slab":  # the bench's tunings for f64 and f32x2
