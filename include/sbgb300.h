@@ -86,6 +86,11 @@ extern "C" {
                            * SB_VARIANT_AUTO with ccol/dcol given and no block/unroll
                            * in the tune picks WSLAB for 2/4-byte storage and SLAB
                            * for 8-byte storage when the layout qualifies */
+#define SB_VADV_TMEM 5    /* float32 compute: WSLAB row staging, factors in tensor
+                           * memory (tcgen05.st / tcgen05.ld) instead of a slab; one
+                           * persistent block per SM; no scratch; needs i unit-stride
+                           * and 2 <= nk <= 256; unroll = ring depth 4, 8 or 16
+                           * (0: deepest that fits) */
 
 /*
  * Launch tuning.  Zero in any field means "choose the default".  The

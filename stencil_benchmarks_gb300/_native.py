@@ -37,7 +37,7 @@ STREAM_INIT, STREAM_COPY, STREAM_SCALE, STREAM_ADD, STREAM_TRIAD = range(5)
 
 VARIANT_AUTO = 0
 HDIFF_TILE, HDIFF_JSCAN, HDIFF_TMA, HDIFF_VSCAN = 1, 2, 3, 4
-VADV_SMEM, VADV_GLOBAL, VADV_SLAB, VADV_WSLAB = 1, 2, 3, 4
+VADV_SMEM, VADV_GLOBAL, VADV_SLAB, VADV_WSLAB, VADV_TMEM = 1, 2, 3, 4, 5
 
 DTYPE_CODES = {"float64": SB_F64, "float32": SB_F32, "bfloat16": SB_BF16, "float32x2": SB_F32X2,
                "fixed64": SB_FIX64}

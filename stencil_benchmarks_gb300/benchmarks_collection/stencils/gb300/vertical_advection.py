@@ -14,7 +14,10 @@ at the column shifted by (1, 0), (0, 1) and (0, 0) for u, v and w
   L2-resident slabs of ``ccol``/``dcol`` (fastest float64 and float-pair
   form);
 * ``NoAlloc``       -- factors in the library's static scratch array
-  (``sb_vadv_noalloc``), for callers that cannot allocate device memory.
+  (``sb_vadv_noalloc``), for callers that cannot allocate device memory;
+* ``TensorMem``     -- float32 compute: rows staged per warp, factors in the
+  SM's tensor memory (one persistent block per SM; fastest float32 and, with
+  16-byte-multiple level strides, bfloat16 form).
 """
 
 from __future__ import annotations
@@ -114,3 +117,19 @@ class NoAlloc(VerticalAdvectionMixin, base.VerticalAdvectionStencil):
             ni, nj, nk, *stage.strides, shift[0], shift[1], _stream_arg(None), ctypes.byref(t) if timed else None,
         )
         return t.value if timed else None
+
+
+class TensorMem(VerticalAdvectionMixin, base.VerticalAdvectionStencil):
+    dtype = Parameter("data type: float32 or bfloat16 (float32 compute)", "float32")
+    unroll_factor = Parameter("levels of inputs kept in flight (4, 8 or 16)", 8, choices=[4, 8, 16])
+
+    def setup(self):
+        super().setup()
+        if self.compute != "float32":
+            raise ParameterError("TensorMem keeps float32 factors in tensor memory: float32 compute only")
+        if self.domain[2] > 256:
+            raise ParameterError("TensorMem holds at most 256 levels per column")
+
+    def launch_component(self, f, named, shift, timed):
+        tune = _native.tune(variant=_native.VADV_TMEM, unroll=self.unroll_factor)
+        return kernels.vadv(*f, named["wcon"], shift, compute=self.compute, tune=tune, timed=timed)

@@ -894,4 +894,246 @@ __device__ __forceinline__ void vadv_warp_column(const S* __restrict__ stage, co
     cp_async_wait<0>();
 }
 
+// ---------------------------------------------------------------------------
+// vertical advection, one warp, factors in tensor memory (TMEM)
+// ---------------------------------------------------------------------------
+// The WSLAB march (rows staged by the warp with 16-byte cp.async chunks) with
+// float32 compute, but each thread keeps its column's factors ccol(k),
+// dcol(k) in its own TMEM lane instead of a global slab: level k at columns
+// 2k, 2k+1 of the warp's column range, written with one tcgen05.st per
+// level and read back eight levels at a time with tcgen05.ld ...x16.  Only
+// pos rows are staged for the backward sweep.  `tcol` is the TMEM address
+// of lane 0 / column 0 of this warp's range (lane field 32 * (warp % 4)); the
+// range holds 2 * ceil(nk / 8) * 8 columns.  All 32 lanes must call this.
+__device__ __forceinline__ void tmem_st2(uint32_t taddr, float a, float b) {
+    asm volatile("tcgen05.st.sync.aligned.32x32b.x2.b32 [%0], {%1, %2};\n" ::"r"(taddr), "r"(__float_as_uint(a)),
+                 "r"(__float_as_uint(b))
+                 : "memory");
+}
+__device__ __forceinline__ void tmem_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;\n" ::: "memory"); }
+// 16 consecutive columns of this thread's lane; returns after the load completed
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&f)[16]) {
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+        "%15}, [%16];\n"
+        "tcgen05.wait::ld.sync.aligned;\n"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+          "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr)
+        : "memory");
+#pragma unroll
+    for (int q = 0; q < 16; ++q) f[q] = __uint_as_float(r[q]);
+}
+
+// KA: the level stride sk * sizeof(S) is a multiple of 16 bytes, so every
+// level's rows share level 0's offsets within their 16-byte granules: the
+// copy addresses advance by a constant and the staged rows sit at fixed
+// ring offsets (far fewer instructions per level).
+template <class S, int D, bool KA, class IDX>
+__device__ __forceinline__ void vadv_tmem_column(const S* __restrict__ stage, const S* __restrict__ pos,
+                                                 const S* __restrict__ tens, const S* tensstage,
+                                                 const S* __restrict__ wcon, S* out, IDX col0, int lane, int nvalid,
+                                                 int nk, IDX sk, IDX wsh, uint32_t tcol, unsigned char* ring) {
+    using C = float;
+    using A = Ar<C>;
+    using W = WarpRing<S, C, D>;
+    constexpr int R = W::R, ES = W::ES, CPR = W::CPR, ROWB = W::ROWB, SLOT = W::SLOT;
+    constexpr int MF = (6 * CPR + 31) / 32;  // forward chunks per lane
+    constexpr int MB = (CPR + 31) / 32;      // backward chunks per lane (pos only)
+    const C dtr = konst<C>(3.0 / 20.0);
+    const bool valid = lane < nvalid;
+    const IDX col = col0 + (IDX)(valid ? lane : nvalid - 1);
+    const int64_t kstep = (int64_t)sk * ES;  // bytes from level k to k+1 in a field
+    const int nbytes = nvalid * ES;
+
+    // forward rows at level k: wcon(k+1) shifted, wcon(k+1), stage(k+1), pos(k), tens(k), tensstage(k)
+    const unsigned char* const g0 = (const unsigned char*)(wcon + col0 + sk + wsh);
+    const unsigned char* const g1 = (const unsigned char*)(wcon + col0 + sk);
+    const unsigned char* const g2 = (const unsigned char*)(stage + col0 + sk);
+    const unsigned char* const g3 = (const unsigned char*)(pos + col0);
+    const unsigned char* const g4 = (const unsigned char*)(tens + col0);
+    const unsigned char* const g5 = (const unsigned char*)(tensstage + col0);
+    auto gsel = [&](int r) -> const unsigned char* {  // r is per lane: selects, not an indexed array
+        return r == 0 ? g0 : r == 1 ? g1 : r == 2 ? g2 : r == 3 ? g3 : r == 4 ? g4 : g5;
+    };
+    unsigned mis0[6];
+#pragma unroll
+    for (int f = 0; f < 6; ++f) mis0[f] = (unsigned)((uintptr_t)gsel(f) & 15u);
+    // chunk m of this lane: slot s = lane + 32 m -> row s / CPR, chunk s % CPR.  Level-0 source
+    // address and (KA) whether the chunk holds a byte of the row, fixed for all levels.
+    const unsigned char* cg[MF];
+    int cdst[MF], cidx[MF];
+    bool cuse[MF];
+#pragma unroll
+    for (int m = 0; m < MF; ++m) {
+        const int sidx = lane + 32 * m, r = sidx / CPR;
+        cidx[m] = r < 6 ? sidx % CPR : CPR;  // CPR = never issued
+        cdst[m] = (r < 6 ? r : 0) * ROWB + (sidx % CPR) * 16;
+        const unsigned char* g = gsel(r < 6 ? r : 0);
+        const uintptr_t a = (uintptr_t)g;
+        const int n = (int)(((a & 15u) + (unsigned)nbytes + 15u) >> 4);
+        cuse[m] = cidx[m] < n;
+        cg[m] = KA ? (const unsigned char*)((a & ~(uintptr_t)15) + 16 * (cuse[m] ? cidx[m] : 0)) : g;
+    }
+    auto issue = [&](int slot, int k) {
+        if (k < nk - 1) {  // uniform
+            const int64_t kb = (int64_t)k * kstep;
+#pragma unroll
+            for (int m = 0; m < MF; ++m) {
+                if constexpr (KA) {
+                    if (cuse[m]) cp_async<16>(ring + slot * SLOT + cdst[m], (const void*)(cg[m] + kb));
+                } else {
+                    const uintptr_t a = (uintptr_t)(cg[m] + kb);
+                    const int n = (int)(((a & 15u) + (unsigned)nbytes + 15u) >> 4);
+                    if (cidx[m] < n)
+                        cp_async<16>(ring + slot * SLOT + cdst[m],
+                                     (const void*)((a & ~(uintptr_t)15) + 16 * cidx[m]));
+                }
+            }
+        }
+        cp_async_commit();
+    };
+    // this lane's element of staged row f in slot 0 (KA: the same offset for every level)
+    const unsigned char* rowb[6];
+#pragma unroll
+    for (int f = 0; f < 6; ++f) rowb[f] = ring + f * ROWB + mis0[f] + lane * ES;
+    auto rd = [&](int slot, int f, unsigned kmis) -> C {
+        if constexpr (KA) {
+            return cvt<C, S>(*(const S*)(rowb[f] + slot * SLOT));
+        } else {
+            return cvt<C, S>(((const S*)(ring + slot * SLOT + f * ROWB + ((mis0[f] + kmis) & 15u)))[lane]);
+        }
+    };
+#pragma unroll
+    for (int u = 0; u < D; ++u) issue(u, 1 + u);
+
+    // ---- forward sweep, k = 0 (direct loads)
+    C gcv = A::template scale2<-2>(A::add(ld<C, S>(wcon + col + sk + wsh), ld<C, S>(wcon + col + sk)));
+    C cs = A::template scale2<-1>(gcv);
+    C sprev = ld<C, S>(stage + col);
+    C scur = ld<C, S>(stage + col + sk);
+    C dup = A::sub(scur, sprev);
+    C bcol = A::sub(dtr, cs);
+    C corr = A::mul(-cs, dup);
+    C dv = A::add(A::add(A::add(A::mul(dtr, ld<C, S>(pos + col)), ld<C, S>(tens + col)), ldc<C, S>(tensstage + col)), corr);
+    C cp = A::div(cs, bcol);
+    C dp = A::div(dv, bcol);
+    tmem_st2(tcol, cp, dp);
+
+    // ---- forward sweep, 0 < k < nk-1
+    for (int kb = 1; kb < nk - 1; kb += R) {
+#pragma unroll
+        for (int u = 0; u < R; ++u) {
+            const int k = kb + u;
+            if (k >= nk - 1) break;  // uniform
+            cp_async_wait<D - 1>();
+            __syncwarp();
+            const unsigned kmis = KA ? 0u : (unsigned)(((int64_t)k * kstep) & 15);
+            const C w1 = rd(u, 0, kmis), w0 = rd(u, 1, kmis);
+            const C snext = rd(u, 2, kmis), p0 = rd(u, 3, kmis);
+            const C t0 = rd(u, 4, kmis), ts0 = rd(u, 5, kmis);
+            issue((u + D) % R, k + D);  // the slot of level k-1: every lane has read it (__syncwarp above)
+            const C as_ = A::template scale2<-1>(-gcv);
+            gcv = A::template scale2<-2>(A::add(w1, w0));
+            cs = A::template scale2<-1>(gcv);
+            const C ddown = A::neg_diff(dup, scur, sprev);
+            dup = A::sub(snext, scur);
+            bcol = A::sub(A::sub(dtr, as_), cs);
+            corr = A::sub(A::mul(-as_, ddown), A::mul(cs, dup));
+            dv = A::add(A::add(A::add(A::mul(dtr, p0), t0), ts0), corr);
+            const C divided = A::rcp(A::sub(bcol, A::mul(cp, as_)));
+            cp = A::mul(cs, divided);
+            dp = A::mul(A::sub(dv, A::mul(dp, as_)), divided);
+            tmem_st2(tcol + 2u * (uint32_t)k, cp, dp);
+            sprev = scur;
+            scur = snext;
+        }
+    }
+    cp_async_wait<0>();
+    __syncwarp();
+
+    // ---- forward sweep, k = nk-1
+    {
+        const IDX o = col + (IDX)(nk - 1) * sk;
+        const C as_ = A::template scale2<-1>(-gcv);
+        bcol = A::sub(dtr, as_);
+        const C ddown = A::neg_diff(dup, scur, sprev);
+        corr = A::mul(-as_, ddown);
+        dv = A::add(A::add(A::add(A::mul(dtr, ld<C, S>(pos + o)), ld<C, S>(tens + o)), ldc<C, S>(tensstage + o)), corr);
+        dp = A::div(A::sub(dv, A::mul(dp, as_)), A::sub(bcol, A::mul(cp, as_)));
+    }
+    tmem_wait_st();
+
+    // ---- backward sweep: pos(k) of level k staged in slot (nk-2-k) % R
+    const unsigned char* const gb0 = (const unsigned char*)(pos + col0);
+    const unsigned mis_p = (unsigned)((uintptr_t)gb0 & 15u);
+    const unsigned char* bg[MB];
+    int bdst[MB], bidx[MB];
+    bool buse[MB];
+#pragma unroll
+    for (int m = 0; m < MB; ++m) {
+        const int sidx = lane + 32 * m;
+        bidx[m] = sidx < CPR ? sidx : CPR;
+        bdst[m] = (sidx < CPR ? sidx : 0) * 16;
+        const uintptr_t a = (uintptr_t)gb0;
+        const int n = (int)(((a & 15u) + (unsigned)nbytes + 15u) >> 4);
+        buse[m] = bidx[m] < n;
+        bg[m] = KA ? (const unsigned char*)((a & ~(uintptr_t)15) + 16 * (buse[m] ? bidx[m] : 0)) : gb0;
+    }
+    auto issue_b = [&](int slot, int k) {
+        if (k >= 0) {
+            const int64_t kb = (int64_t)k * kstep;
+#pragma unroll
+            for (int m = 0; m < MB; ++m) {
+                if constexpr (KA) {
+                    if (buse[m]) cp_async<16>(ring + slot * SLOT + bdst[m], (const void*)(bg[m] + kb));
+                } else {
+                    const uintptr_t a = (uintptr_t)(bg[m] + kb);
+                    const int n = (int)(((a & 15u) + (unsigned)nbytes + 15u) >> 4);
+                    if (bidx[m] < n)
+                        cp_async<16>(ring + slot * SLOT + bdst[m],
+                                     (const void*)((a & ~(uintptr_t)15) + 16 * bidx[m]));
+                }
+            }
+        }
+        cp_async_commit();
+    };
+#pragma unroll
+    for (int u = 0; u < D; ++u) issue_b(u, nk - 2 - u);
+    C data = dp;
+    if (valid) {
+        const IDX o = col + (IDX)(nk - 1) * sk;
+        st<S, C>(out + o, A::mul(dtr, A::sub(data, ld<C, S>(pos + o))));
+    }
+    const unsigned char* const prow = ring + mis_p + lane * ES;  // KA: pos element of slot 0
+    S* optr = out + col;
+    int slot = 0;  // ring slot of the next level
+    for (int w = (nk - 2) >> 3; w >= 0; --w) {
+        float f[16];  // ccol, dcol of levels 8w .. 8w+7
+        tmem_ld16(tcol + 16u * (uint32_t)w, f);
+#pragma unroll
+        for (int q = 7; q >= 0; --q) {
+            const int k = 8 * w + q;
+            if (k > nk - 2) continue;  // uniform
+            cp_async_wait<D - 1>();
+            __syncwarp();
+            C p0;
+            if constexpr (KA) {
+                p0 = cvt<C, S>(*(const S*)(prow + slot * SLOT));
+            } else {
+                const unsigned kp = (unsigned)(((int64_t)k * kstep) & 15);
+                p0 = cvt<C, S>(((const S*)(ring + slot * SLOT + ((mis_p + kp) & 15u)))[lane]);
+            }
+            const int refill = slot + D >= R ? slot + D - R : slot + D;  // the previous level's slot
+            issue_b(refill, k - D);
+            data = A::sub(f[2 * q + 1], A::mul(f[2 * q], data));
+            if (valid) st<S, C>(optr + (IDX)k * sk, A::mul(dtr, A::sub(data, p0)));
+            slot = slot + 1 == R ? 0 : slot + 1;
+        }
+    }
+    cp_async_wait<0>();
+    __syncwarp();
+}
+
 }  // namespace sb

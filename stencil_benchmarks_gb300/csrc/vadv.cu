@@ -333,6 +333,100 @@ int launch_wslab(int bx, int depth, int blocks_per_sm, const DeviceProps* p, cud
     return SB_ERR_UNSUPPORTED;
 }
 
+// ---------------------------------------------------------------------------
+// TMEM variant (float32 compute): one persistent block of 4*G warps per SM.
+// Warp w solves 32-column groups with vadv_tmem_column and keeps its
+// columns' factors in TMEM lanes 32*(w%4) .. +31 (the lanes warp w may
+// access), columns (w/4)*cpw .. +cpw-1 of the block's 512-column allocation.
+// The block allocates all 512 columns and asks for enough shared memory that
+// no second block shares its SM, so the allocation never waits.
+// ---------------------------------------------------------------------------
+template <class S, int D, bool KA>
+__global__ void __launch_bounds__(512, 1)
+    vadv_tmem_kernel(const S* __restrict__ stage, const S* __restrict__ pos, const S* __restrict__ tens,
+                     const S* tensstage, const S* __restrict__ wcon, S* out, int ni, int nj, int nk, int sj, int sk,
+                     int wsh, int cpw) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int nwarps = blockDim.x >> 5;
+    uint32_t* s_taddr = reinterpret_cast<uint32_t*>(smem_raw);
+    unsigned char* ring = smem_raw + 16 + warp * WarpRing<S, float, D>::BYTES;
+    if (warp == 0) {
+        const uint32_t dst = (uint32_t)__cvta_generic_to_shared(s_taddr), ncols = 512u;
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(dst), "r"(ncols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    const uint32_t tbase = *reinterpret_cast<volatile uint32_t*>(s_taddr);
+    const uint32_t tcol = tbase + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)((warp >> 2) * cpw);
+    const int gx = (ni + 31) / 32;
+    const int64_t ngroups = (int64_t)gx * nj;
+    for (int64_t g = (int64_t)blockIdx.x * nwarps + warp; g < ngroups; g += (int64_t)gridDim.x * nwarps) {
+        const int i0 = (int)(g % gx) * 32;
+        const int j = (int)(g / gx);
+        const int nvalid = min(32, ni - i0);
+        vadv_tmem_column<S, D, KA, int>(stage, pos, tens, tensstage, wcon, out, i0 + j * sj, lane, nvalid, nk, sk,
+                                        wsh, tcol, ring);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    if (warp == 0) {
+        const uint32_t ncols = 512u;
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tbase), "r"(ncols) : "memory");
+    }
+}
+
+template <class S, int D>
+int launch_tmem_one(int g4, int cpw, const DeviceProps* p, cudaStream_t stream, const void* stage, const void* pos,
+                    const void* tens, const void* tensstage, const void* wcon, void* out, int64_t ni, int64_t nj,
+                    int64_t nk, int64_t sj, int64_t sk, int64_t wsh) {
+    auto kernel = ((int64_t)sk * (int64_t)sizeof(S)) % 16 == 0 ? vadv_tmem_kernel<S, D, true> : vadv_tmem_kernel<S, D, false>;
+    // fewer warps per lane quarter when their rings do not fit
+    g4 = std::min<int64_t>(g4, (p->smem_optin - 16) / (4 * (int64_t)WarpRing<S, float, D>::BYTES));
+    if (g4 < 1) return SB_ERR_UNSUPPORTED;
+    const int nwarps = 4 * g4;
+    // at least 120 KB: one block per SM, so the 512-column allocation is free
+    const size_t smem = std::max<size_t>(16 + (size_t)nwarps * WarpRing<S, float, D>::BYTES, 120 * 1024);
+    if ((int64_t)smem > p->smem_optin) return SB_ERR_UNSUPPORTED;
+    SB_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const int64_t ngroups = ceil_div(ni, (int64_t)32) * nj;
+    const int64_t grid = std::min<int64_t>(p->sm_count, ceil_div(ngroups, (int64_t)nwarps));
+    kernel<<<(unsigned)grid, 32 * nwarps, smem, stream>>>((const S*)stage, (const S*)pos, (const S*)tens,
+                                                          (const S*)tensstage, (const S*)wcon, (S*)out, (int)ni,
+                                                          (int)nj, (int)nk, (int)sj, (int)sk, (int)wsh, cpw);
+    return SB_OK;
+}
+
+// TMEM variant if this launch qualifies (float32 compute, i unit-stride,
+// positive strides, 32-bit offsets, 2 <= nk <= 256); SB_ERR_UNSUPPORTED
+// otherwise.  depth 0 = the deepest ring that fits.
+template <class S, class C>
+int launch_tmem(int depth, const DeviceProps* p, cudaStream_t stream, const void* stage, const void* pos,
+                const void* tens, const void* tensstage, const void* wcon, void* out, int64_t ni, int64_t nj,
+                int64_t nk, int64_t si, int64_t sj, int64_t sk, int64_t wsh) {
+    if constexpr (!std::is_same<C, float>::value) {
+        return SB_ERR_UNSUPPORTED;
+    } else {
+        if (si != 1 || sj <= 0 || sk <= 0 || nk < 2 || nk > 256) return SB_ERR_UNSUPPORTED;
+        const int64_t span = (ni + 1) * si + nj * sj + (nk + 1) * sk;
+        if (span >= (1LL << 31) || (int64_t)ni * nj * nk >= (1LL << 31)) return SB_ERR_UNSUPPORTED;
+        const int cpw = 16 * (int)ceil_div(nk, (int64_t)8);  // ccol, dcol of ceil8(nk) levels
+        const int g4 = std::min(4, 512 / cpw);             // warps per TMEM lane quarter
+        int rc = SB_ERR_UNSUPPORTED;
+        if ((depth == 0 || depth == 16) && rc == SB_ERR_UNSUPPORTED)
+            rc = launch_tmem_one<S, 16>(g4, cpw, p, stream, stage, pos, tens, tensstage, wcon, out, ni, nj, nk, sj, sk, wsh);
+        if ((depth == 0 || depth == 8) && rc == SB_ERR_UNSUPPORTED)
+            rc = launch_tmem_one<S, 8>(g4, cpw, p, stream, stage, pos, tens, tensstage, wcon, out, ni, nj, nk, sj, sk, wsh);
+        if (depth == 4 && rc == SB_ERR_UNSUPPORTED)
+            rc = launch_tmem_one<S, 4>(g4, cpw, p, stream, stage, pos, tens, tensstage, wcon, out, ni, nj, nk, sj, sk, wsh);
+        return rc;
+    }
+}
+
 template <class S, class C>
 int launch_typed(const void* stage, const void* pos, const void* tens, const void* tensstage,
                  const void* wcon, void* out, void* ccol, void* dcol, int64_t ni, int64_t nj, int64_t nk,
@@ -347,6 +441,18 @@ int launch_typed(const void* stage, const void* pos, const void* tens, const voi
     SB_CHECK(bx * by <= 256 && bx >= 1 && by >= 1, SB_ERR_INVALID, "vadv block (%d, %d) exceeds 256 threads", bx, by);
     const size_t smem = 2 * sizeof(C) * (size_t)nk * (size_t)(bx * by);
     const bool can_global = ccol && dcol && sizeof(S) == sizeof(C);
+    // float32 compute, no explicit shape: factors in tensor memory (512x512x80
+    // float32 137 us against 171 us for WSLAB and 180 us for SMEM async;
+    // bfloat16 113 us when the level stride is a multiple of 16 bytes, else
+    // the staging address arithmetic makes it no faster than WSLAB / SMEM)
+    if constexpr (std::is_same<C, float>::value) {
+        if (variant == SB_VARIANT_AUTO && !(tune && (tune->block_x || tune->block_y || tune->unroll)) &&
+            (sizeof(S) == 4 || (sk * (int64_t)sizeof(S)) % 16 == 0)) {
+            const int arc = launch_tmem<S, C>(8, p, stream, stage, pos, tens, tensstage, wcon, out, ni, nj, nk, si,
+                                              sj, sk, wsh);
+            if (arc != SB_ERR_UNSUPPORTED) return arc;
+        }
+    }
     if (variant == SB_VARIANT_AUTO && ccol && dcol && !(tune && (tune->block_x || tune->block_y || tune->unroll))) {
         // scratch fields given and no explicit shape: the persistent slab forms
         // (row-staged for 2- and 4-byte storage), falling back below if the
@@ -363,8 +469,18 @@ int launch_typed(const void* stage, const void* pos, const void* tens, const voi
     }
     if (variant == SB_VARIANT_AUTO) variant = ((int64_t)smem <= p->smem_optin) ? SB_VADV_SMEM : SB_VADV_GLOBAL;
     SB_CHECK(variant == SB_VADV_SMEM || variant == SB_VADV_GLOBAL || variant == SB_VADV_SLAB ||
-                 variant == SB_VADV_WSLAB,
+                 variant == SB_VADV_WSLAB || variant == SB_VADV_TMEM,
              SB_ERR_UNSUPPORTED, "vadv variant %d is not available", variant);
+    if (variant == SB_VADV_TMEM) {
+        const int d = (tune && tune->unroll > 0) ? tune->unroll : 0;
+        SB_CHECK(d == 0 || d == 4 || d == 8 || d == 16, SB_ERR_INVALID, "vadv TMEM ring depth must be 4, 8 or 16");
+        const int rc2 = launch_tmem<S, C>(d, p, stream, stage, pos, tens, tensstage, wcon, out, ni, nj, nk, si, sj,
+                                          sk, wsh);
+        SB_CHECK(rc2 != SB_ERR_UNSUPPORTED, SB_ERR_UNSUPPORTED,
+                 "vadv TMEM variant: needs float32 compute, i unit-stride, positive strides, 32-bit offsets and "
+                 "2 <= nk <= 256");
+        return rc2;
+    }
     if (variant == SB_VADV_WSLAB) {
         SB_CHECK(ccol && dcol, SB_ERR_INVALID, "vadv WSLAB variant needs ccol/dcol scratch fields");
         const int d = (tune && tune->unroll > 0) ? tune->unroll : 4;

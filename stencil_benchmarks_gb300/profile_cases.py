@@ -13,7 +13,7 @@ fields before the next case.  The kernel variants are the defaults of the
 library, except vadv-f64 and vadv-f32x2, which use the caller-scratch
 (GLOBAL) variant as ``bench.py`` does.  ``:<variant>`` picks another one
 (hdiff: tile, jscan, tma, vscan -- tma with rows padded to 64 bytes so that the
-j/k strides suit the tensor copies; vadv: smem, global, slab, wslab -- global,
+j/k strides suit the tensor copies; vadv: smem, global, slab, wslab, tmem -- global,
 slab and wslab with ccol/dcol scratch fields).
 """
 
@@ -50,7 +50,7 @@ def _field(rng, storage, halo, lo, hi, alignment=0):
 
 VARIANTS = {"tile": _native.HDIFF_TILE, "jscan": _native.HDIFF_JSCAN, "tma": _native.HDIFF_TMA,
             "vscan": _native.HDIFF_VSCAN,
-            "smem": _native.VADV_SMEM, "wslab": _native.VADV_WSLAB,
+            "smem": _native.VADV_SMEM, "wslab": _native.VADV_WSLAB, "tmem": _native.VADV_TMEM,
             "global": _native.VADV_GLOBAL, "slab": _native.VADV_SLAB}
 
 

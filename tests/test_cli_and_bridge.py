@@ -26,7 +26,8 @@ def test_cli_command_tree():
     stencils = group.commands["stencils"].commands["gb300"]
     assert set(stencils.commands) >= {"basic", "horizontal-diffusion", "vertical-advection"}
     assert set(stencils.commands["horizontal-diffusion"].commands) == {"j-scan", "tile"}
-    assert set(stencils.commands["vertical-advection"].commands) == {"shared-mem", "global-scratch", "slab", "no-alloc"}
+    assert set(stencils.commands["vertical-advection"].commands) == {"shared-mem", "global-scratch", "slab", "no-alloc",
+                                                                     "tensor-mem"}
     assert set(stencils.commands["basic"].commands) >= {"copy", "laplacian", "onesided-average",
                                                         "symmetric-average"}
     assert "native" in group.commands["stream"].commands["gb300"].commands

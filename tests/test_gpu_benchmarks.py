@@ -48,6 +48,19 @@ def test_vadv_benchmark_forms(cls, all_components, lib):
     b.run()
 
 
+@pytest.mark.parametrize("dtype", ["float32", "bfloat16"])
+@pytest.mark.parametrize("all_components", [False, True])
+def test_vadv_tensor_mem_benchmark(dtype, all_components, lib):
+    """The reference's numpy verification of float32 / bfloat16-storage runs
+    with the factors in tensor memory."""
+    b = vertical_advection.TensorMem(domain=(64, 40, 30), halo=(1, 1, 1), dtype=dtype,
+                                     all_components=all_components)
+    for _ in range(2):
+        b.run()
+    with pytest.raises(benchmark.ParameterError):
+        vertical_advection.TensorMem(domain=(64, 40, 30), halo=(1, 1, 1), dtype="float64")
+
+
 @pytest.mark.parametrize("cls,compute", [(horizontal_diffusion.JScan, "fixed64"),
                                          (horizontal_diffusion.JScan, "float32x2"),
                                          (horizontal_diffusion.Tile, "float32x2"),

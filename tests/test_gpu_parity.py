@@ -324,6 +324,51 @@ def test_vadv_slab(variant, bx, depth, per_sm, storage, compute, lib):
         _assert_bits(got, want, f"vadv slab {variant} {bx} depth {depth} per_sm {per_sm} {domain}")
 
 
+@pytest.mark.parametrize("depth", [0, 4, 8, 16])
+@pytest.mark.parametrize("storage", ["float32", "bfloat16"])
+def test_vadv_tmem(depth, storage, lib):
+    """Factors in tensor memory: level counts around the 8-level load window
+    and the per-warp column ranges (nk 64 -> 16 warps, 80 -> 12, 128 -> 8,
+    256 -> 4 per block), row ends with 1 or 2 valid lanes, many column
+    groups per warp."""
+    t = _native.tune(variant=_native.VADV_TMEM, unroll=depth)
+    for domain in ((97, 19, 2), (97, 19, 3), (33, 40, 9), (130, 7, 41), (64, 5, 64), (40, 6, 80), (35, 3, 128),
+                   (34, 2, 137), (33, 2, 256)):
+        got, want = _run_vadv(domain, (1, 1, 0), storage, "float32", tune=t, seed=40 + domain[2])
+        _assert_bits(got, want, f"vadv tmem depth {depth} {storage} {domain}")
+
+
+@pytest.mark.parametrize("shift", [(1, 0), (0, 1), (0, 0)])
+def test_vadv_tmem_shifts_and_layouts(shift, lib):
+    t = _native.tune(variant=_native.VADV_TMEM)
+    got, want = _run_vadv((45, 20, 17), (1, 1, 1), "float32", "float32", tune=t, seed=12, shift=shift)
+    _assert_bits(got, want, f"vadv tmem shift {shift}")
+    got, want = _run_vadv((64, 8, 137), (1, 1, 0), "bfloat16", "float32", alignment=64, tune=t, seed=15,
+                          shift=shift)
+    _assert_bits(got, want, f"vadv tmem aligned bf16 shift {shift}")
+
+
+def test_vadv_tmem_full_size(lib):
+    """512x512x80 float32: 8192 column groups over 152 blocks of 12 warps."""
+    t = _native.tune(variant=_native.VADV_TMEM)
+    got, want = _run_vadv((512, 512, 80), (1, 1, 0), "float32", "float32", tune=t, seed=44)
+    _assert_bits(got, want, "vadv tmem 512x512x80")
+
+
+@pytest.mark.parametrize("storage,compute,domain,layout", [
+    ("float64", "float64", (40, 6, 9), (2, 1, 0)),    # float64 compute
+    ("float32", "float64", (40, 6, 9), (2, 1, 0)),    # float64 compute
+    ("float32", "float32", (40, 6, 257), (2, 1, 0)),  # nk > 256
+    ("float32", "float32", (40, 6, 9), (0, 1, 2)),    # i not unit-stride
+])
+def test_vadv_tmem_rejects(storage, compute, domain, layout, lib):
+    t = _native.tune(variant=_native.VADV_TMEM)
+    with pytest.raises(_native.SbError) as err:
+        _run_vadv(domain, (1, 1, 0), storage, compute, layout=layout, tune=t)
+    assert err.value.code == _native.SB_ERR_UNSUPPORTED
+    assert "TMEM" in err.value.message
+
+
 @pytest.mark.parametrize(
     "domain,halo,layout,alignment",
     [((5, 4, 2), (1, 1, 0), (2, 1, 0), 0), ((64, 8, 137), (1, 1, 0), (2, 1, 0), 64),
