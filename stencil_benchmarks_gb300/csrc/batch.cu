@@ -46,6 +46,8 @@ struct DevDomain {
     void* out;
     int64_t item_begin;  // first item of this domain in its queue
     int32_t items_i, items_j;
+    int32_t ka;  // vadv: the level stride is a multiple of 16 bytes (TMEM staging shortcut)
+    int32_t pad;
 };
 
 struct DevTable {
@@ -159,6 +161,69 @@ __global__ void __launch_bounds__(BT)
     }
 }
 
+// float32-compute vadv with the factors in tensor memory (vadv_tmem_column):
+// one persistent block of 4*G warps per SM and bucket; each warp takes
+// 32-column items of the bucket's domains from the bucket queue.  Columns of
+// TMEM per warp: cpw = 16 * ceil(cap / 8) for the bucket's largest nk.  The
+// block allocates all 512 columns and the launch asks for enough shared
+// memory that no other TMEM block shares its SM.
+template <class S, int D>
+__global__ void __launch_bounds__(512, 1)
+    batch_vadv_tmem_kernel(const DevTable* __restrict__ tab, unsigned long long* __restrict__ counter, int bucket,
+                           int cpw) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int first = tab->bucket_first[bucket], last = tab->bucket_first[bucket + 1];
+    const int64_t total = tab->bucket_items[bucket];
+    if (total == 0) return;  // whole block, before any TMEM allocation
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    uint32_t* s_taddr = reinterpret_cast<uint32_t*>(smem_raw);
+    unsigned char* ring = smem_raw + 16 + warp * WarpRing<S, float, D>::BYTES;
+    if (warp == 0) {
+        const uint32_t dst = (uint32_t)__cvta_generic_to_shared(s_taddr), ncols = 512u;
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(dst), "r"(ncols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    const uint32_t tbase = *reinterpret_cast<volatile uint32_t*>(s_taddr);
+    const uint32_t tcol = tbase + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)((warp >> 2) * cpw);
+    for (;;) {
+        unsigned long long item = 0;
+        if (lane == 0) item = atomicAdd(counter, 1ULL);
+        item = __shfl_sync(0xffffffffu, item, 0);
+        if ((int64_t)item >= total) break;  // whole warp
+        int lo = first, hi = last - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (tab->dom[mid].item_begin <= (int64_t)item) lo = mid; else hi = mid - 1;
+        }
+        const DevDomain& dm = tab->dom[lo];
+        const int64_t local = (int64_t)item - dm.item_begin;
+        const int i0 = (int)(local % dm.items_i) * 32;
+        const int j = (int)(local / dm.items_i);
+        const int nvalid = min(32, dm.ni - i0);
+        const int col0 = i0 + j * (int)dm.sj;
+        if (dm.ka)
+            vadv_tmem_column<S, D, true, int>((const S*)dm.f[0], (const S*)dm.f[1], (const S*)dm.f[2],
+                                              (const S*)dm.f[3], (const S*)dm.f[4], (S*)dm.out, col0, lane, nvalid,
+                                              dm.nk, (int)dm.sk, (int)dm.wsh, tcol, ring);
+        else
+            vadv_tmem_column<S, D, false, int>((const S*)dm.f[0], (const S*)dm.f[1], (const S*)dm.f[2],
+                                               (const S*)dm.f[3], (const S*)dm.f[4], (S*)dm.out, col0, lane, nvalid,
+                                               dm.nk, (int)dm.sk, (int)dm.wsh, tcol, ring);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    if (warp == 0) {
+        const uint32_t ncols = 512u;
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tbase), "r"(ncols) : "memory");
+    }
+}
+constexpr int kTmemDepth = 8;
+
 struct Kinds {
     void (*hdiff)(dim3, dim3, cudaStream_t, const DevTable*, unsigned long long*);
     void (*vadv32)(dim3, dim3, size_t, cudaStream_t, const DevTable*, unsigned long long*, int, int, int, void*);
@@ -167,6 +232,10 @@ struct Kinds {
     const void* vadv32_fn;
     const void* vadv64_fn;
     int storage_bytes, compute_bytes;
+    // float32 vadv with factors in tensor memory (nullptr for other compute types)
+    void (*vadv_tmem)(dim3, dim3, size_t, cudaStream_t, const DevTable*, unsigned long long*, int, int);
+    const void* vadv_tmem_fn;
+    int tmem_ring_bytes;  // staging ring per warp
 };
 
 template <class S, class C, int U, class IDX>
@@ -178,6 +247,12 @@ void run_vadv(dim3 g, dim3 b, size_t smem, cudaStream_t s, const DevTable* t, un
               int cap, int ring_offset, void* slab) {
     batch_vadv_kernel<S, C, BT, kVadvDepth, IDX, P, SLAB><<<g, b, smem, s>>>(t, c, bucket, cap, ring_offset,
                                                                              (P*)slab);
+}
+
+template <class S>
+void run_vadv_tmem(dim3 g, dim3 b, size_t smem, cudaStream_t s, const DevTable* t, unsigned long long* c,
+                   int bucket, int cpw) {
+    batch_vadv_tmem_kernel<S, kTmemDepth><<<g, b, smem, s>>>(t, c, bucket, cpw);
 }
 
 // hdiff computes in HC, vadv in VC with its recurrences in P
@@ -196,6 +271,15 @@ Kinds kinds_for() {
     k.vadv64_fn = (const void*)&batch_vadv_kernel<S, VC, 64, kVadvDepth, IDX, P, SLAB>;
     k.storage_bytes = sizeof(typename RingOf<S>::T);  // ring entry
     k.compute_bytes = sizeof(P);                      // factor entry
+    if constexpr (std::is_same<VC, float>::value && std::is_same<P, float>::value && std::is_same<IDX, int>::value) {
+        k.vadv_tmem = &run_vadv_tmem<S>;
+        k.vadv_tmem_fn = (const void*)&batch_vadv_tmem_kernel<S, kTmemDepth>;
+        k.tmem_ring_bytes = WarpRing<S, float, kTmemDepth>::BYTES;
+    } else {
+        k.vadv_tmem = nullptr;
+        k.vadv_tmem_fn = nullptr;
+        k.tmem_ring_bytes = 0;
+    }
     return k;
 }
 
@@ -246,6 +330,12 @@ struct sb_batch {
     cudaGraphExec_t exec = nullptr;
     bool graph_idx64 = false;
     int64_t total_items = 0;
+    // float32 vadv in tensor memory: possible for this batch's form and tune,
+    // used by the current domain set, used by the captured graph
+    bool tmem_capable = false, use_tmem = false, graph_tmem = false;
+    int tmem_block[kBuckets] = {}, tmem_cpw[kBuckets] = {};
+    int vadv_tmem_grid = 0;
+    size_t tmem_smem = 0;
 };
 
 namespace {
@@ -289,6 +379,8 @@ int capture_graph(sb_batch* b) {
         if (b->vadv_smem[q] > 48 * 1024)
             SB_CUDA(cudaFuncSetAttribute(vadv_fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b->vadv_smem[q]));
     }
+    if (b->use_tmem)
+        SB_CUDA(cudaFuncSetAttribute(k.vadv_tmem_fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b->tmem_smem));
     cudaStream_t s0 = b->streams[0];
     SB_CUDA(cudaStreamBeginCapture(s0, cudaStreamCaptureModeThreadLocal));
     cudaMemcpyAsync(b->dev_table, b->host_table, table_bytes(b->max_domains), cudaMemcpyHostToDevice, s0);
@@ -299,8 +391,12 @@ int capture_graph(sb_batch* b) {
     cudaEventRecord(b->joins[0], b->streams[1]);
     for (int q = 0; q < kBuckets; ++q) {
         cudaStreamWaitEvent(b->streams[2 + q], b->fork, 0);
-        vadv_run(dim3(b->vadv_grid[q]), dim3(b->vadv_block), b->vadv_smem[q], b->streams[2 + q], b->dev_table,
-                 b->counters + 1 + q, q, b->cap[q], b->ring_offset[q], b->slab[q]);
+        if (b->use_tmem)
+            k.vadv_tmem(dim3(b->vadv_tmem_grid), dim3(b->tmem_block[q]), b->tmem_smem, b->streams[2 + q],
+                        b->dev_table, b->counters + 1 + q, q, b->tmem_cpw[q]);
+        else
+            vadv_run(dim3(b->vadv_grid[q]), dim3(b->vadv_block), b->vadv_smem[q], b->streams[2 + q], b->dev_table,
+                     b->counters + 1 + q, q, b->cap[q], b->ring_offset[q], b->slab[q]);
         cudaEventRecord(b->joins[1 + q], b->streams[2 + q]);
     }
     for (int q = 0; q < 1 + kBuckets; ++q) cudaStreamWaitEvent(s0, b->joins[q], 0);
@@ -313,6 +409,7 @@ int capture_graph(sb_batch* b) {
     b->graph = graph;
     SB_CUDA(cudaGraphInstantiate(&b->exec, graph, 0));
     b->graph_idx64 = b->idx64;
+    b->graph_tmem = b->use_tmem;
     return SB_OK;
 }
 
@@ -370,6 +467,22 @@ int sb_batch_create(sb_batch** out, int storage, int compute, int max_domains, i
         const int vdef = k.slab ? std::min(fit, 8) : fit;
         const int vper = b->tune.vadv_blocks_per_sm > 0 ? std::min(b->tune.vadv_blocks_per_sm, fit) : vdef;
         b->vadv_grid[q] = p->sm_count * std::max(1, vper);
+    }
+    if (k.vadv_tmem && b->vadv_block == 32 && max_nk <= 256) {
+        // per bucket: TMEM columns per warp for its cap, warps per block as the
+        // 512 columns and the shared memory allow; >= 120 KB of shared memory
+        // keeps every other TMEM block off the SM
+        const int fit4 = (int)((p->smem_optin - 16) / (4 * (int64_t)k.tmem_ring_bytes));
+        b->tmem_capable = fit4 >= 1;
+        size_t smem = 120 * 1024;
+        for (int q = 0; q < kBuckets && b->tmem_capable; ++q) {
+            b->tmem_cpw[q] = 16 * (int)ceil_div((int64_t)b->cap[q], (int64_t)8);
+            const int g4 = std::max(1, std::min({4, 512 / b->tmem_cpw[q], fit4}));
+            b->tmem_block[q] = 128 * g4;
+            smem = std::max(smem, 16 + (size_t)(4 * g4) * k.tmem_ring_bytes);
+        }
+        b->tmem_smem = smem;
+        b->vadv_tmem_grid = p->sm_count;
     }
     size_t slab_total = 0;
     size_t slab_off[kBuckets] = {};
@@ -450,6 +563,8 @@ int sb_batch_set(sb_batch* b, const sb_domain* domains, int n) {
     for (auto& v : vd)
         std::stable_sort(v.begin(), v.end(), [&](int x, int y) { return domains[x].nk > domains[y].nk; });
     bool idx64 = false;
+    bool tmem_ok = b->tmem_capable;
+    const int es = storage_size(b->storage);
     DevTable* t = b->host_table;
     int slot = 0;
     auto fill = [&](int q, int64_t& items) {
@@ -475,6 +590,8 @@ int sb_batch_set(sb_batch* b, const sb_domain* domains, int n) {
             items += (int64_t)d.items_i * d.items_j * ceil_div(s.nk, b->tune.hdiff_planes);
         } else {
             d.wsh = (int64_t)s.wshift_i * s.si + (int64_t)s.wshift_j * s.sj;
+            d.ka = (s.sk * es) % 16 == 0;
+            if (s.si != 1 || s.sj <= 0 || s.sk <= 0) tmem_ok = false;
             d.items_i = (int32_t)ceil_div(s.ni, b->vadv_block);
             d.items_j = (int32_t)s.nj;
             items += (int64_t)d.items_i * d.items_j;
@@ -496,6 +613,7 @@ int sb_batch_set(sb_batch* b, const sb_domain* domains, int n) {
     t->ndomains = n;
     b->total_items = total;
     b->idx64 = idx64;
+    b->use_tmem = tmem_ok && !idx64;
     return SB_OK;
 }
 
@@ -506,7 +624,7 @@ int sb_batch_launch(sb_batch* b, void* stream, double* time_s) {
     SB_CUDA(cudaGetDevice(&dev));
     SB_CHECK(dev == b->device, SB_ERR_INVALID, "batch was created on device %d, current device is %d", b->device,
              dev);
-    if (!b->exec || b->graph_idx64 != b->idx64) {
+    if (!b->exec || b->graph_idx64 != b->idx64 || b->graph_tmem != b->use_tmem) {
         int rc = capture_graph(b);
         if (rc) return rc;
     }

@@ -82,6 +82,24 @@ def test_batch_tunings(block, per_sm, rows, planes, order, lib):
     _check(specs, devs, hosts, refs)
 
 
+@pytest.mark.parametrize("storage", ["float32", "bfloat16"])
+@pytest.mark.parametrize("vadv_block,max_nk", [(32, 256), (64, 256), (32, 300)])
+def test_batch_vadv_paths(storage, vadv_block, max_nk, lib):
+    """float32 vadv with the factors in tensor memory (vadv block 32, nk <= 256;
+    each bucket's blocks sized for its cap) and the shared-memory / slab path
+    (vadv block 64, or max_nk above 256) give the per-domain results."""
+    specs = _random_specs(31, 10, max_ij=70, max_k=256)
+    built = [device_domain(s, storage) for s in specs]
+    doms, devs, hosts = zip(*built)
+    refs = _reference_outputs(specs, doms, devs, hosts, "float32")
+    batch = Batch(storage, "float32", max_domains=16, max_nk=max_nk, vadv_block=vadv_block)
+    for _ in range(2):  # the second replay reuses the captured graph
+        batch.set(doms)
+        batch.launch()
+        _native.synchronize()
+        _check(specs, devs, hosts, refs)
+
+
 def test_batch_reuse_replays_the_graph_with_a_new_table(lib):
     batch = Batch("float32", max_domains=16, max_nk=48)
     for seed in (21, 22, 23):
