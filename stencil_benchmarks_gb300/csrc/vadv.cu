@@ -444,10 +444,12 @@ int launch_typed(const void* stage, const void* pos, const void* tens, const voi
     // float32 compute, no explicit shape: factors in tensor memory (512x512x80
     // float32 137 us against 171 us for WSLAB and 180 us for SMEM async;
     // bfloat16 113 us when the level stride is a multiple of 16 bytes, else
-    // the staging address arithmetic makes it no faster than WSLAB / SMEM)
+    // the staging address arithmetic makes it no faster than WSLAB / SMEM).
+    // Below 2048 column groups of 32 (256 x 256) the one-block-per-SM launch
+    // is not filled and SMEM async is as fast or faster (22 vs 27 us at 64^2).
     if constexpr (std::is_same<C, float>::value) {
         if (variant == SB_VARIANT_AUTO && !(tune && (tune->block_x || tune->block_y || tune->unroll)) &&
-            (sizeof(S) == 4 || (sk * (int64_t)sizeof(S)) % 16 == 0)) {
+            ceil_div(ni, (int64_t)32) * nj >= 2048 && (sizeof(S) == 4 || (sk * (int64_t)sizeof(S)) % 16 == 0)) {
             const int arc = launch_tmem<S, C>(8, p, stream, stage, pos, tens, tensstage, wcon, out, ni, nj, nk, si,
                                               sj, sk, wsh);
             if (arc != SB_ERR_UNSUPPORTED) return arc;

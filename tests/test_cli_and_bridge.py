@@ -25,7 +25,7 @@ def test_cli_command_tree():
     assert isinstance(group, click.Group)
     stencils = group.commands["stencils"].commands["gb300"]
     assert set(stencils.commands) >= {"basic", "horizontal-diffusion", "vertical-advection"}
-    assert set(stencils.commands["horizontal-diffusion"].commands) == {"j-scan", "tile"}
+    assert set(stencils.commands["horizontal-diffusion"].commands) == {"j-scan", "tile", "tma-tile", "vector-scan"}
     assert set(stencils.commands["vertical-advection"].commands) == {"shared-mem", "global-scratch", "slab", "no-alloc",
                                                                      "tensor-mem"}
     assert set(stencils.commands["basic"].commands) >= {"copy", "laplacian", "onesided-average",

@@ -31,7 +31,8 @@ def test_default_construction_runs_and_verifies(bmark, lib):
     instance.run()
 
 
-@pytest.mark.parametrize("cls", [horizontal_diffusion.JScan, horizontal_diffusion.Tile])
+@pytest.mark.parametrize("cls", [horizontal_diffusion.JScan, horizontal_diffusion.Tile, horizontal_diffusion.TmaTile,
+                                 horizontal_diffusion.VectorScan])
 @pytest.mark.parametrize("dtype", ["float64", "float32", "bfloat16"])
 def test_hdiff_benchmark_forms(cls, dtype, lib):
     b = cls(domain=(100, 77, 9), halo=(2, 2, 0), dtype=dtype, data_sets=2, alignment=0)
