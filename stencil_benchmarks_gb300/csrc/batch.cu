@@ -46,7 +46,7 @@ struct DevDomain {
     void* out;
     int64_t item_begin;  // first item of this domain in its queue
     int32_t items_i, items_j;
-    int32_t ka;  // vadv: the level stride is a multiple of 16 bytes (TMEM staging shortcut)
+    int32_t kp;  // vadv: level stride 0 (1) or 8 (2) modulo 16 bytes, else 0 (TMEM staging shortcuts)
     int32_t pad;
 };
 
@@ -205,14 +205,18 @@ __global__ void __launch_bounds__(512, 1)
         const int j = (int)(local / dm.items_i);
         const int nvalid = min(32, dm.ni - i0);
         const int col0 = i0 + j * (int)dm.sj;
-        if (dm.ka)
-            vadv_tmem_column<S, D, true, int>((const S*)dm.f[0], (const S*)dm.f[1], (const S*)dm.f[2],
-                                              (const S*)dm.f[3], (const S*)dm.f[4], (S*)dm.out, col0, lane, nvalid,
-                                              dm.nk, (int)dm.sk, (int)dm.wsh, tcol, ring);
+        if (dm.kp == 1)
+            vadv_tmem_column<S, D, 1, int>((const S*)dm.f[0], (const S*)dm.f[1], (const S*)dm.f[2],
+                                           (const S*)dm.f[3], (const S*)dm.f[4], (S*)dm.out, col0, lane, nvalid,
+                                           dm.nk, (int)dm.sk, (int)dm.wsh, tcol, ring);
+        else if (dm.kp == 2)
+            vadv_tmem_column<S, D, 2, int>((const S*)dm.f[0], (const S*)dm.f[1], (const S*)dm.f[2],
+                                           (const S*)dm.f[3], (const S*)dm.f[4], (S*)dm.out, col0, lane, nvalid,
+                                           dm.nk, (int)dm.sk, (int)dm.wsh, tcol, ring);
         else
-            vadv_tmem_column<S, D, false, int>((const S*)dm.f[0], (const S*)dm.f[1], (const S*)dm.f[2],
-                                               (const S*)dm.f[3], (const S*)dm.f[4], (S*)dm.out, col0, lane, nvalid,
-                                               dm.nk, (int)dm.sk, (int)dm.wsh, tcol, ring);
+            vadv_tmem_column<S, D, 0, int>((const S*)dm.f[0], (const S*)dm.f[1], (const S*)dm.f[2],
+                                           (const S*)dm.f[3], (const S*)dm.f[4], (S*)dm.out, col0, lane, nvalid,
+                                           dm.nk, (int)dm.sk, (int)dm.wsh, tcol, ring);
     }
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
     __syncthreads();
@@ -590,7 +594,7 @@ int sb_batch_set(sb_batch* b, const sb_domain* domains, int n) {
             items += (int64_t)d.items_i * d.items_j * ceil_div(s.nk, b->tune.hdiff_planes);
         } else {
             d.wsh = (int64_t)s.wshift_i * s.si + (int64_t)s.wshift_j * s.sj;
-            d.ka = (s.sk * es) % 16 == 0;
+            d.kp = (s.sk * es) % 16 == 0 ? 1 : (s.sk * es) % 16 == 8 ? 2 : 0;
             if (s.si != 1 || s.sj <= 0 || s.sk <= 0) tmem_ok = false;
             d.items_i = (int32_t)ceil_div(s.ni, b->vadv_block);
             d.items_j = (int32_t)s.nj;

@@ -926,11 +926,13 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&f)[16]) {
     for (int q = 0; q < 16; ++q) f[q] = __uint_as_float(r[q]);
 }
 
-// KA: the level stride sk * sizeof(S) is a multiple of 16 bytes, so every
-// level's rows share level 0's offsets within their 16-byte granules: the
-// copy addresses advance by a constant and the staged rows sit at fixed
-// ring offsets (far fewer instructions per level).
-template <class S, int D, bool KA, class IDX>
+// KP: how the level stride sk * sizeof(S) sits on 16-byte granules.  KP = 1:
+// a multiple of 16 bytes, so every level's rows share level 0's offsets
+// within their granules; KP = 2: 8 modulo 16, so even and odd levels each
+// share one set of offsets.  Then the copy addresses advance by a constant
+// and the staged rows sit at fixed ring offsets (per parity), which takes
+// far fewer instructions per level than the general case (KP = 0).
+template <class S, int D, int KP, class IDX>
 __device__ __forceinline__ void vadv_tmem_column(const S* __restrict__ stage, const S* __restrict__ pos,
                                                  const S* __restrict__ tens, const S* tensstage,
                                                  const S* __restrict__ wcon, S* out, IDX col0, int lane, int nvalid,
@@ -960,31 +962,38 @@ __device__ __forceinline__ void vadv_tmem_column(const S* __restrict__ stage, co
     unsigned mis0[6];
 #pragma unroll
     for (int f = 0; f < 6; ++f) mis0[f] = (unsigned)((uintptr_t)gsel(f) & 15u);
-    // chunk m of this lane: slot s = lane + 32 m -> row s / CPR, chunk s % CPR.  Level-0 source
-    // address and (KA) whether the chunk holds a byte of the row, fixed for all levels.
-    const unsigned char* cg[MF];
+    // chunk m of this lane: slot s = lane + 32 m -> row s / CPR, chunk s % CPR.  For level
+    // parity q (KP > 0): the source of level k is cg[q][m] + k * kstep, and cuse[q][m] says
+    // whether the chunk holds a byte of the row.
+    const unsigned kph = (unsigned)(kstep & 15);  // granule offset added by one level
+    const unsigned char* cg[2][MF];
     int cdst[MF], cidx[MF];
-    bool cuse[MF];
+    bool cuse[2][MF];
 #pragma unroll
     for (int m = 0; m < MF; ++m) {
         const int sidx = lane + 32 * m, r = sidx / CPR;
         cidx[m] = r < 6 ? sidx % CPR : CPR;  // CPR = never issued
         cdst[m] = (r < 6 ? r : 0) * ROWB + (sidx % CPR) * 16;
         const unsigned char* g = gsel(r < 6 ? r : 0);
-        const uintptr_t a = (uintptr_t)g;
-        const int n = (int)(((a & 15u) + (unsigned)nbytes + 15u) >> 4);
-        cuse[m] = cidx[m] < n;
-        cg[m] = KA ? (const unsigned char*)((a & ~(uintptr_t)15) + 16 * (cuse[m] ? cidx[m] : 0)) : g;
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+            const unsigned mq = (unsigned)(((uintptr_t)g + (q ? kph : 0u)) & 15u);
+            const int n = (int)((mq + (unsigned)nbytes + 15u) >> 4);
+            cuse[q][m] = cidx[m] < n;
+            cg[q][m] = KP ? g - mq + 16 * (cuse[q][m] ? cidx[m] : 0) : g;
+        }
     }
     auto issue = [&](int slot, int k) {
         if (k < nk - 1) {  // uniform
             const int64_t kb = (int64_t)k * kstep;
 #pragma unroll
             for (int m = 0; m < MF; ++m) {
-                if constexpr (KA) {
-                    if (cuse[m]) cp_async<16>(ring + slot * SLOT + cdst[m], (const void*)(cg[m] + kb));
+                if constexpr (KP > 0) {
+                    const bool odd = KP == 2 && (k & 1);
+                    const bool use = odd ? cuse[1][m] : cuse[0][m];
+                    if (use) cp_async<16>(ring + slot * SLOT + cdst[m], (const void*)((odd ? cg[1][m] : cg[0][m]) + kb));
                 } else {
-                    const uintptr_t a = (uintptr_t)(cg[m] + kb);
+                    const uintptr_t a = (uintptr_t)(cg[0][m] + kb);
                     const int n = (int)(((a & 15u) + (unsigned)nbytes + 15u) >> 4);
                     if (cidx[m] < n)
                         cp_async<16>(ring + slot * SLOT + cdst[m],
@@ -994,14 +1003,19 @@ __device__ __forceinline__ void vadv_tmem_column(const S* __restrict__ stage, co
         }
         cp_async_commit();
     };
-    // this lane's element of staged row f in slot 0 (KA: the same offset for every level)
-    const unsigned char* rowb[6];
+    // this lane's element of staged row f in slot 0, for even and odd levels (KP > 0)
+    const unsigned char* rowb[2][6];
 #pragma unroll
-    for (int f = 0; f < 6; ++f) rowb[f] = ring + f * ROWB + mis0[f] + lane * ES;
-    auto rd = [&](int slot, int f, unsigned kmis) -> C {
-        if constexpr (KA) {
-            return cvt<C, S>(*(const S*)(rowb[f] + slot * SLOT));
+    for (int f = 0; f < 6; ++f) {
+        rowb[0][f] = ring + f * ROWB + mis0[f] + lane * ES;
+        rowb[1][f] = ring + f * ROWB + ((mis0[f] + kph) & 15u) + lane * ES;
+    }
+    auto rd = [&](int slot, int f, int k) -> C {
+        if constexpr (KP > 0) {
+            const bool odd = KP == 2 && (k & 1);
+            return cvt<C, S>(*(const S*)((odd ? rowb[1][f] : rowb[0][f]) + slot * SLOT));
         } else {
+            const unsigned kmis = (unsigned)(((int64_t)k * kstep) & 15);
             return cvt<C, S>(((const S*)(ring + slot * SLOT + f * ROWB + ((mis0[f] + kmis) & 15u)))[lane]);
         }
     };
@@ -1029,10 +1043,9 @@ __device__ __forceinline__ void vadv_tmem_column(const S* __restrict__ stage, co
             if (k >= nk - 1) break;  // uniform
             cp_async_wait<D - 1>();
             __syncwarp();
-            const unsigned kmis = KA ? 0u : (unsigned)(((int64_t)k * kstep) & 15);
-            const C w1 = rd(u, 0, kmis), w0 = rd(u, 1, kmis);
-            const C snext = rd(u, 2, kmis), p0 = rd(u, 3, kmis);
-            const C t0 = rd(u, 4, kmis), ts0 = rd(u, 5, kmis);
+            const C w1 = rd(u, 0, k), w0 = rd(u, 1, k);
+            const C snext = rd(u, 2, k), p0 = rd(u, 3, k);
+            const C t0 = rd(u, 4, k), ts0 = rd(u, 5, k);
             issue((u + D) % R, k + D);  // the slot of level k-1: every lane has read it (__syncwarp above)
             const C as_ = A::template scale2<-1>(-gcv);
             gcv = A::template scale2<-2>(A::add(w1, w0));
@@ -1068,28 +1081,33 @@ __device__ __forceinline__ void vadv_tmem_column(const S* __restrict__ stage, co
     // ---- backward sweep: pos(k) of level k staged in slot (nk-2-k) % R
     const unsigned char* const gb0 = (const unsigned char*)(pos + col0);
     const unsigned mis_p = (unsigned)((uintptr_t)gb0 & 15u);
-    const unsigned char* bg[MB];
+    const unsigned char* bg[2][MB];
     int bdst[MB], bidx[MB];
-    bool buse[MB];
+    bool buse[2][MB];
 #pragma unroll
     for (int m = 0; m < MB; ++m) {
         const int sidx = lane + 32 * m;
         bidx[m] = sidx < CPR ? sidx : CPR;
         bdst[m] = (sidx < CPR ? sidx : 0) * 16;
-        const uintptr_t a = (uintptr_t)gb0;
-        const int n = (int)(((a & 15u) + (unsigned)nbytes + 15u) >> 4);
-        buse[m] = bidx[m] < n;
-        bg[m] = KA ? (const unsigned char*)((a & ~(uintptr_t)15) + 16 * (buse[m] ? bidx[m] : 0)) : gb0;
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+            const unsigned mq = (unsigned)(((uintptr_t)gb0 + (q ? kph : 0u)) & 15u);
+            const int n = (int)((mq + (unsigned)nbytes + 15u) >> 4);
+            buse[q][m] = bidx[m] < n;
+            bg[q][m] = KP ? gb0 - mq + 16 * (buse[q][m] ? bidx[m] : 0) : gb0;
+        }
     }
     auto issue_b = [&](int slot, int k) {
         if (k >= 0) {
             const int64_t kb = (int64_t)k * kstep;
 #pragma unroll
             for (int m = 0; m < MB; ++m) {
-                if constexpr (KA) {
-                    if (buse[m]) cp_async<16>(ring + slot * SLOT + bdst[m], (const void*)(bg[m] + kb));
+                if constexpr (KP > 0) {
+                    const bool odd = KP == 2 && (k & 1);
+                    const bool use = odd ? buse[1][m] : buse[0][m];
+                    if (use) cp_async<16>(ring + slot * SLOT + bdst[m], (const void*)((odd ? bg[1][m] : bg[0][m]) + kb));
                 } else {
-                    const uintptr_t a = (uintptr_t)(bg[m] + kb);
+                    const uintptr_t a = (uintptr_t)(bg[0][m] + kb);
                     const int n = (int)(((a & 15u) + (unsigned)nbytes + 15u) >> 4);
                     if (bidx[m] < n)
                         cp_async<16>(ring + slot * SLOT + bdst[m],
@@ -1106,7 +1124,8 @@ __device__ __forceinline__ void vadv_tmem_column(const S* __restrict__ stage, co
         const IDX o = col + (IDX)(nk - 1) * sk;
         st<S, C>(out + o, A::mul(dtr, A::sub(data, ld<C, S>(pos + o))));
     }
-    const unsigned char* const prow = ring + mis_p + lane * ES;  // KA: pos element of slot 0
+    const unsigned char* const prow0 = ring + mis_p + lane * ES;  // KP > 0: pos element of slot 0, even levels
+    const unsigned char* const prow1 = ring + ((mis_p + kph) & 15u) + lane * ES;  // odd levels
     S* optr = out + col;
     int slot = 0;  // ring slot of the next level
     for (int w = (nk - 2) >> 3; w >= 0; --w) {
@@ -1119,8 +1138,9 @@ __device__ __forceinline__ void vadv_tmem_column(const S* __restrict__ stage, co
             cp_async_wait<D - 1>();
             __syncwarp();
             C p0;
-            if constexpr (KA) {
-                p0 = cvt<C, S>(*(const S*)(prow + slot * SLOT));
+            if constexpr (KP > 0) {
+                const bool odd = KP == 2 && (k & 1);
+                p0 = cvt<C, S>(*(const S*)((odd ? prow1 : prow0) + slot * SLOT));
             } else {
                 const unsigned kp = (unsigned)(((int64_t)k * kstep) & 15);
                 p0 = cvt<C, S>(((const S*)(ring + slot * SLOT + ((mis_p + kp) & 15u)))[lane]);

@@ -341,7 +341,7 @@ int launch_wslab(int bx, int depth, int blocks_per_sm, const DeviceProps* p, cud
 // The block allocates all 512 columns and asks for enough shared memory that
 // no second block shares its SM, so the allocation never waits.
 // ---------------------------------------------------------------------------
-template <class S, int D, bool KA>
+template <class S, int D, int KP>
 __global__ void __launch_bounds__(512, 1)
     vadv_tmem_kernel(const S* __restrict__ stage, const S* __restrict__ pos, const S* __restrict__ tens,
                      const S* tensstage, const S* __restrict__ wcon, S* out, int ni, int nj, int nk, int sj, int sk,
@@ -368,7 +368,7 @@ __global__ void __launch_bounds__(512, 1)
         const int i0 = (int)(g % gx) * 32;
         const int j = (int)(g / gx);
         const int nvalid = min(32, ni - i0);
-        vadv_tmem_column<S, D, KA, int>(stage, pos, tens, tensstage, wcon, out, i0 + j * sj, lane, nvalid, nk, sk,
+        vadv_tmem_column<S, D, KP, int>(stage, pos, tens, tensstage, wcon, out, i0 + j * sj, lane, nvalid, nk, sk,
                                         wsh, tcol, ring);
     }
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
@@ -384,7 +384,8 @@ template <class S, int D>
 int launch_tmem_one(int g4, int cpw, const DeviceProps* p, cudaStream_t stream, const void* stage, const void* pos,
                     const void* tens, const void* tensstage, const void* wcon, void* out, int64_t ni, int64_t nj,
                     int64_t nk, int64_t sj, int64_t sk, int64_t wsh) {
-    auto kernel = ((int64_t)sk * (int64_t)sizeof(S)) % 16 == 0 ? vadv_tmem_kernel<S, D, true> : vadv_tmem_kernel<S, D, false>;
+    const int64_t kmod = ((int64_t)sk * (int64_t)sizeof(S)) % 16;
+    auto kernel = kmod == 0 ? vadv_tmem_kernel<S, D, 1> : kmod == 8 ? vadv_tmem_kernel<S, D, 2> : vadv_tmem_kernel<S, D, 0>;
     // fewer warps per lane quarter when their rings do not fit
     g4 = std::min<int64_t>(g4, (p->smem_optin - 16) / (4 * (int64_t)WarpRing<S, float, D>::BYTES));
     if (g4 < 1) return SB_ERR_UNSUPPORTED;
@@ -449,7 +450,7 @@ int launch_typed(const void* stage, const void* pos, const void* tens, const voi
     // is not filled and SMEM async is as fast or faster (22 vs 27 us at 64^2).
     if constexpr (std::is_same<C, float>::value) {
         if (variant == SB_VARIANT_AUTO && !(tune && (tune->block_x || tune->block_y || tune->unroll)) &&
-            ceil_div(ni, (int64_t)32) * nj >= 2048 && (sizeof(S) == 4 || (sk * (int64_t)sizeof(S)) % 16 == 0)) {
+            ceil_div(ni, (int64_t)32) * nj >= 2048 && (sizeof(S) == 4 || (sk * (int64_t)sizeof(S)) % 8 == 0)) {
             const int arc = launch_tmem<S, C>(8, p, stream, stage, pos, tens, tensstage, wcon, out, ni, nj, nk, si,
                                               sj, sk, wsh);
             if (arc != SB_ERR_UNSUPPORTED) return arc;
