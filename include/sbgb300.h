@@ -72,7 +72,7 @@ extern "C" {
                            * aligned j/k strides and halo corner)                   */
 #define SB_HDIFF_VSCAN 4  /* JSCAN with V columns per lane moved as one aligned
                            * vector (block_x = strip width 32*V: 64 for 8-byte,
-                           * 128 for 4-byte, 128 or 256 for 2-byte storage); i
+                           * 64 or 128 for 4-byte, 128 or 256 for 2-byte storage); i
                            * unit-stride, j/k strides multiples of the vector,
                            * inp/coeff/out at one offset from a vector boundary */
 #define SB_VADV_SMEM 1    /* one thread per column, ccol/dcol in shared memory     */

@@ -507,13 +507,19 @@ int launch_typed(const void* inp, const void* coeff, void* out, int64_t ni, int6
             if (rc_tma != SB_ERR_UNSUPPORTED) return rc_tma;
         }
     }
-    // bfloat16 storage and float-pair compute: vector strips (V columns per
-    // lane) issue fewer instructions per point than JSCAN (56 vs 62 us and
-    // 271 vs 313 us at 512x512x80); float32 stays on JSCAN (52 vs 59 us).
+    // bfloat16 storage, float-pair and float32 compute: vector strips (V
+    // columns per lane) issue fewer instructions per point than JSCAN (56 vs
+    // 62 us, 271 vs 313 us and, with V = 2, 51 vs 53 us at 512x512x80).
     if constexpr (std::is_same<S, bf16>::value || std::is_same<C, f32x2>::value) {
         if (variant == SB_VARIANT_AUTO) {
             constexpr int V = sizeof(S) == 8 ? 2 : 4;
             const int rc_v = launch_vscan<S, C, V>(inp, coeff, out, ni, nj, nk, si, sj, sk, 1, 16, 1, 1, stream, p);
+            if (rc_v != SB_ERR_UNSUPPORTED) return rc_v;
+        }
+    }
+    if constexpr (std::is_same<S, float>::value && std::is_same<C, float>::value) {
+        if (variant == SB_VARIANT_AUTO) {
+            const int rc_v = launch_vscan<S, C, 2>(inp, coeff, out, ni, nj, nk, si, sj, sk, 2, 16, 1, 4, stream, p);
             if (rc_v != SB_ERR_UNSUPPORTED) return rc_v;
         }
     }
@@ -566,10 +572,11 @@ int launch_typed(const void* inp, const void* coeff, void* out, int64_t ni, int6
                     rc2 = launch_vscan<S, C, 2>(inp, coeff, out, ni, nj, nk, si, sj, sk, nw, ty, kper, unroll, stream, p);
                 }
             } else if constexpr (sizeof(S) == 4) {
-                if (width == 128) {
-                    shape_ok = true;
+                if (width == 64 || width == 128) shape_ok = true;
+                if (width == 64)
+                    rc2 = launch_vscan<S, C, 2>(inp, coeff, out, ni, nj, nk, si, sj, sk, nw, ty, kper, unroll, stream, p);
+                if (width == 128)
                     rc2 = launch_vscan<S, C, 4>(inp, coeff, out, ni, nj, nk, si, sj, sk, nw, ty, kper, unroll, stream, p);
-                }
             } else {
                 if (width == 128 || width == 256) shape_ok = true;
                 if (width == 128)
@@ -578,8 +585,8 @@ int launch_typed(const void* inp, const void* coeff, void* out, int64_t ni, int6
                     rc2 = launch_vscan<S, C, 8>(inp, coeff, out, ni, nj, nk, si, sj, sk, nw, ty, kper, unroll, stream, p);
             }
             SB_CHECK(shape_ok, SB_ERR_INVALID,
-                     "hdiff vscan strip width (block_x) must be 64 for 8-byte, 128 for 4-byte and 128 or 256 for "
-                     "2-byte storage (got %d)", width);
+                     "hdiff vscan strip width (block_x) must be 64 for 8-byte, 64 or 128 for 4-byte and 128 or 256 "
+                     "for 2-byte storage (got %d)", width);
             SB_CHECK(rc2 != SB_ERR_UNSUPPORTED, SB_ERR_UNSUPPORTED,
                      "hdiff VSCAN: needs i unit-stride, j/k strides that are multiples of the %d-column vector and "
                      "inp/coeff/out at the same offset from a vector boundary", width / 32);

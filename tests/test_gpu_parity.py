@@ -178,7 +178,7 @@ def test_hdiff_tma_full_size_fp32(lib):
     _assert_bits(got, want, "hdiff tma 512x512x80 float32")
 
 
-VSCAN_WIDTHS = {"float64": (64,), "float32": (128,), "bfloat16": (128, 256)}
+VSCAN_WIDTHS = {"float64": (64,), "float32": (64, 128), "bfloat16": (128, 256)}
 
 
 @pytest.mark.parametrize("storage,compute", FORMS)
@@ -219,7 +219,7 @@ def test_hdiff_vscan_rejects_unqualified_layouts(layout, alignment, lib):
 
 
 def test_hdiff_vscan_rejects_bad_width(lib):
-    t = _native.tune(variant=_native.HDIFF_VSCAN, block_x=64)
+    t = _native.tune(variant=_native.HDIFF_VSCAN, block_x=32)
     with pytest.raises(_native.SbError) as err:
         _run_hdiff((64, 8, 2), (2, 2, 0), "float32", "float32", alignment=64, tune=t)
     assert err.value.code == _native.SB_ERR_INVALID
