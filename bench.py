@@ -71,6 +71,12 @@ FAST_VADV_COMPUTE = "float32x2"
 FAST_VADV_TUNE = {"variant": 3, "block_x": 64, "unroll": 2, "k_per_cta": 32}
 
 
+# Algorithmic fp64 operations per grid point of the reference's arithmetic
+# (the exact kernels' ceiling on GB300): hdiff about 16 (Laplacian once per
+# point, two limited fluxes, the update); vadv about 26 plus one divide.
+FP64_OPS = {"hdiff": 16, "vadv": 27}
+
+
 def compulsory_bytes(kind, s=8):
     """Algorithmic HBM bytes per launch (each input read once, output written once)."""
     if kind == "hdiff":  # inp with its 2-point i/j halo, coeff, out
@@ -436,11 +442,14 @@ def run_gpu(args, dist):
         triad = {"n": TRIAD_N, "dtype": "f64", "best_s": best, "gbs": 3 * 8 * TRIAD_N / best / 1e9}
         del bufs
 
+    # ---- fp64 instruction rate (outside the timed region): the exact kernels' ceiling
+    fp64_peak = max(kernels.arith_rate(0), kernels.arith_rate(1))
+
     return {
         "info": info, "elapsed": elapsed_max, "t_hdiff": t_hdiff, "t_vadv": t_vadv, "clocks": clk,
         "gpu_launches": gpu_launches, "e2e_time": e2e_time, "e2e_serial_time": e2e_serial_time,
         "e2e_steps": e2e_steps, "h2d": h2d, "d2h": d2h,
-        "triad": triad, "fast": fast,
+        "triad": triad, "fast": fast, "fp64_peak": fp64_peak,
     }
 
 
@@ -630,7 +639,14 @@ def main(argv=None):
                                                    "rate on GB300 (0.52 Tops/s measured)",
                          "kernel": dominant, "achieved": achieved, "peak": peak,
                          "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
-                         "traffic": traffic, "algorithmic_bytes": compulsory_bytes(dominant)},
+                         "traffic": traffic, "algorithmic_bytes": compulsory_bytes(dominant),
+                         "fp64_pipe": {
+                             "what": "algorithmic fp64 operations per second (hdiff 16, vadv 27 per point, a divide "
+                                     "counted once) / the fp64 add-or-FMA instruction rate measured in this run",
+                             "achieved": FP64_OPS[dominant] * POINTS / t_dom, "peak": res["fp64_peak"],
+                             "unit": "op/s", "frac": FP64_OPS[dominant] * POINTS / t_dom / res["fp64_peak"],
+                             "hdiff_frac": FP64_OPS["hdiff"] * POINTS / t_h / res["fp64_peak"],
+                             "vadv_frac": FP64_OPS["vadv"] * POINTS / t_v / res["fp64_peak"]}},
             "kernels": {
                 "hdiff": {"ms": t_h * 1e3, "gpoints_s": POINTS / t_h / 1e9,
                           "hbm_gbs": compulsory_bytes("hdiff") / t_h / 1e9,
