@@ -33,6 +33,7 @@ from __future__ import annotations
 import collections
 import ctypes
 import math
+import gc
 import time
 import weakref
 from dataclasses import dataclass, field
@@ -377,15 +378,23 @@ def run_load(server: Server, requests: List[Request], rate: float, seed: int = 5
     time) and step the server until all complete.  Returns summary statistics."""
     rng = np.random.Generator(np.random.PCG64(seed))
     offsets = np.cumsum(rng.exponential(1.0 / rate, size=len(requests)))
-    t0 = time.perf_counter()
-    nxt = 0
-    while nxt < len(requests) or server.busy():
-        now = time.perf_counter() - t0
-        while nxt < len(requests) and offsets[nxt] <= now:
-            requests[nxt].arrival = t0 + offsets[nxt]
-            server.submit(requests[nxt])
-            nxt += 1
-        server.step()
+    # no cyclic-garbage pauses inside the latency-critical loop (collected once before)
+    gc.collect()
+    gc_was_enabled = gc.isenabled()
+    gc.disable()
+    try:
+        t0 = time.perf_counter()
+        nxt = 0
+        while nxt < len(requests) or server.busy():
+            now = time.perf_counter() - t0
+            while nxt < len(requests) and offsets[nxt] <= now:
+                requests[nxt].arrival = t0 + offsets[nxt]
+                server.submit(requests[nxt])
+                nxt += 1
+            server.step()
+    finally:
+        if gc_was_enabled:
+            gc.enable()
     lat = np.array([r.latency for r in requests])
     first = min(r.arrival for r in requests)
     last = max(r.completed for r in requests)
