@@ -39,7 +39,7 @@ extern "C" {
 #define SB_OK 0
 #define SB_ERR_INVALID 1     /* invalid argument: shape, stride, type, alignment */
 #define SB_ERR_CUDA 2        /* a CUDA runtime call failed                         */
-#define SB_ERR_UNSUPPORTED 3 /* valid request this build does not implement        */
+#define SB_ERR_UNSUPPORTED 3 /* valid request the library does not implement       */
 #define SB_ERR_NOMEM 4       /* device or host allocation failed                   */
 #define SB_ERR_TIMEOUT 5     /* a bounded device-side wait gave up                 */
 #define SB_ERR_BUDGET 6      /* request exceeds a configured memory budget         */

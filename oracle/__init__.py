@@ -10,8 +10,8 @@ This package restates, on the CPU, the arithmetic that the reference
   (OpenMP) restatement of hdiff / vadv used as the timed CPU baseline.
 
 Only ``tests/``, ``__graft_entry__.smoke()`` and ``bench.py`` (its CPU-baseline
-and reference arms) may import this package, and only as the checker or as the
-timed CPU baseline.  The product package ``stencil_benchmarks_gb300`` never
+and reference arms) may import this package, and only to check results or as
+the timed CPU baseline.  The product package ``stencil_benchmarks_gb300`` never
 imports it; it has no CPU compute path at all.
 
 Parity pin: every function here is checked bit-for-bit against golden vectors

@@ -14,7 +14,7 @@ Scheduling (``Server.step``), repeated by the caller's loop:
    (latency = completion seen - arrival) and return their memory to the pool;
 2. admit: waiting requests, in arrival order, get their fields if the pool's
    budget allows (150 GB by default); one ``sb_fill_batch`` launch creates the
-   inputs of everything admitted in this round;
+   inputs of everything admitted in this step;
 3. dispatch: for every precision form with admitted requests and a free slot,
    up to ``max_batch`` of them are packed into that slot's ``Batch`` and
    launched (one graph replay) on the slot's stream, after the fill.
