@@ -144,6 +144,16 @@ __device__ __forceinline__ f32x2 shfl_down<f32x2>(f32x2 v, unsigned d) {
 // ---------------------------------------------------------------------------
 template <class C>
 struct Ar;
+
+// Rare fp64 paths of Ar<double>, kept out of line: inline, the compiler
+// evaluates them under a predicate on every call, and each predicated fp64
+// instruction still takes a slot of GB300's narrow fp64 pipe.
+static __device__ __noinline__ double fp64_mul_cold(double a, double b) { return __dmul_rn(a, b); }
+static __device__ __noinline__ double fp64_sub_cold(double a, double b) { return __dsub_rn(a, b); }
+static __device__ __noinline__ double fp64_limit_cold(double f, double a1, double a0) {
+    return (__dmul_rn(f, __dsub_rn(a1, a0)) > 0.0) ? 0.0 : f;
+}
+
 template <>
 struct Ar<double> {
     static __device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, b); }
@@ -163,8 +173,8 @@ struct Ar<double> {
         if (e >= 1 && e <= 2046 && en >= 1 && en <= 2046) {
             return __hiloint2double(hi + E * (1 << 20), __double2loint(x));
         }
-        return __dmul_rn(x, E >= 0 ? (double)(1 << (E >= 0 ? E : 0))
-                                   : 1.0 / (double)(1 << (E >= 0 ? 0 : -E)));
+        return fp64_mul_cold(x, E >= 0 ? (double)(1 << (E >= 0 ? E : 0))
+                                       : 1.0 / (double)(1 << (E >= 0 ? 0 : -E)));
     }
 
     // Exact `(f * (a1 - a0) > 0) ? 0 : f` (the reference's flux limiter).
@@ -194,13 +204,14 @@ struct Ar<double> {
             const bool fpos = hf >= 0;
             return (fpos == gt) ? 0.0 : f;  // same sign -> product > 0 -> limited
         }
-        return (__dmul_rn(f, __dsub_rn(a1, a0)) > 0.0) ? 0.0 : f;
+        return fp64_limit_cold(f, a1, a0);
     }
 
     // -x, except that (a - b) and (b - a) both give +0 when a == b: returns
     // the exact value of (b - a) given x = (a - b).
     static __device__ __forceinline__ double neg_diff(double x, double a, double b) {
-        return ((__double_as_longlong(x) << 1) == 0) ? __dsub_rn(b, a) : -x;
+        if ((__double_as_longlong(x) << 1) == 0) return fp64_sub_cold(b, a);
+        return -x;
     }
 };
 
