@@ -642,7 +642,9 @@ def main(argv=None):
                          "traffic": traffic, "algorithmic_bytes": compulsory_bytes(dominant),
                          "fp64_pipe": {
                              "what": "algorithmic fp64 operations per second (hdiff 16, vadv 27 per point, a divide "
-                                     "counted once) / the fp64 add-or-FMA instruction rate measured in this run",
+                                     "counted once) / the fp64 add-or-FMA instruction rate measured in this run; can "
+                                     "exceed 1 where exact power-of-two scales and the limiter's sign tests run on "
+                                     "the integer pipe",
                              "achieved": FP64_OPS[dominant] * POINTS / t_dom, "peak": res["fp64_peak"],
                              "unit": "op/s", "frac": FP64_OPS[dominant] * POINTS / t_dom / res["fp64_peak"],
                              "hdiff_frac": FP64_OPS["hdiff"] * POINTS / t_h / res["fp64_peak"],

@@ -503,7 +503,7 @@ int launch_typed(const void* inp, const void* coeff, void* out, int64_t ni, int6
     const bool auto_tile = variant == SB_VARIANT_AUTO && std::is_same<C, double>::value;
     if constexpr (std::is_same<S, double>::value && std::is_same<C, double>::value) {
         if (variant == SB_VARIANT_AUTO) {
-            const int rc_tma = launch_tma<S, C, 128, 4>(inp, coeff, out, ni, nj, nk, si, sj, sk, 16, 4, stream, p);
+            const int rc_tma = launch_tma<S, C, 128, 4>(inp, coeff, out, ni, nj, nk, si, sj, sk, 16, 2, stream, p);
             if (rc_tma != SB_ERR_UNSUPPORTED) return rc_tma;
         }
     }
