@@ -526,8 +526,8 @@ def run_served(n_requests=2000, rates=(1000.0, 5000.0, 20000.0), seed=11, float6
     out = []
     for rate in rates:
         stats = serving.run_load(server, serving.request_specs(n_requests, seed=seed), rate=rate)
-        out.append({k: stats[k] for k in ("rate_offered", "requests", "p50_ms", "p99_ms", "throughput_req_s",
-                                          "gpoints_s", "peak_pool_gb")})
+        out.append({k: stats[k] for k in ("rate_offered", "requests", "p50_ms", "p99_ms", "mean_ms",
+                                          "throughput_req_s", "gpoints_s", "peak_pool_gb", "max_waiting")})
     return out
 
 
@@ -679,14 +679,16 @@ def main(argv=None):
         }
         if res["triad"]:
             line["stream_triad"]["frac_of_" + peak_kind] = res["triad"]["gbs"] / peak
-        if not args.no_batched:
-            line["batched"] = run_batched()
+        # serving first: its latencies are measured in a process that has not
+        # yet created and torn down the autotuner's many batch objects
         if not args.no_served:
             line["served"] = run_served()
             line["served_fast_f64"] = {
                 "what": "float64 requests with fixed-point hdiff and float-pair vadv (within 1e-12 / 1e-10 of "
                         "the field scale); float32 and bfloat16 requests unchanged",
                 "rates": run_served(rates=(5000.0, 20000.0), float64_compute="fixed64")}
+        if not args.no_batched:
+            line["batched"] = run_batched()
         if not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline_sample()
         print(json.dumps(line), flush=True)
