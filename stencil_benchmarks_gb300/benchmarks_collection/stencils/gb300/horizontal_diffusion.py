@@ -27,7 +27,7 @@ class HorizontalDiffusionMixin(StencilMixin):
 
     def launch(self, fields, timed):
         inp, coeff, out = fields
-        return kernels.hdiff(inp, coeff, out, compute=self.compute, tune=self.tune(), timed=timed)
+        return kernels.hdiff(inp, coeff, out, compute=self.compute, tune=self.current_tune(), timed=timed)
 
 
 class JScan(HorizontalDiffusionMixin, base.HorizontalDiffusionStencil):
@@ -43,6 +43,10 @@ class JScan(HorizontalDiffusionMixin, base.HorizontalDiffusionStencil):
     def tune(self):
         return _native.tune(variant=_native.HDIFF_JSCAN, block_y=self.block_size[0], tile_y=self.block_size[1],
                             k_per_cta=self.k_per_block, unroll=self.unroll_factor)
+
+    def tune_candidates(self):
+        return [self.tune()] + [_native.tune(variant=_native.HDIFF_JSCAN, block_y=nw, tile_y=ty, k_per_cta=1, unroll=u)
+                                for nw in (1, 2, 4) for ty in (16, 32, 64) for u in (2, 4)]
 
 
 class Tile(HorizontalDiffusionMixin, base.HorizontalDiffusionStencil):
@@ -61,6 +65,11 @@ class Tile(HorizontalDiffusionMixin, base.HorizontalDiffusionStencil):
         bx, by, ty = self.block_size
         return _native.tune(variant=_native.HDIFF_TILE, block_x=bx, block_y=by, tile_y=ty,
                             k_per_cta=self.k_per_block)
+
+    def tune_candidates(self):
+        return [self.tune()] + [_native.tune(variant=_native.HDIFF_TILE, block_x=bx, block_y=by, tile_y=ty, k_per_cta=k)
+                                for bx, by in ((128, 4), (64, 4), (64, 8), (128, 2)) for ty in (8, 16, 32)
+                                for k in (2, 4)]
 
 
 class TmaTile(HorizontalDiffusionMixin, base.HorizontalDiffusionStencil):
@@ -81,6 +90,11 @@ class TmaTile(HorizontalDiffusionMixin, base.HorizontalDiffusionStencil):
         return _native.tune(variant=_native.HDIFF_TMA, block_x=bx, block_y=by, tile_y=ty,
                             k_per_cta=self.k_per_block)
 
+    def tune_candidates(self):
+        return [self.tune()] + [_native.tune(variant=_native.HDIFF_TMA, block_x=bx, block_y=by, tile_y=ty, k_per_cta=k)
+                                for bx, by in ((128, 4), (64, 4), (64, 8), (128, 2)) for ty in (8, 12, 16, 32)
+                                for k in (2, 4)]
+
 
 class VectorScan(HorizontalDiffusionMixin, base.HorizontalDiffusionStencil):
     block_size = Parameter("strip width (32 x columns per lane; 0: 16 bytes per lane), warps per block, "
@@ -100,3 +114,9 @@ class VectorScan(HorizontalDiffusionMixin, base.HorizontalDiffusionStencil):
             width = {8: 64, 4: 128, 2: 128}[self.dtype_size]
         return _native.tune(variant=_native.HDIFF_VSCAN, block_x=width, block_y=nw, tile_y=rows,
                             k_per_cta=self.k_per_block, unroll=self.unroll_factor)
+
+    def tune_candidates(self):
+        widths = {8: (64,), 4: (64, 128), 2: (128, 256)}[self.dtype_size]
+        return [self.tune()] + [_native.tune(variant=_native.HDIFF_VSCAN, block_x=w, block_y=nw, tile_y=ty,
+                                             k_per_cta=1, unroll=u)
+                                for w in widths for nw in (1, 2, 4) for ty in (16, 32) for u in (1, 4)]

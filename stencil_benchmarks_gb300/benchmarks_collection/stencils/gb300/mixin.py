@@ -13,6 +13,7 @@ fields) rather than on every run.
 
 from __future__ import annotations
 
+import statistics
 import time
 
 from .... import _native
@@ -31,6 +32,45 @@ class StencilMixin(Benchmark):
         choices=["auto", "float32", "float64", "float32x2", "fixed64"],
     )
     device = Parameter("CUDA device index", 0)
+    autotune = Parameter("time this implementation's candidate launch shapes on the benchmark's own fields "
+                         "during setup and run the fastest (reported as `tune`)", False)
+
+    def tune(self):
+        """This implementation's launch shape (None: the library's choice)."""
+        return None
+
+    def tune_candidates(self):
+        """Launch shapes the autotuner times: this implementation's own family."""
+        return [self.tune()]
+
+    def current_tune(self):
+        picked = getattr(self, "_picked_tune", None)
+        return picked[0] if picked is not None else self.tune()
+
+    def _pick_tune(self):
+        fields = self._device_fields
+        best, best_t = None, None
+        for cand in self.tune_candidates():
+            for host, dev in zip(self._data[0], fields):
+                dev.upload(host)
+            self._picked_tune = (cand,)
+            try:
+                self.launch(fields, timed=False)
+                t = statistics.median(self.launch(fields, timed=True) for _ in range(3))
+            except _native.SbError:
+                continue
+            if best_t is None or t < best_t:
+                best, best_t = cand, t
+        self._picked_tune = None
+        if best_t is None:
+            raise ParameterError("autotune: no candidate launch shape runs on this layout")
+        return best
+
+    @staticmethod
+    def describe_tune(t) -> str:
+        if t is None:
+            return "library default"
+        return " ".join(f"{name}={getattr(t, name)}" for name, _ in t._fields_ if getattr(t, name))
 
     def setup(self):
         super().setup()
@@ -50,6 +90,9 @@ class StencilMixin(Benchmark):
         if self.compute_dtype == "fixed64" and self.stencil_kind != "horizontal_diffusion":
             raise ParameterError("fixed64 compute is provided for horizontal diffusion only")
         self._device_fields = [Field.like_host(host, self.dtype, self.halo) for host in self._data[0]]
+        self._picked_tune = None
+        if self.autotune:
+            self._picked_tune = (self._pick_tune(),)
 
     @property
     def compute(self) -> str:
@@ -81,4 +124,6 @@ class StencilMixin(Benchmark):
             raise ExecutionError(str(err)) from err
         for host, dev in zip(data, fields):
             dev.download(host)
+        if self.autotune:
+            return {"time": elapsed, "tune": self.describe_tune(self.current_tune())}
         return {"time": elapsed}

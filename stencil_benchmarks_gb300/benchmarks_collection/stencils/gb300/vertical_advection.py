@@ -64,10 +64,16 @@ class VerticalAdvectionMixin(StencilMixin):
 
 
 class SharedMem(VerticalAdvectionMixin, base.VerticalAdvectionStencil):
-    def launch_component(self, f, named, shift, timed):
-        tune = _native.tune(variant=_native.VADV_SMEM, block_x=self.block_size[0], block_y=self.block_size[1],
+    def tune(self):
+        return _native.tune(variant=_native.VADV_SMEM, block_x=self.block_size[0], block_y=self.block_size[1],
                             unroll=self.unroll_factor)
-        return kernels.vadv(*f, named["wcon"], shift, compute=self.compute, tune=tune, timed=timed)
+
+    def tune_candidates(self):
+        return [self.tune()] + [_native.tune(variant=_native.VADV_SMEM, block_x=bx, block_y=by, unroll=u)
+                                for bx, by in ((32, 1), (64, 1), (32, 2)) for u in (2, 4, 8)]
+
+    def launch_component(self, f, named, shift, timed):
+        return kernels.vadv(*f, named["wcon"], shift, compute=self.compute, tune=self.current_tune(), timed=timed)
 
 
 class GlobalScratch(VerticalAdvectionMixin, base.VerticalAdvectionStencil):
@@ -79,11 +85,17 @@ class GlobalScratch(VerticalAdvectionMixin, base.VerticalAdvectionStencil):
         if self.dtype_size != {"float64": 8, "float32": 4, "float32x2": 8}[self.compute]:
             raise ParameterError("GlobalScratch keeps the factors in ccol/dcol: storage and compute types must match")
 
-    def launch_component(self, f, named, shift, timed):
-        tune = _native.tune(variant=_native.VADV_GLOBAL, block_x=self.block_size[0], block_y=self.block_size[1],
+    def tune(self):
+        return _native.tune(variant=_native.VADV_GLOBAL, block_x=self.block_size[0], block_y=self.block_size[1],
                             unroll=self.unroll_factor)
+
+    def tune_candidates(self):
+        return [self.tune()] + [_native.tune(variant=_native.VADV_GLOBAL, block_x=bx, block_y=1, unroll=u)
+                                for bx in (32, 64, 128) for u in (1, 2, 4)]
+
+    def launch_component(self, f, named, shift, timed):
         return kernels.vadv(*f, named["wcon"], shift, ccol=named["ccol"], dcol=named["dcol"], compute=self.compute,
-                            tune=tune, timed=timed)
+                            tune=self.current_tune(), timed=timed)
 
 
 class Slab(VerticalAdvectionMixin, base.VerticalAdvectionStencil):
@@ -99,11 +111,17 @@ class Slab(VerticalAdvectionMixin, base.VerticalAdvectionStencil):
         if self.block_size[0] not in (32, 64):
             raise ParameterError("Slab blocks have 32 or 64 threads")
 
-    def launch_component(self, f, named, shift, timed):
-        tune = _native.tune(variant=_native.VADV_SLAB, block_x=self.block_size[0], k_per_cta=self.block_size[1],
+    def tune(self):
+        return _native.tune(variant=_native.VADV_SLAB, block_x=self.block_size[0], k_per_cta=self.block_size[1],
                             unroll=self.unroll_factor)
+
+    def tune_candidates(self):
+        return [self.tune()] + [_native.tune(variant=_native.VADV_SLAB, block_x=bx, k_per_cta=per, unroll=u)
+                                for bx in (32, 64) for per in (0, 8, 16) for u in (2, 4, 8)]
+
+    def launch_component(self, f, named, shift, timed):
         return kernels.vadv(*f, named["wcon"], shift, ccol=named["ccol"], dcol=named["dcol"], compute=self.compute,
-                            tune=tune, timed=timed)
+                            tune=self.current_tune(), timed=timed)
 
 
 class NoAlloc(VerticalAdvectionMixin, base.VerticalAdvectionStencil):
@@ -130,6 +148,11 @@ class TensorMem(VerticalAdvectionMixin, base.VerticalAdvectionStencil):
         if self.domain[2] > 256:
             raise ParameterError("TensorMem holds at most 256 levels per column")
 
+    def tune(self):
+        return _native.tune(variant=_native.VADV_TMEM, unroll=self.unroll_factor)
+
+    def tune_candidates(self):
+        return [_native.tune(variant=_native.VADV_TMEM, unroll=u) for u in (4, 8, 16)]
+
     def launch_component(self, f, named, shift, timed):
-        tune = _native.tune(variant=_native.VADV_TMEM, unroll=self.unroll_factor)
-        return kernels.vadv(*f, named["wcon"], shift, compute=self.compute, tune=tune, timed=timed)
+        return kernels.vadv(*f, named["wcon"], shift, compute=self.compute, tune=self.current_tune(), timed=timed)

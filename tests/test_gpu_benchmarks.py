@@ -116,3 +116,20 @@ def test_cli_runs_a_benchmark(lib, tmp_path):
                    "--domain", "[32,64]", "32", "8", "--halo", "2", "2", "0"], standalone_mode=False)
     lines = out.read_text().splitlines()
     assert len(lines) == 1 + 4  # header + 2 domains x 2 executions
+
+
+@pytest.mark.parametrize("cls,kw", [
+    (horizontal_diffusion.JScan, {"halo": (2, 2, 0)}),
+    (horizontal_diffusion.TmaTile, {"halo": (2, 2, 0)}),
+    (horizontal_diffusion.VectorScan, {"halo": (2, 2, 0), "dtype": "bfloat16"}),
+    (vertical_advection.SharedMem, {"halo": (1, 1, 0)}),
+    (vertical_advection.Slab, {"halo": (1, 1, 0)}),
+    (vertical_advection.TensorMem, {"halo": (1, 1, 0)}),
+])
+def test_autotune_parameter(cls, kw, lib):
+    """autotune=True times the implementation's candidate shapes during setup,
+    runs the fastest (reported as `tune`) and still verifies."""
+    b = cls(domain=(96, 64, 40), autotune=True, **kw)
+    for _ in range(2):
+        r = b.run()
+        assert r["time"] > 0 and isinstance(r["tune"], str) and r["tune"]
