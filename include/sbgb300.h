@@ -64,7 +64,12 @@ extern "C" {
 #define SB_DEFAULT 4
 
 /* ---- kernel variants ------------------------------------------------------ */
-#define SB_VARIANT_AUTO 0
+#define SB_VARIANT_AUTO 0  /* the library's choice, where the layout qualifies:
+                            * hdiff: TMA for float64, VSCAN for float32, bfloat16
+                            * and float pairs, JSCAN otherwise (and for fixed64);
+                            * vadv: TMEM for float32 compute on >= 2048 column
+                            * groups (bfloat16: level stride a multiple of 8 bytes),
+                            * else SLAB / WSLAB when ccol/dcol are given, else SMEM */
 #define SB_HDIFF_TILE 1   /* smem-staged k-plane tiles, lap/flx/fly once per point */
 #define SB_HDIFF_JSCAN 2  /* register j-march, i-neighbours by warp shuffles       */
 #define SB_HDIFF_TMA 3    /* TILE with inp k-planes staged by TMA (cp.async.bulk.tensor)
@@ -85,7 +90,8 @@ extern "C" {
                            * 16-byte copies (needs i unit-stride); same tune fields.
                            * SB_VARIANT_AUTO with ccol/dcol given and no block/unroll
                            * in the tune picks WSLAB for 2/4-byte storage and SLAB
-                           * for 8-byte storage when the layout qualifies */
+                           * for 8-byte storage when the layout qualifies and TMEM
+                           * does not apply */
 #define SB_VADV_TMEM 5    /* float32 compute: WSLAB row staging, factors in tensor
                            * memory (tcgen05.st / tcgen05.ld) instead of a slab; one
                            * persistent block per SM; no scratch; needs i unit-stride
@@ -186,7 +192,8 @@ int sb_hdiff(int storage, int compute, const void* inp, const void* coeff, void*
  * for v, (0,0) for w.  ccol/dcol may be NULL; they are only used as scratch
  * (the reference's fields of the same names, compute-type sized elements) by
  * SB_VADV_GLOBAL, SB_VADV_SLAB, SB_VADV_WSLAB, and by SB_VARIANT_AUTO, which
- * picks a slab form when they are given.  Needs nk >= 2.                      */
+ * picks a slab form when they are given and the tensor-memory form does not
+ * apply.  Needs nk >= 2.                                                       */
 int sb_vadv(int storage, int compute, const void* stage, const void* pos, const void* tens,
             const void* tensstage, const void* wcon, void* out, void* ccol, void* dcol, int64_t ni,
             int64_t nj, int64_t nk, int64_t si, int64_t sj, int64_t sk, int wshift_i, int wshift_j,
