@@ -2,7 +2,9 @@
 
 Counterpart of stencil_benchmarks/benchmarks_collection/stencils/cuda_hip/
 horizontal_diffusion.py:40-128 (whose implementations are named after their
-algorithm).  Both classes run ``sb_hdiff``:
+algorithm).  Every class derives from the reference's
+``HorizontalDiffusionStencil`` (fields, verification, ``data_size``) and runs
+``sb_hdiff``:
 
 * ``JScan``      -- warp j-march with shuffles (HBM-efficient float32 form);
 * ``Tile``       -- shared-memory k-plane tiles (fewest fp64 operations);
@@ -15,15 +17,21 @@ algorithm).  Both classes run ``sb_hdiff``:
 
 from __future__ import annotations
 
+from stencil_benchmarks.benchmark import Parameter, ParameterError
+from stencil_benchmarks.benchmarks_collection.stencils import base
+
 from .... import _native, kernels
-from ....benchmark import Parameter, ParameterError
-from .. import base
 from .mixin import StencilMixin
 
 
 class HorizontalDiffusionMixin(StencilMixin):
     def tune(self):
         raise NotImplementedError
+
+    @property
+    def compulsory_bytes(self):
+        ni, nj, nk = self.domain
+        return ((ni + 4) * (nj + 4) * nk + 2 * ni * nj * nk) * self.dtype_size
 
     def launch(self, fields, timed):
         inp, coeff, out = fields
@@ -35,8 +43,8 @@ class JScan(HorizontalDiffusionMixin, base.HorizontalDiffusionStencil):
     unroll_factor = Parameter("rows loaded per batch (1, 2, 4 or 8)", 4, choices=[1, 2, 4, 8])
     k_per_block = Parameter("k-planes per block", 1)
 
-    def setup(self):
-        super().setup()
+    def check_parameters(self):
+        super().check_parameters()
         if not 1 <= self.block_size[0] <= 8 or self.block_size[1] < 1:
             raise ParameterError("block_size: 1..8 warps and at least 1 row")
 
@@ -53,8 +61,8 @@ class Tile(HorizontalDiffusionMixin, base.HorizontalDiffusionStencil):
     block_size = Parameter("threads along i, threads along j, rows per tile", (64, 4, 16))
     k_per_block = Parameter("k-planes per block", 4)
 
-    def setup(self):
-        super().setup()
+    def check_parameters(self):
+        super().check_parameters()
         bx, by, ty = self.block_size
         if (bx, by) not in {(32, 4), (32, 8), (64, 2), (64, 4), (64, 8), (128, 2), (128, 4)}:
             raise ParameterError("block_size[:2] must be one of 32x4, 32x8, 64x2, 64x4, 64x8, 128x2, 128x4")
@@ -77,8 +85,8 @@ class TmaTile(HorizontalDiffusionMixin, base.HorizontalDiffusionStencil):
     block_size = Parameter("threads along i, threads along j, rows per tile", (128, 4, 16))
     k_per_block = Parameter("k-planes per block (double-buffered)", 4)
 
-    def setup(self):
-        super().setup()
+    def check_parameters(self):
+        super().check_parameters()
         bx, by, ty = self.block_size
         if (bx, by) not in {(32, 8), (64, 4), (64, 8), (128, 2), (128, 4)}:
             raise ParameterError("block_size[:2] must be one of 32x8, 64x4, 64x8, 128x2, 128x4")
@@ -102,8 +110,8 @@ class VectorScan(HorizontalDiffusionMixin, base.HorizontalDiffusionStencil):
     unroll_factor = Parameter("rows loaded per batch (1, 2, 4 or 8)", 1, choices=[1, 2, 4, 8])
     k_per_block = Parameter("k-planes per block", 1)
 
-    def setup(self):
-        super().setup()
+    def check_parameters(self):
+        super().check_parameters()
         width, nw, rows = self.block_size
         if width not in (0, 64, 128, 256) or not 1 <= nw <= 8 or rows < 1:
             raise ParameterError("block_size: width 0, 64, 128 or 256, 1..8 warps, at least 1 row")

@@ -1,14 +1,24 @@
 """The GB300 backend: common part of every stencil benchmark.
 
 Counterpart of the reference's cuda_hip ``StencilMixin``
-(stencil_benchmarks/benchmarks_collection/stencils/cuda_hip/mixin.py:50-175):
-the same ``dry_runs`` / ``timers`` / ``gpu_architecture`` knobs and the same
-``run_stencil`` contract -- copy the host fields to the device, launch,
-time the launch with CUDA events ("gpu") or the host clock ("wall"), copy the
-fields back, return ``{"time": seconds}``.  Instead of rendering and
-compiling a kernel per parameter set it calls the prebuilt sm_103a library;
-the device fields are allocated once in ``setup`` (same layout as the host
-fields) rather than on every run.
+(stencil_benchmarks/benchmarks_collection/stencils/cuda_hip/mixin.py:50-175).
+The concrete classes derive from this mixin and from the reference's own
+``Stencil`` subclasses (stencil_benchmarks/benchmarks_collection/stencils/
+base.py), so the reference allocates and fills the host fields, runs and
+verifies them (``Stencil.run``, ``verify_stencil``) and reports
+``bandwidth``; this mixin only implements ``run_stencil``: copy the host
+fields to the device, launch the prebuilt sm_103a kernel, time the launch
+with CUDA events ("gpu") or the host clock ("wall"), copy the fields back and
+return ``{"time": seconds}`` plus ``gpoints_per_s`` and ``hbm_gbs``
+(compulsory bytes over the time).  The device fields are allocated once in
+``setup`` with the host fields' layout, instead of on every run.
+
+Additions to the reference's parameters: ``compute_dtype`` (the storage type
+stays ``dtype``), ``device`` and ``autotune``.  ``dtype`` also accepts
+"bfloat16" (host fields hold the 16-bit patterns as uint16, filled from the
+reference's U[0, 1) distribution rounded to nearest even); the reference's
+numpy verification has no bfloat16 type, so bfloat16 storage needs
+``verify=False``.
 """
 
 from __future__ import annotations
@@ -16,9 +26,19 @@ from __future__ import annotations
 import statistics
 import time
 
+import numpy as np
+from stencil_benchmarks.benchmark import Benchmark, ExecutionError, Parameter, ParameterError
+from stencil_benchmarks.tools import array as ref_array
+
 from .... import _native
-from ....benchmark import Benchmark, ExecutionError, Parameter, ParameterError
 from ....device import Field
+
+BFLOAT16 = "bfloat16"
+
+
+def _round_to_bf16_bits(values: np.ndarray) -> np.ndarray:
+    bits = values.astype(np.float32).view(np.uint32).astype(np.uint64)
+    return ((bits + 0x7FFF + ((bits >> 16) & 1)) >> 16).astype(np.uint16)
 
 
 class StencilMixin(Benchmark):
@@ -34,6 +54,28 @@ class StencilMixin(Benchmark):
     device = Parameter("CUDA device index", 0)
     autotune = Parameter("time this implementation's candidate launch shapes on the benchmark's own fields "
                          "during setup and run the fastest (reported as `tune`)", False)
+
+    # -- bfloat16 storage on top of the reference's field allocation ----------
+
+    @property
+    def dtype_size(self):
+        return 2 if self.dtype == BFLOAT16 else np.dtype(self.dtype).itemsize
+
+    def alloc_field(self, domain_with_halo, layout, index_to_align):
+        if self.dtype != BFLOAT16:
+            return super().alloc_field(domain_with_halo, layout, index_to_align)
+        # the reference's layout/alignment rule on a 2-byte element type
+        return ref_array.alloc_array(domain_with_halo, np.uint16, layout, self.alignment,
+                                     index_to_align=index_to_align, apply_offset=self.offset_allocations)
+
+    def random_field(self):
+        if self.dtype != BFLOAT16:
+            return super().random_field()
+        data = self.empty_field()
+        data[...] = _round_to_bf16_bits(np.random.default_rng().random(data.shape))
+        return data
+
+    # -- tuning -------------------------------------------------------------
 
     def tune(self):
         """This implementation's launch shape (None: the library's choice)."""
@@ -72,8 +114,22 @@ class StencilMixin(Benchmark):
             return "library default"
         return " ".join(f"{name}={getattr(t, name)}" for name, _ in t._fields_ if getattr(t, name))
 
+    # -- setup / run ----------------------------------------------------------
+
+    def check_parameters(self):
+        """Reject unsupported parameter values before any field is allocated."""
+        if self.dtype not in ("float64", "float32", BFLOAT16):
+            raise ParameterError(f"unsupported dtype {self.dtype!r}: float64, float32 or bfloat16")
+        if self.dtype == BFLOAT16 and self.verify:
+            raise ParameterError("bfloat16 storage: the reference's numpy verification has no bfloat16 type, "
+                                 "run with verify=False")
+        if self.compute_dtype == "float32" and self.dtype == "float64":
+            raise ParameterError("float64 storage with float32 compute is not provided")
+        if self.compute_dtype in ("float32x2", "fixed64") and self.dtype != "float64":
+            raise ParameterError(f"{self.compute_dtype} compute needs float64 storage")
+
     def setup(self):
-        super().setup()
+        self.check_parameters()
         if self.dry_runs < 0:
             raise ParameterError("dry_runs must be non-negative")
         try:
@@ -82,13 +138,8 @@ class StencilMixin(Benchmark):
             raise ParameterError(str(err)) from err
         if self.device >= ndev:
             raise ParameterError(f"CUDA device {self.device} not available ({ndev} device(s))")
+        super().setup()
         _native.call("sb_set_device", self.device)
-        if self.compute_dtype == "float32" and self.dtype == "float64":
-            raise ParameterError("float64 storage with float32 compute is not provided")
-        if self.compute_dtype in ("float32x2", "fixed64") and self.dtype != "float64":
-            raise ParameterError(f"{self.compute_dtype} compute needs float64 storage")
-        if self.compute_dtype == "fixed64" and self.stencil_kind != "horizontal_diffusion":
-            raise ParameterError("fixed64 compute is provided for horizontal diffusion only")
         self._device_fields = [Field.like_host(host, self.dtype, self.halo) for host in self._data[0]]
         self._picked_tune = None
         if self.autotune:
@@ -99,6 +150,11 @@ class StencilMixin(Benchmark):
         if self.compute_dtype == "auto":
             return "float64" if self.dtype == "float64" else "float32"
         return self.compute_dtype
+
+    @property
+    def compulsory_bytes(self) -> int:
+        """Bytes a perfect kernel moves: each input read once, each output written once."""
+        raise NotImplementedError
 
     def launch(self, fields, timed: bool):
         """Launch the stencil on device ``fields``; with ``timed`` return seconds."""
@@ -124,6 +180,11 @@ class StencilMixin(Benchmark):
             raise ExecutionError(str(err)) from err
         for host, dev in zip(data, fields):
             dev.download(host)
+        result = {
+            "time": elapsed,
+            "gpoints_per_s": float(np.prod(self.domain)) / elapsed / 1e9,
+            "hbm_gbs": self.compulsory_bytes / elapsed / 1e9,
+        }
         if self.autotune:
-            return {"time": elapsed, "tune": self.describe_tune(self.current_tune())}
-        return {"time": elapsed}
+            result["tune"] = self.describe_tune(self.current_tune())
+        return result

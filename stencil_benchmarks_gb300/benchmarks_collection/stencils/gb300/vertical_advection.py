@@ -1,7 +1,9 @@
 """Vertical advection on GB300: ``sbench stencils gb300 vertical-advection <impl>``.
 
 Counterpart of stencil_benchmarks/benchmarks_collection/stencils/cuda_hip/
-vertical_advection.py:39-73.  The fields and the in-place update of
+vertical_advection.py:39-73.  Every class derives from the reference's
+``VerticalAdvectionStencil`` (fields, verification, ``data_size``).  The
+fields and the in-place update of
 ``utensstage`` (and, with ``all_components``, ``vtensstage``/``wtensstage``)
 are the reference's; each component is one ``sb_vadv`` launch, with wcon read
 at the column shifted by (1, 0), (0, 1) and (0, 0) for u, v and w
@@ -25,10 +27,13 @@ from __future__ import annotations
 import ctypes
 import warnings
 
+import numpy as np
+
+from stencil_benchmarks.benchmark import Parameter, ParameterError
+from stencil_benchmarks.benchmarks_collection.stencils import base
+
 from .... import _native, kernels
-from ....benchmark import Parameter, ParameterError
 from ....device import _stream_arg
-from .. import base
 from .mixin import StencilMixin
 
 _SHIFTS = {"u": (1, 0), "v": (0, 1), "w": (0, 0)}
@@ -38,13 +43,24 @@ class VerticalAdvectionMixin(StencilMixin):
     block_size = Parameter("threads per block along i and j", (32, 1))
     unroll_factor = Parameter("levels of inputs kept in flight (1, 2, 4 or 8)", 4, choices=[1, 2, 4, 8])
 
-    def setup(self):
-        super().setup()
+    def check_parameters(self):
+        super().check_parameters()
+        if self.compute_dtype == "fixed64":
+            raise ParameterError("fixed64 compute is provided for horizontal diffusion only")
+        if self.domain[2] < 2 and int(np.prod(self.domain)) > 0:
+            raise ParameterError("vertical advection needs at least 2 levels")
         if self.verify and self.dry_runs:
             warnings.warn(
                 "using --dry-runs together with verification might lead to false negatives for "
                 "stencils with read-write fields"
             )
+
+    @property
+    def compulsory_bytes(self):
+        ni, nj, nk = self.domain
+        comps = 3 if self.all_components else 1
+        # per component: stage, pos, tens, tensstage read + tensstage written; wcon once (+ shifted column/row)
+        return (comps * 5 * ni * nj * nk + (ni + 1) * (nj + 1) * nk) * self.dtype_size
 
     def components(self, fields):
         named = dict(zip(self.args, fields))
@@ -80,8 +96,8 @@ class GlobalScratch(VerticalAdvectionMixin, base.VerticalAdvectionStencil):
     block_size = Parameter("threads per block along i and j", (64, 1))
     unroll_factor = Parameter("levels of inputs kept in flight (1, 2, 4 or 8)", 2, choices=[1, 2, 4, 8])
 
-    def setup(self):
-        super().setup()
+    def check_parameters(self):
+        super().check_parameters()
         if self.dtype_size != {"float64": 8, "float32": 4, "float32x2": 8}[self.compute]:
             raise ParameterError("GlobalScratch keeps the factors in ccol/dcol: storage and compute types must match")
 
@@ -103,8 +119,8 @@ class Slab(VerticalAdvectionMixin, base.VerticalAdvectionStencil):
                            (32, 8))
     unroll_factor = Parameter("levels of inputs kept in flight (2, 4 or 8)", 4, choices=[2, 4, 8])
 
-    def setup(self):
-        super().setup()
+    def check_parameters(self):
+        super().check_parameters()
         if self.dtype_size != {"float64": 8, "float32": 4, "float32x2": 8}.get(self.compute, 0) and not (
                 self.dtype == "bfloat16" and self.compute == "float32"):
             raise ParameterError("Slab stages its ccol/dcol factors in ring entries: compute type as wide as storage")
@@ -141,8 +157,8 @@ class TensorMem(VerticalAdvectionMixin, base.VerticalAdvectionStencil):
     dtype = Parameter("data type: float32 or bfloat16 (float32 compute)", "float32")
     unroll_factor = Parameter("levels of inputs kept in flight (4, 8 or 16)", 8, choices=[4, 8, 16])
 
-    def setup(self):
-        super().setup()
+    def check_parameters(self):
+        super().check_parameters()
         if self.compute != "float32":
             raise ParameterError("TensorMem keeps float32 factors in tensor memory: float32 compute only")
         if self.domain[2] > 256:

@@ -9,17 +9,19 @@ per kernel with the reference's keys ``name``, ``bandwidth`` (MB/s of the best
 round, 2 or 3 arrays moved), ``avg-time``, ``time`` (the best) and
 ``max-time``.  With ``verify`` the final arrays are checked against the
 scalar recurrence with the reference's criterion (average relative error at
-most 1e-6 for float32, 1e-13 for float64).
+most 1e-6 for float32, 1e-13 for float64); a failure raises the reference's
+``ValidationError``.  The class derives from the reference's ``Benchmark``,
+so it registers as ``stream gb300 native``.
 """
 
 from __future__ import annotations
 
 import numpy as np
+from stencil_benchmarks.benchmark import Benchmark, ExecutionError, Parameter, ParameterError
+from stencil_benchmarks.tools.validation import ValidationError
 
 from ... import _native, kernels
-from ...benchmark import Benchmark, ExecutionError, Parameter, ParameterError
 from ...device import DeviceBuffer, copy_to_host
-from ...validation import ValidationError
 
 
 class Native(Benchmark):

@@ -8,7 +8,8 @@ runs on the cubic-ish domains 32x32x80, 64x64x80, ..., 1024x1024x80
 (``--min-exp``/``--max-exp`` change the range), ``--executions`` times each,
 and every execution becomes one CSV row holding the configuration name, all
 benchmark parameters and the result columns.  The table is written with the
-standard library (the reference builds a pandas DataFrame).
+standard library: the reference's driver (tools/multirun.py) imports pandas
+at module level, which neither machine here has.
 
     python -m stencil_benchmarks_gb300.collection basic-bandwidth out.csv -e 11
     python -m stencil_benchmarks_gb300.collection horizontal-diffusion-bandwidth out.csv -o dtype='"float32"'
@@ -27,8 +28,11 @@ import re
 import warnings
 from typing import Callable, Dict, Iterable, List, Optional, Sequence, Tuple
 
-from . import benchmark
 from .benchmarks_collection.stencils.gb300 import basic, horizontal_diffusion as hdiff, vertical_advection as vadv
+from .host import load
+
+load()
+from stencil_benchmarks.benchmark import ParameterError  # noqa: E402
 
 
 class Configuration:
@@ -72,7 +76,7 @@ def run_scaling_benchmark(configurations: Sequence[Configuration], executions: i
             for config in configurations:
                 try:
                     instance = config.instantiate(domain, preprocess)
-                except benchmark.ParameterError as err:
+                except ParameterError as err:
                     echo(f"skipping {config.name} on {domain}: {err}")
                     continue
                 for _ in range(executions):

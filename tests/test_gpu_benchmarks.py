@@ -1,24 +1,49 @@
-"""Every registered benchmark, run through the Benchmark API with verification
-(the reference's test_benchmarks_collection.py strategy, here on the GPU and
-with the CPU oracle installed as the verifier)."""
+"""Every gb300 benchmark class run through the reference's own Benchmark API:
+``Stencil.run`` cycles the data sets, calls ``run_stencil`` and verifies with
+the reference's numpy ``verify_stencil`` (the strategy of the reference's
+test_benchmarks_collection.py, here on the GPU).  Exact forms are also
+checked bit for bit against the oracle, and bfloat16 storage (which the
+reference's verification cannot take) against the oracle only."""
 
 from __future__ import annotations
 
+import copy
+
 import pytest
 
-from stencil_benchmarks_gb300 import benchmark
-from stencil_benchmarks_gb300 import benchmarks_collection  # noqa: F401
-from stencil_benchmarks_gb300.benchmarks_collection.stencils.gb300 import (
+from tests.host_framework import require
+from tests.verifiers import check_bit_exact
+
+pytestmark = pytest.mark.gpu
+
+require()
+
+import stencil_benchmarks.benchmarks_collection  # noqa: E402,F401
+from stencil_benchmarks import benchmark  # noqa: E402
+from stencil_benchmarks.benchmarks_collection.stencils import base  # noqa: E402
+
+from stencil_benchmarks_gb300 import benchmarks_collection  # noqa: E402,F401
+from stencil_benchmarks_gb300.benchmarks_collection.stencils.gb300 import (  # noqa: E402
     basic,
     horizontal_diffusion,
     vertical_advection,
 )
-from stencil_benchmarks_gb300.benchmarks_collection.stream import gb300 as stream
-
-pytestmark = pytest.mark.gpu
+from stencil_benchmarks_gb300.benchmarks_collection.stream import gb300 as stream  # noqa: E402
 
 OURS = sorted((b for b in benchmark.REGISTRY if b.__module__.startswith("stencil_benchmarks_gb300.")),
               key=lambda b: (b.__module__, b.__name__))
+HDIFF = [horizontal_diffusion.JScan, horizontal_diffusion.Tile, horizontal_diffusion.TmaTile,
+         horizontal_diffusion.VectorScan]
+
+
+def run_checked(b, exact=True):
+    """One ``run()`` through the reference's Stencil.run, then the oracle check."""
+    index = b._run % b.data_sets
+    before = copy.deepcopy(b._data[index])
+    result = b.run()
+    if exact:
+        check_bit_exact(b, before, b._data[index])
+    return result
 
 
 @pytest.mark.parametrize("bmark", OURS, ids=lambda b: f"{b.__module__.split('.')[-1]}.{b.__name__}")
@@ -27,37 +52,51 @@ def test_default_construction_runs_and_verifies(bmark, lib):
     results = instance.run()
     results = results if isinstance(results, list) else [results]
     assert all(r["time"] > 0 for r in results)
-    # a second execution (the data set cycles / STREAM reruns)
-    instance.run()
+    instance.run()  # a second execution
 
 
-@pytest.mark.parametrize("cls", [horizontal_diffusion.JScan, horizontal_diffusion.Tile, horizontal_diffusion.TmaTile,
-                                 horizontal_diffusion.VectorScan])
+@pytest.mark.parametrize("cls", HDIFF, ids=lambda c: c.__name__)
+def test_hdiff_128x128x64_through_the_reference_stencil_run(cls, lib):
+    """hdiff fp64 on 128x128x64 with a (2, 2, 0) halo (arrays 132x132x64), the
+    reference's own Stencil.run and verify_stencil, every implementation, and
+    bit for bit against the oracle; two data sets cycle so every other run
+    starts on fields that are not the previous run's."""
+    b = cls(domain=(128, 128, 64), halo=(2, 2, 0), data_sets=2)
+    assert isinstance(b, base.HorizontalDiffusionStencil)
+    assert b._data[0].inp.shape == (132, 132, 64)
+    for _ in range(3):
+        r = run_checked(b)
+        assert r["bandwidth"] == pytest.approx(b.data_size / r["time"] / 1e9)
+        assert r["gpoints_per_s"] > 0 and r["hbm_gbs"] > 0
+
+
+@pytest.mark.parametrize("cls", HDIFF, ids=lambda c: c.__name__)
 @pytest.mark.parametrize("dtype", ["float64", "float32", "bfloat16"])
 def test_hdiff_benchmark_forms(cls, dtype, lib):
-    b = cls(domain=(100, 77, 9), halo=(2, 2, 0), dtype=dtype, data_sets=2, alignment=0)
+    b = cls(domain=(100, 77, 9), halo=(2, 2, 0), dtype=dtype, data_sets=2, alignment=0,
+            verify=dtype != "bfloat16")
     for _ in range(3):
-        r = b.run()
+        r = run_checked(b)
         assert r["gpoints_per_s"] > 0 and r["bandwidth"] > 0
 
 
 @pytest.mark.parametrize("cls", [vertical_advection.SharedMem, vertical_advection.GlobalScratch,
-                                 vertical_advection.Slab, vertical_advection.NoAlloc])
+                                 vertical_advection.Slab, vertical_advection.NoAlloc], ids=lambda c: c.__name__)
 @pytest.mark.parametrize("all_components", [False, True])
 def test_vadv_benchmark_forms(cls, all_components, lib):
     b = cls(domain=(64, 40, 30), halo=(1, 1, 1), all_components=all_components)
-    b.run()
+    run_checked(b)
+    run_checked(b)
 
 
 @pytest.mark.parametrize("dtype", ["float32", "bfloat16"])
 @pytest.mark.parametrize("all_components", [False, True])
 def test_vadv_tensor_mem_benchmark(dtype, all_components, lib):
-    """The reference's numpy verification of float32 / bfloat16-storage runs
-    with the factors in tensor memory."""
+    """float32 / bfloat16-storage runs with the factors in tensor memory."""
     b = vertical_advection.TensorMem(domain=(64, 40, 30), halo=(1, 1, 1), dtype=dtype,
-                                     all_components=all_components)
+                                     all_components=all_components, verify=dtype != "bfloat16")
     for _ in range(2):
-        b.run()
+        run_checked(b)
     with pytest.raises(benchmark.ParameterError):
         vertical_advection.TensorMem(domain=(64, 40, 30), halo=(1, 1, 1), dtype="float64")
 
@@ -70,7 +109,9 @@ def test_vadv_tensor_mem_benchmark(dtype, all_components, lib):
 def test_fast_float64_forms_verify(cls, compute, lib):
     """The fast float64 forms pass the reference's own float64 tolerance."""
     halo = (2, 2, 0) if cls.__module__.endswith("horizontal_diffusion") else (1, 1, 0)
-    cls(domain=(90, 70, 12), halo=halo, compute_dtype=compute, data_sets=2).run()
+    b = cls(domain=(90, 70, 12), halo=halo, compute_dtype=compute, data_sets=2)
+    b.run()
+    b.run()
 
 
 def test_fast_forms_parameter_checks(lib):
@@ -81,8 +122,8 @@ def test_fast_forms_parameter_checks(lib):
 
 
 def test_vadv_fp32_storage_with_fp64_solve(lib):
-    vertical_advection.SharedMem(domain=(64, 40, 30), halo=(1, 1, 0), dtype="float32",
-                                 compute_dtype="float64").run()
+    b = vertical_advection.SharedMem(domain=(64, 40, 30), halo=(1, 1, 0), dtype="float32", compute_dtype="float64")
+    run_checked(b)
 
 
 @pytest.mark.parametrize("cls,kw", [
@@ -93,7 +134,7 @@ def test_vadv_fp32_storage_with_fp64_solve(lib):
     (basic.Copy, {"layout": (0, 1, 2), "alignment": 64}),
 ])
 def test_basic_benchmark_variants(cls, kw, lib):
-    cls(domain=(50, 30, 20), **kw).run()
+    run_checked(cls(domain=(50, 30, 20), **kw))
 
 
 def test_wall_timers_and_dry_runs(lib):
@@ -107,21 +148,23 @@ def test_stream_native(lib):
     assert all(r["bandwidth"] > 0 and r["time"] <= r["avg-time"] <= r["max-time"] for r in res)
 
 
-def test_cli_runs_a_benchmark(lib, tmp_path):
+def test_reference_cli_runs_a_gb300_benchmark(lib, tmp_path):
+    """The reference's CLI (through the launcher) runs, verifies and reports."""
     pytest.importorskip("click")
     from stencil_benchmarks_gb300 import cli
 
     out = tmp_path / "res.csv"
-    cli.main(args=["-e", "2", "-o", str(out), "stencils", "gb300", "horizontal-diffusion", "j-scan",
+    cli.main(args=["-e", "2", "-o", str(out), "stencils", "gb300", "horizontal-diffusion", "tma-tile",
                    "--domain", "[32,64]", "32", "8", "--halo", "2", "2", "0"], standalone_mode=False)
     lines = out.read_text().splitlines()
     assert len(lines) == 1 + 4  # header + 2 domains x 2 executions
+    assert "bandwidth" in lines[0] and "gpoints_per_s" in lines[0]
 
 
 @pytest.mark.parametrize("cls,kw", [
     (horizontal_diffusion.JScan, {"halo": (2, 2, 0)}),
     (horizontal_diffusion.TmaTile, {"halo": (2, 2, 0)}),
-    (horizontal_diffusion.VectorScan, {"halo": (2, 2, 0), "dtype": "bfloat16"}),
+    (horizontal_diffusion.VectorScan, {"halo": (2, 2, 0), "dtype": "bfloat16", "verify": False}),
     (vertical_advection.SharedMem, {"halo": (1, 1, 0)}),
     (vertical_advection.Slab, {"halo": (1, 1, 0)}),
     (vertical_advection.TensorMem, {"halo": (1, 1, 0)}),
@@ -131,5 +174,5 @@ def test_autotune_parameter(cls, kw, lib):
     runs the fastest (reported as `tune`) and still verifies."""
     b = cls(domain=(96, 64, 40), autotune=True, **kw)
     for _ in range(2):
-        r = b.run()
+        r = run_checked(b)
         assert r["time"] > 0 and isinstance(r["tune"], str) and r["tune"]
