@@ -496,6 +496,8 @@ def run_batched(seed=3, n_domains=64, storage="float32", reps=5):
     batch.set(doms)
     t_batch = autotune.time_batch(batch, reps=reps, warmup=2, stream=stream)
     info = batch.info()
+    stream.synchronize()
+    checked = verify_batched(specs, built, storage)
     ta, ts = statistics.median(t_async), statistics.median(t_sync)
     return {
         "workload": f"{n_domains} uneven domains (half hdiff, half vadv), ni,nj in {{32..512 step 32}}, "
@@ -509,7 +511,44 @@ def run_batched(seed=3, n_domains=64, storage="float32", reps=5):
         "speedup_vs_back_to_back": ta / t_batch,
         "speedup_vs_each_synchronised": ts / t_batch,
         "autotuned": best, "candidates_timed": len(table),
+        "verified": all(ok for _, ok in checked),
+        "verified_domains": [f"{what}: {ok}" for what, ok in checked],
     }
+
+
+def verify_batched(specs, built, storage):
+    """Compare the batch's outputs of the tallest and the widest domain bit for
+    bit with a per-domain launch of the plain kernel into a fresh field."""
+    from stencil_benchmarks_gb300 import _native, kernels
+    from stencil_benchmarks_gb300.device import Field
+
+    def interior(host, spec, halo):
+        return np.ascontiguousarray(host[halo[0]:halo[0] + spec.ni, halo[1]:halo[1] + spec.nj,
+                                         halo[2]:halo[2] + spec.nk])
+
+    def download(field, like):
+        span = int(np.sum((np.array(like.shape) - 1) * np.array(like.strides))) + like.itemsize
+        out = np.ndarray(like.shape, dtype=like.dtype, strides=like.strides, buffer=np.zeros(span, dtype=np.uint8))
+        field.download(out)
+        return out
+
+    tall = max(range(len(specs)), key=lambda q: (specs[q].nk, specs[q].points))
+    wide = max(range(len(specs)), key=lambda q: (specs[q].ni * specs[q].nj, specs[q].nk))
+    results = []
+    for what, q in (("tallest", tall), ("widest", wide)):
+        spec, (dom, dev, host) = specs[q], built[q]
+        halo = dev["out"].halo
+        got = interior(download(dev["out"], host["out"]), spec, halo)
+        fresh = Field.like_host(host["out"], storage, halo)
+        if spec.op == "hdiff":
+            kernels.hdiff(dom.inp, dom.coeff, fresh)
+        else:
+            kernels.vadv(dom.stage, dom.pos, dom.tens, dom.tensstage, dom.wcon, out=fresh)
+        _native.synchronize()
+        want = interior(download(fresh, host["out"]), spec, halo)
+        same = got.tobytes() == want.tobytes()
+        results.append((f"{what} {spec.op} {spec.ni}x{spec.nj}x{spec.nk}", bool(same)))
+    return results
 
 
 def run_served(n_requests=2000, rates=(1000.0, 5000.0, 20000.0), seed=11, float64_compute="float64"):

@@ -121,9 +121,30 @@ const char* sb_last_error(void);
 int sb_version(void);
 int sb_device_count(int* count);
 int sb_set_device(int device);
+int sb_get_device(int* device); /* the calling thread's current device */
 int sb_device_info(int device, char* name, int name_len, int* sm_count, int* cc_major,
                    int* cc_minor, size_t* total_mem, int* l2_bytes, int* smem_optin);
 int sb_synchronize(void);
+
+/* Bounded waits.  The only kernels that wait on the device are the hdiff
+ * TMA tiles (SB_HDIFF_TMA), which wait on an mbarrier for each plane's tensor
+ * copy.  A wait gives up after a bounded number of polls; the whole thread
+ * block then stops before storing that plane, waits (bounded) for the copies
+ * it still has in flight and sets a process-wide status word held in
+ * page-locked, device-mapped host memory (allocated by the first TMA launch:
+ * make the first sb_hdiff call before any stream capture).  The give-up is
+ * reported as SB_ERR_TIMEOUT, and the word cleared, by the first of: a timed
+ * sb_hdiff call (after its launch), the next sb_hdiff call (before it
+ * launches anything), sb_synchronize, sb_stream_synchronize,
+ * sb_event_synchronize, or sb_kernel_status.  No reference counterpart (its
+ * kernels do not wait on the device).
+ * sb_kernel_status: SB_ERR_TIMEOUT if a launch has given up since the last
+ * report, else SB_OK; does not synchronise.
+ * sb_debug_wait_limit: testing aid, the polls of each first wait (0: give up
+ * at once; -1: the default, 2^20); the drain of copies in flight always uses
+ * the default.                                                              */
+int sb_kernel_status(void);
+int sb_debug_wait_limit(int polls);
 
 /* ---- memory (reference: stencils/cuda_hip/api.py:54-94 via libcudart) ---- */
 int sb_malloc(void** ptr, size_t bytes);
@@ -305,6 +326,8 @@ int sb_arena_destroy(sb_arena* arena);
  * 64 slots fails with SB_ERR_BUDGET before launching.  The first call on a
  * device looks up the array's device address (cudaGetSymbolAddress) and
  * caches it: make that first call before any stream capture on the device.
+ * The cached address does not survive cudaDeviceReset: a process that resets
+ * a device must not call this entry point on that device afterwards.
  * Every call shares the array, so calls that overlap on the GPU race and
  * must be serialised by the caller; every factor is written before it is
  * read, so no state carries over between calls.                             */

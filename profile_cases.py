@@ -1,6 +1,6 @@
 """Launch named kernel cases a fixed number of times (for ncu captures).
 
-    python -m stencil_benchmarks_gb300.profile_cases [--warmup W] [--launches L] CASE...
+    python profile_cases.py [--warmup W] [--launches L] CASE...
 
 CASE is ``<stencil>-<form>[:<variant>]`` with stencil in hdiff, vadv, triad, copy, lap and
 form in f64, f32, bf16 (bf16 = bfloat16 storage, f32 compute), f32x2
@@ -22,12 +22,15 @@ from __future__ import annotations
 import argparse
 import statistics
 import sys
+from pathlib import Path
 
 import numpy as np
 
-from . import _native, kernels
-from . import array as sbarray
-from .device import DeviceBuffer, Field
+sys.path.insert(0, str(Path(__file__).resolve().parent))
+
+from stencil_benchmarks_gb300 import _native, kernels  # noqa: E402
+from stencil_benchmarks_gb300 import array as sbarray  # noqa: E402
+from stencil_benchmarks_gb300.device import DeviceBuffer, Field  # noqa: E402
 
 NI, NJ, NK = 512, 512, 80
 STORAGE = {"f64": ("float64", "float64"), "f32": ("float32", "float32"), "bf16": ("bfloat16", "float32"),

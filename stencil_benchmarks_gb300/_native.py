@@ -91,10 +91,13 @@ SIGNATURES = {
     "sb_version": [],
     "sb_device_count": [ctypes.POINTER(_int)],
     "sb_set_device": [_int],
+    "sb_get_device": [ctypes.POINTER(_int)],
     "sb_device_info": [_int, ctypes.c_char_p, _int, ctypes.POINTER(_int), ctypes.POINTER(_int),
                        ctypes.POINTER(_int), ctypes.POINTER(_size), ctypes.POINTER(_int),
                        ctypes.POINTER(_int)],
     "sb_synchronize": [],
+    "sb_kernel_status": [],
+    "sb_debug_wait_limit": [_int],
     "sb_malloc": [ctypes.POINTER(_vp), _size],
     "sb_free": [_vp],
     "sb_malloc_host": [ctypes.POINTER(_vp), _size],
@@ -185,6 +188,12 @@ def call(name, *args):
 def device_count() -> int:
     n = ctypes.c_int(0)
     call("sb_device_count", ctypes.byref(n))
+    return n.value
+
+
+def current_device() -> int:
+    n = ctypes.c_int(0)
+    call("sb_get_device", ctypes.byref(n))
     return n.value
 
 

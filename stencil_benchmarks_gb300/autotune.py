@@ -89,7 +89,7 @@ def autotune_batch(storage: str, domains: Sequence[Domain], max_nk: int, compute
 
     With a cache hit the list is empty and no kernel runs."""
     compute = compute or ("float64" if storage == "float64" else "float32")
-    key = "|".join([_native.device_info(0)["name"], storage, compute, signature(domains)])
+    key = "|".join([_native.device_info(_native.current_device())["name"], storage, compute, signature(domains)])
     path = cache_path()
     cache = _load_cache(path) if use_cache else {}
     if use_cache and key in cache:

@@ -18,7 +18,10 @@ stays ``dtype``), ``device`` and ``autotune``.  ``dtype`` also accepts
 "bfloat16" (host fields hold the 16-bit patterns as uint16, filled from the
 reference's U[0, 1) distribution rounded to nearest even); the reference's
 numpy verification has no bfloat16 type, so bfloat16 storage needs
-``verify=False``.
+``verify=False``.  A compute type wider than the storage (float32 fields,
+float64 arithmetic) is more accurate than the reference's check, which
+recomputes in the storage type: in ill-conditioned vertical-advection columns
+the two can differ by more than the reference's float32 tolerance.
 """
 
 from __future__ import annotations

@@ -48,6 +48,20 @@ struct DeviceProps {
 int device_props(const DeviceProps** out);
 
 // ---------------------------------------------------------------------------
+// bounded device-side waits
+// ---------------------------------------------------------------------------
+// A kernel whose wait gives up sets a process-wide status word that lives in
+// page-locked, device-mapped host memory (allocated on the first call of
+// status_word), so the host reads it without synchronising.  take_wait_status
+// returns SB_ERR_TIMEOUT (with a message) and clears the word if it was set.
+int status_word(int** device_ptr);
+int take_wait_status();
+// Polls of a first wait before a thread block gives up (default 2^20; the
+// drain of copies still in flight after a give-up always uses the default).
+constexpr int kDefaultWaitPolls = 1 << 20;
+int wait_polls();
+
+// ---------------------------------------------------------------------------
 // element types
 // ---------------------------------------------------------------------------
 using bf16 = __nv_bfloat16;

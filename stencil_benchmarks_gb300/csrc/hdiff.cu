@@ -263,16 +263,20 @@ int launch_tile(const void* inp, const void* coeff, void* out, int64_t ni, int64
 // 16 bytes) and holds global i = i0 - 2 - off + c in column c; the box is
 // TX + PADX columns wide (PADX >= 4 + the largest off) and TY + 4 rows high.
 // Boxes reaching past the array are zero-filled by the hardware; those
-// columns and rows only feed points that are not stored.  Waits are bounded:
-// a wait that gives up sets g_tma_timeout, waits (bounded) for the other
-// stage's copy and the CTA returns; sb_hdiff reports SB_ERR_TIMEOUT.
-__device__ int g_tma_timeout = 0;
+// columns and rows only feed points that are not stored.  Waits are bounded
+// (`polls` tries).  The give-up decision is taken by the whole CTA at the
+// barrier after the lap phase (__syncthreads_or of the threads' results), so
+// all threads leave together and none stores an output of that plane; before
+// leaving, the leader waits (with the default bound) for the copies the CTA
+// still has in flight and sets the status word, which the next status check
+// of the library reports as SB_ERR_TIMEOUT.  Only if such a copy does not
+// land within the default bound either can the CTA exit with it pending.
 thread_local bool t_tma_used = false;
 
 __device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t phase) {
-    for (int it = 0; it < (1 << 20); ++it) {
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t phase, int polls) {
+    for (int it = 0; it < polls; ++it) {
         uint32_t done;
         asm volatile(
             "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
@@ -316,7 +320,8 @@ struct TmaSmem {
 template <class S, class C, int TX, int NTY>
 __global__ void __launch_bounds__(TX* NTY)
     hdiff_tma_kernel(const __grid_constant__ CUtensorMap tmap, const S* __restrict__ coeff, S* __restrict__ out,
-                     int ni, int nj, int nk, int64_t sj, int64_t sk, int TY, int kper, int off) {
+                     int ni, int nj, int nk, int64_t sj, int64_t sk, int TY, int kper, int off, int polls,
+                     int* status) {
     using A = Ar<C>;
     using M = TmaSmem<S, C>;
     using T = typename std::conditional<M::CONV, C, S>::type;  // element type the stencil reads
@@ -350,11 +355,17 @@ __global__ void __launch_bounds__(TX* NTY)
     uint32_t phases = 0u;  // bit q: parity to wait for on stage q
     for (int k = k0; k < k1; ++k) {
         const int sidx = (k - k0) & 1;
-        if (!mbar_wait(bar0 + 8 * sidx, (phases >> sidx) & 1u)) {
-            atomicExch(&g_tma_timeout, 1);
-            if (k + 1 < k1) mbar_wait(bar0 + 8 * (sidx ^ 1), (phases >> (sidx ^ 1)) & 1u);
-            return;
-        }
+        const bool landed = mbar_wait(bar0 + 8 * sidx, (phases >> sidx) & 1u, polls);
+        // a CTA that gives up: drain its copies in flight, flag, leave together
+        auto give_up = [&]() {
+            if (leader) {
+                mbar_wait(bar0 + 8 * sidx, (phases >> sidx) & 1u, kDefaultWaitPolls);
+                if (k + 1 < k1) mbar_wait(bar0 + 8 * (sidx ^ 1), (phases >> (sidx ^ 1)) & 1u, kDefaultWaitPolls);
+                *(volatile int*)status = 1;
+                __threadfence_system();
+            }
+            __syncthreads();
+        };
         phases ^= 1u << sidx;
         // s_in(r, c) <-> global (i0 - 2 + c, j0 - 2 + r)
         const S* s_land = reinterpret_cast<const S*>(smem_tma + sidx * stage) + off;
@@ -362,7 +373,11 @@ __global__ void __launch_bounds__(TX* NTY)
         if constexpr (M::CONV) {
             for (int r = ty; r < TY + 4; r += NTY)
                 for (int c = tx; c < TX + 4; c += TX) s_conv[r * BX + c] = cvt<C, S>(s_land[r * BX + c]);
-            __syncthreads();
+            if (__syncthreads_or(!landed)) {
+                phases ^= 1u << sidx;  // the drain waits on the phase not yet seen
+                give_up();
+                return;
+            }
             s_in = s_conv;
         } else {
             s_in = s_land;
@@ -377,7 +392,13 @@ __global__ void __launch_bounds__(TX* NTY)
                 s_lap[jj * WL + ii] = A::sub(A::template scale2<2>(cvt<C, T>(c[0])), sum);
             }
         }
-        __syncthreads();
+        if constexpr (M::CONV) {
+            __syncthreads();
+        } else if (__syncthreads_or(!landed)) {
+            phases ^= 1u << sidx;  // the drain waits on the phase not yet seen
+            give_up();
+            return;
+        }
         for (int jj = ty; jj < TY; jj += NTY) {
             for (int ii = tx; ii < WF; ii += TX) {
                 const C* l = s_lap + (jj + 1) * WL + ii;
@@ -470,21 +491,13 @@ int launch_tma(const void* inp, const void* coeff, void* out, int64_t ni, int64_
     if (smem > 48 * 1024) SB_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const int64_t gx = ceil_div(ni, TX), gy = ceil_div(nj, ty), gz = ceil_div(nk, kper);
     SB_CHECK(gy <= p->max_grid_y && gz <= p->max_grid_z, SB_ERR_INVALID, "hdiff grid too large");
+    int* status = nullptr;
+    const int rc = status_word(&status);
+    if (rc) return rc;
     t_tma_used = true;
     kernel<<<dim3((unsigned)gx, (unsigned)gy, (unsigned)gz), dim3(TX, NTY), smem, stream>>>(
-        tmap, (const S*)coeff, (S*)out, (int)ni, (int)nj, (int)nk, sj, sk, ty, kper, off);
+        tmap, (const S*)coeff, (S*)out, (int)ni, (int)nj, (int)nk, sj, sk, ty, kper, off, wait_polls(), status);
     return SB_OK;
-}
-
-// After a synchronous (timed) TMA launch: SB_ERR_TIMEOUT if a CTA gave up
-// waiting for its copies (the flag is cleared).
-int tma_timeout_status() {
-    int flag = 0;
-    SB_CUDA(cudaMemcpyFromSymbol(&flag, g_tma_timeout, sizeof(int)));
-    if (!flag) return SB_OK;
-    const int zero = 0;
-    SB_CUDA(cudaMemcpyToSymbol(g_tma_timeout, &zero, sizeof(int)));
-    return fail(SB_ERR_TIMEOUT, "hdiff TMA: a thread block timed out waiting for its tensor copies");
 }
 
 template <class S, class C>
@@ -647,6 +660,9 @@ extern "C" int sb_hdiff(int storage, int compute, const void* inp, const void* c
         if (time_s) *time_s = 0.0;
         return SB_OK;
     }
+    // a give-up of an earlier launch is reported before anything new runs
+    rc = take_wait_status();
+    if (rc) return rc;
     cudaStream_t s = (cudaStream_t)stream;
     t_tma_used = false;
     rc = timed(s, time_s, [&]() {
@@ -664,6 +680,6 @@ extern "C" int sb_hdiff(int storage, int compute, const void* inp, const void* c
             return launch_typed<bf16, float>(inp, coeff, out, ni, nj, nk, si, sj, sk, tune, s);
         return fail(SB_ERR_UNSUPPORTED, "unsupported storage/compute combination (%d, %d)", storage, compute);
     });
-    if (rc == SB_OK && time_s && t_tma_used) rc = tma_timeout_status();
+    if (rc == SB_OK && time_s && t_tma_used) rc = take_wait_status();
     return rc;
 }

@@ -1,5 +1,6 @@
 // Library plumbing behind the C ABI: error strings, device queries, memory,
 // streams/events, L2 flush and the arithmetic-rate probe.
+#include <atomic>
 #include <cstdarg>
 #include <cstring>
 #include <mutex>
@@ -49,6 +50,38 @@ int device_props(const DeviceProps** out) {
     *out = &p;
     return SB_OK;
 }
+
+namespace {
+std::once_flag g_status_once;
+int* g_status = nullptr;  // host address == device address (unified addressing)
+cudaError_t g_status_error = cudaSuccess;
+std::atomic<int> g_wait_polls{kDefaultWaitPolls};
+}  // namespace
+
+int status_word(int** device_ptr) {
+    std::call_once(g_status_once, [] {
+        void* p = nullptr;
+        g_status_error = cudaHostAlloc(&p, sizeof(int), cudaHostAllocMapped | cudaHostAllocPortable);
+        if (g_status_error == cudaSuccess) {
+            g_status = static_cast<int*>(p);
+            __atomic_store_n(g_status, 0, __ATOMIC_RELEASE);
+        }
+    });
+    if (!g_status)
+        return fail(SB_ERR_CUDA, "cudaHostAlloc of the wait-status word failed: %s",
+                    cudaGetErrorString(g_status_error));
+    *device_ptr = g_status;
+    return SB_OK;
+}
+
+int take_wait_status() {
+    if (!g_status || !__atomic_exchange_n(g_status, 0, __ATOMIC_ACQ_REL)) return SB_OK;
+    return fail(SB_ERR_TIMEOUT,
+                "a thread block of an earlier launch gave up waiting for its tensor copies: that launch's "
+                "output is incomplete");
+}
+
+int wait_polls() { return g_wait_polls.load(std::memory_order_relaxed); }
 
 int check_domain(int64_t ni, int64_t nj, int64_t nk, int64_t si, int64_t sj, int64_t sk) {
     SB_CHECK(ni >= 0 && nj >= 0 && nk >= 0, SB_ERR_INVALID,
@@ -182,6 +215,12 @@ int sb_set_device(int device) {
     return SB_OK;
 }
 
+int sb_get_device(int* device) {
+    SB_CHECK(device, SB_ERR_INVALID, "device is NULL");
+    SB_CUDA(cudaGetDevice(device));
+    return SB_OK;
+}
+
 int sb_device_info(int device, char* name, int name_len, int* sm_count, int* cc_major,
                    int* cc_minor, size_t* total_mem, int* l2_bytes, int* smem_optin) {
     cudaDeviceProp prop;
@@ -201,6 +240,14 @@ int sb_device_info(int device, char* name, int name_len, int* sm_count, int* cc_
 
 int sb_synchronize(void) {
     SB_CUDA(cudaDeviceSynchronize());
+    return take_wait_status();
+}
+
+int sb_kernel_status(void) { return take_wait_status(); }
+
+int sb_debug_wait_limit(int polls) {
+    SB_CHECK(polls >= -1, SB_ERR_INVALID, "polls must be >= -1");
+    g_wait_polls.store(polls < 0 ? kDefaultWaitPolls : polls, std::memory_order_relaxed);
     return SB_OK;
 }
 
@@ -283,7 +330,7 @@ int sb_stream_destroy(void* stream) {
 
 int sb_stream_synchronize(void* stream) {
     SB_CUDA(cudaStreamSynchronize((cudaStream_t)stream));
-    return SB_OK;
+    return take_wait_status();
 }
 
 int sb_event_create(void** event) {
@@ -306,7 +353,7 @@ int sb_event_record(void* event, void* stream) {
 
 int sb_event_synchronize(void* event) {
     SB_CUDA(cudaEventSynchronize((cudaEvent_t)event));
-    return SB_OK;
+    return take_wait_status();
 }
 
 int sb_event_elapsed(void* start, void* stop, double* seconds) {

@@ -100,3 +100,28 @@ def download_output(req):
     f.download(host)
     hi, hj, hk = f.halo
     return host[hi:hi + req.ni, hj:hj + req.nj, hk:hk + req.nk]
+
+
+def expected_output_c(req):
+    """``expected_output`` computed by the C oracle (OpenMP; same bits as the
+    numpy oracle, which its golden tests pin), for large requests."""
+    from oracle import cport
+
+    fields, halo = request_inputs(req)
+    compute = np.float64 if req.storage == "float64" else np.float32
+    if req.storage == "bfloat16":
+        fields = {n: ora.bf16_bits_to_f32(a.ravel(order="F")).reshape(a.shape, order="F")
+                  for n, a in fields.items()}
+    fields = {n: np.asfortranarray(a, dtype=compute) for n, a in fields.items()}
+    domain = (req.ni, req.nj, req.nk)
+    first = next(iter(fields.values()))
+    out = np.zeros(first.shape, dtype=compute, order="F")
+    if req.op == "hdiff":
+        cport.hdiff(fields["inp"], fields["coeff"], out, domain, halo)
+    else:
+        cport.vadv(fields["stage"], fields["pos"], fields["tens"], fields["tensstage"], fields["wcon"], domain, halo,
+                   (1, 0), out=out)
+    res = out[tuple(slice(h, h + n) for h, n in zip(halo, domain))]
+    if req.storage == "bfloat16":
+        return ora.f32_to_bf16_bits(np.ascontiguousarray(res, dtype=np.float32)).reshape(res.shape)
+    return np.asarray(res).astype(req.storage)

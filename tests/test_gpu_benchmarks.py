@@ -122,7 +122,13 @@ def test_fast_forms_parameter_checks(lib):
 
 
 def test_vadv_fp32_storage_with_fp64_solve(lib):
-    b = vertical_advection.SharedMem(domain=(64, 40, 30), halo=(1, 1, 0), dtype="float32", compute_dtype="float64")
+    """float32 storage with float64 arithmetic: bit for bit against the oracle
+    run in float64 on the stored values.  The reference's check recomputes in
+    float32 and, in the ill-conditioned columns U[0, 1) fields produce, its
+    own float32 error exceeds its tolerance, so verify=False here."""
+    b = vertical_advection.SharedMem(domain=(64, 40, 30), halo=(1, 1, 0), dtype="float32", compute_dtype="float64",
+                                     verify=False)
+    run_checked(b)
     run_checked(b)
 
 

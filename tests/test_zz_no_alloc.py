@@ -7,7 +7,9 @@ cause.  sb_vadv_noalloc keeps the elimination factors in a fixed array inside
 the library instead of caller-provided scratch.  These tests call it through
 the C ABI and check that two calls in a row give exactly what the regular
 entry point sb_vadv gives (bit-identical, the tolerance of every fp64 and
-fp32 parity test here).  The file is named so that pytest collects it last.
+fp32 parity test here), and exactly what the oracle computes in the compute
+type on the stored inputs, rounded once to storage.  The file is named so
+that pytest collects it last.
 """
 
 from __future__ import annotations
@@ -17,16 +19,19 @@ import ctypes
 import numpy as np
 import pytest
 
+from oracle import stencils as ora
 from stencil_benchmarks_gb300 import _native, kernels
 from tests.gpu_helpers import (
     VADV_ARGS,
     VADV_DISTS,
     bits_equal,
+    compute_view,
     download_like,
     host_field,
     interior,
     mismatch_report,
     rng_fields,
+    round_to_storage,
     to_device,
 )
 
@@ -54,7 +59,8 @@ def _noalloc(dev, domain, storage, compute, shift=(1, 0)):
         raise _native.SbError("sb_vadv_noalloc", rc, _native.last_error())
 
 
-@pytest.mark.parametrize("storage,compute", [("float64", "float64"), ("float32", "float32"), ("float32", "float64")])
+@pytest.mark.parametrize("storage,compute", [("float64", "float64"), ("float32", "float32"), ("float32", "float64"),
+                                             ("bfloat16", "float32")])
 def test_noalloc_matches_regular_entry_point_twice(storage, compute, lib):
     # two calls in a row on different problems: the second must not see
     # anything the first left in the shared scratch array
@@ -68,6 +74,10 @@ def test_noalloc_matches_regular_entry_point_twice(storage, compute, lib):
                      out=dev["utensstage"], compute=compute)
         want = interior(download_like(dev["utensstage"], hosts["utensstage"]), domain, halo)
         assert bits_equal(got, want), f"call {call}: " + mismatch_report(got, want)
+        oracle = ora._vadv_component(*(compute_view(hosts[n], storage, compute) for n in VADV_ARGS),
+                                     domain, halo, *shift)
+        want = round_to_storage(oracle, storage)
+        assert bits_equal(got, want), f"call {call} vs the oracle: " + mismatch_report(got, want)
 
 
 def test_noalloc_rejects_columns_taller_than_its_scratch(lib):
