@@ -16,7 +16,9 @@ Printed JSON line (rank 0):
   roofline     the dominant kernel's compulsory HBM bytes per launch / its
                average CUDA-event duration, against the measured copy peak
   cpu_baseline the C restatement of the reference arithmetic (OpenMP, all
-               host cores) on the same workload
+               host cores) on the same workload; `reference_backends` beside
+               it times the reference's own OpenMP hdiff/vadv classes and its
+               numpy hdiff through its Benchmark API
   stream_triad STREAM triad on 2^29 fp64 (the bandwidth calibration kernel)
   fast_f64     the same step with fixed-point hdiff and float-pair vadv
                (within the stated tolerances, not bit-identical), with its
@@ -54,13 +56,17 @@ POINTS = NI * NJ * NK
 TRIAD_N = 1 << 29
 METRIC = "hdiff+vadv GPoints/s (fp64, 512x512x80)"
 UNIT = "GPoints/s"
+# the workload, identical in both arms' lines
+CONFIG = {"workload": "hdiff+vadv fp64 512x512x80 (halo 2,2,0 / 1,1,0)",
+          "l2": "inputs > L2 (1.35 GB of fields per step), no flush"}
 
 
 # fp64 vadv on GB300 is bound by the fp64 pipe; the SLAB variant (persistent
-# threads, factors in compact L2-resident slabs of the ccol/dcol scratch
-# fields) keeps the most columns in flight and is the fastest exact form
-# (1.33 ms vs 1.37 ms GLOBAL and 1.49 ms SMEM at 512x512x80).
-VADV_TUNE = {"variant": 3, "block_x": 32, "unroll": 4, "k_per_cta": 8}
+# threads, factors in compact slabs of the ccol/dcol scratch fields) keeps the
+# most columns in flight and is the fastest exact form.  Its nine products per
+# level run as integer arithmetic (bit-identical), which needs 24 blocks per SM
+# to hide the longer integer sequences: 980 us against 1175 us all-fp64.
+VADV_TUNE = {"variant": 3, "block_x": 32, "unroll": 4, "k_per_cta": 24}
 
 # The fast float64 step: hdiff with exact 64-bit fixed-point sums and one
 # float64 FMA per point (float64 rounding level), vadv in float-pair
@@ -172,6 +178,32 @@ class ClockSampler:
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax),
                 "power_w_max": max(power) if power else None, "samples": len(sm),
                 "reasons": sorted(reasons)}
+
+
+class GpuUtilSampler(ClockSampler):
+    """Mean nvidia-smi utilization.gpu (percent of time a kernel was running)
+    over a window."""
+
+    QUERY = "index,utilization.gpu"
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        vals = []
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            try:
+                vals.append(float(parts[1]))
+            except (IndexError, ValueError):
+                continue
+        return statistics.mean(vals) if vals else None
 
 
 # ---------------------------------------------------------------------------
@@ -551,23 +583,80 @@ def verify_batched(specs, built, storage):
     return results
 
 
-def run_served(n_requests=2000, rates=(1000.0, 5000.0, 20000.0), seed=11, float64_compute="float64"):
-    """Continuous-batching server under Poisson arrivals (mixed hdiff/vadv,
-    sizes log-uniform 32..1024, nk 40..137, fp64/fp32/bf16 at 20/60/20 %,
-    150 GB budget).  The full 10,000-request sweep is
-    ``python -m stencil_benchmarks_gb300.serving``."""
+SERVE_RATES = (1000.0, 5000.0, 10000.0, 20000.0, 50000.0)
+
+
+def run_served(n_requests=10000, rates=SERVE_RATES, seed=11, float64_compute="float64", mode="batched"):
+    """The serving workload: n_requests requests (hdiff / vadv 50/50, ni, nj
+    log-uniform in [32, 1024] rounded to 32, nk in [40, 137], fp64 / fp32 /
+    bf16-storage at 20/60/20 %, 150 GB budget) at each Poisson arrival rate;
+    "batched" packs queued requests into graph replays of the persistent
+    kernels, "plain" launches one kernel per request (same admission, slots
+    and streams)."""
     from stencil_benchmarks_gb300 import serving
 
-    server = serving.Server(budget_bytes=150e9, max_batch=64, slots_per_form=3, float64_compute=float64_compute)
+    server = serving.Server(budget_bytes=150e9, max_batch=64, slots_per_form=3, float64_compute=float64_compute,
+                            mode=mode)
     # warm-up: enough requests that every slot of every form has launched (and
     # captured its graph) before the measured rates
     serving.run_load(server, serving.request_specs(1024, seed=seed + 1000), rate=1e6)
     out = []
     for rate in rates:
+        util = GpuUtilSampler()
+        util.start()
         stats = serving.run_load(server, serving.request_specs(n_requests, seed=seed), rate=rate)
-        out.append({k: stats[k] for k in ("rate_offered", "requests", "p50_ms", "p99_ms", "mean_ms",
-                                          "throughput_req_s", "gpoints_s", "peak_pool_gb", "max_waiting")})
+        stats["gpu_util_pct"] = util.stop()
+        out.append(stats)
+    del server
     return out
+
+
+def served_precision_errors(n=12, seed=97):
+    """Max |err| / max |exact| and the pointwise p99 relative error of served
+    requests of each precision against the exact float64 computation of the
+    same stored inputs (the library's float64 kernels, bit-identical to the
+    reference's numpy), on a sample of n requests per precision."""
+    from stencil_benchmarks_gb300 import kernels, serving
+    from stencil_benchmarks_gb300 import array as sbarray
+    from stencil_benchmarks_gb300.device import Field
+
+    reqs = [r for r in serving.request_specs(8 * n, seed=seed, sizes=(32, 512))]
+    picked = []
+    for form in serving.FORMS:
+        picked += [r for r in reqs if r.storage == form][:n]
+    server = serving.Server(budget_bytes=40e9, max_batch=16, slots_per_form=2, keep_outputs=True, keep_inputs=True)
+    for r in picked:
+        server.submit(r)
+    server.drain()
+    errors = {}
+    for form in serving.FORMS:
+        worst, p99s = 0.0, []
+        for r in (q for q in picked if q.storage == form):
+            host = {}
+            for name, f in r.fields.items():
+                a = np.empty(f.shape, dtype=sbarray.storage_numpy_dtype(form), order="F")
+                f.download(a)
+                host[name] = (a.astype(np.uint32) << 16).view(np.float32) if form == "bfloat16" else a
+            wide = {name: np.asfortranarray(a, dtype=np.float64) for name, a in host.items()}
+            dev = {name: Field.like_host(a, "float64", r.fields["out"].halo) for name, a in wide.items()}
+            for name, a in wide.items():
+                dev[name].upload(a)
+            if r.op == "hdiff":
+                kernels.hdiff(dev["inp"], dev["coeff"], dev["out"])
+            else:
+                kernels.vadv(dev["stage"], dev["pos"], dev["tens"], dev["tensstage"], dev["wcon"], out=dev["out"])
+            exact = np.empty_like(wide["out"])
+            dev["out"].download(exact)
+            hi, hj, hk = r.fields["out"].halo
+            sl = (slice(hi, hi + r.ni), slice(hj, hj + r.nj), slice(hk, hk + r.nk))
+            got, want = np.asarray(wide["out"][sl], np.float64), exact[sl]
+            scale = float(np.max(np.abs(want))) or 1.0
+            worst = max(worst, float(np.max(np.abs(got - want))) / scale)
+            big = np.abs(want) >= 1e-2 * np.sqrt(np.mean(want * want))
+            p99s.append(float(np.percentile(np.abs(got - want)[big] / np.abs(want)[big], 99)))
+            server.release(r)
+        errors[form] = {"requests": n, "max_abs_over_scale": worst, "p99_pointwise_rel": max(p99s) if p99s else 0.0}
+    return errors
 
 
 def cpu_baseline_sample(threads=None):
@@ -594,13 +683,132 @@ def cpu_baseline_sample(threads=None):
     }
 
 
+# The reference's own CPU backends (stencils/openmp/horizontal_diffusion.py:50-138,
+# stencils/openmp/vertical_advection.py:53-82, stencils/numpy/horizontal_diffusion.py:39-56),
+# run through its own Benchmark classes: each renders its C++ template and
+# compiles it with g++ -fopenmp -Ofast -march=native at setup.
+REF_HDIFF = ("Rolling", "OnTheFlyVec", "OnTheFly")
+REF_VADV = ("KInnermostVec", "KInnermost")
+
+
+def reference_instances(hd, va):
+    """Construct the reference's OpenMP hdiff and vadv benchmarks on the bench's
+    seeded inputs: {"hdiff": {name: instance}, "vadv": {...}}; raises if the
+    reference cannot be loaded or its code does not compile here."""
+    from stencil_benchmarks_gb300 import host
+
+    host.load()
+    from stencil_benchmarks.benchmarks_collection.stencils.openmp import horizontal_diffusion as ref_hd
+    from stencil_benchmarks.benchmarks_collection.stencils.openmp import vertical_advection as ref_va
+
+    out = {"hdiff": {}, "vadv": {}}
+    for name in REF_HDIFF:
+        b = getattr(ref_hd, name)(domain=(NI, NJ, NK), halo=HDIFF_HALO, dtype="float64", verify=False)
+        for f in ("inp", "coeff"):
+            getattr(b._data[0], f)[...] = hd[f]
+        out["hdiff"][name] = b
+    for name in REF_VADV:
+        b = getattr(ref_va, name)(domain=(NI, NJ, NK), halo=VADV_HALO, dtype="float64", verify=False)
+        for f in ("ustage", "upos", "utens", "utensstage", "wcon"):
+            getattr(b._data[0], f)[...] = va[f]
+        out["vadv"][name] = b
+    return out
+
+
+def reference_backends(runs=3):
+    """Median kernel time (the reference's own timer) of each reference CPU
+    backend on the bench's step, and the numpy single-thread hdiff."""
+    hd, va = make_inputs(seed=7)
+    result = {"threads": int(os.environ.get("OMP_NUM_THREADS", os.cpu_count())), "cpu": _cpu_model()}
+    try:
+        inst = reference_instances(hd, va)
+    except Exception as err:  # noqa: BLE001 - reported, the port still runs
+        result["unavailable"] = f"{type(err).__name__}: {err}"[:300]
+        return result
+    for kind, group in inst.items():
+        for name, b in group.items():
+            b.run()
+            result[f"openmp_{kind}_{name}_ms"] = 1e3 * statistics.median(b.run()["time"] for _ in range(runs))
+    for kind in ("hdiff", "vadv"):
+        best = min(inst[kind], key=lambda n: result[f"openmp_{kind}_{n}_ms"])
+        result[f"best_{kind}"] = best
+    step = result[f"openmp_hdiff_{result['best_hdiff']}_ms"] + result[f"openmp_vadv_{result['best_vadv']}_ms"]
+    result["openmp_step_ms"] = step
+    result["openmp_value"] = 2 * POINTS / (step * 1e-3) / 1e9
+    from stencil_benchmarks.benchmarks_collection.stencils.numpy import horizontal_diffusion as np_hd
+
+    b = np_hd.OnTheFly(domain=(NI, NJ, NK), halo=HDIFF_HALO, dtype="float64", verify=False)
+    b._data[0].inp[...] = hd["inp"]
+    b._data[0].coeff[...] = hd["coeff"]
+    result["numpy_hdiff_OnTheFly_ms"] = 1e3 * b.run()["time"]
+    return result
+
+
+def _cpu_model():
+    try:
+        for line in open("/proc/cpuinfo"):
+            if line.lower().startswith(("model name", "cpu model")):
+                return line.split(":", 1)[1].strip()
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name"):
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    return "unknown"
+
+
 def run_reference(args, dist):
-    """--impl reference: the reference arithmetic on the host cores (C port)."""
+    """--impl reference: the reference's own OpenMP backends (best hdiff + best
+    vadv) on the host cores, each step timed by the reference's own timer;
+    the C port if the reference cannot be loaded or compiled here."""
     if dist.rank != 0:
         return 0
+    os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count()))
+    hd, va = make_inputs(seed=7)
+    try:
+        inst = reference_instances(hd, va)
+    except Exception as err:  # noqa: BLE001
+        print(f"reference backends unavailable ({type(err).__name__}: {err}); timing the C port", file=sys.stderr)
+        return run_reference_port(args, hd, va, dist)
+    best = {}
+    for kind, group in inst.items():
+        timings = {}
+        for name, b in group.items():
+            for _ in range(max(1, args.warmup)):
+                b.run()
+            timings[name] = statistics.median(b.run()["time"] for _ in range(3))
+        best[kind] = min(timings, key=timings.get)
+    h, v = inst["hdiff"][best["hdiff"]], inst["vadv"][best["vadv"]]
+    step_times = []
+    for _ in range(args.steps):
+        step_times.append(h.run()["time"] + v.run()["time"])
+    elapsed = sum(step_times)
+    value = 2 * POINTS * args.steps / elapsed / 1e9
+    threads = int(os.environ["OMP_NUM_THREADS"])
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": elapsed / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded PCG64, workload distributions)",
+        "config": dict(CONFIG),
+        "cpu_baseline": {
+            "value": value, "unit": UNIT, "cores": threads, "kind": "reference",
+            "sample": f"every step is the full 512x512x80 fp64 step: the reference's OpenMP "
+                      f"horizontal_diffusion.{best['hdiff']} + vertical_advection.{best['vadv']} (fastest of "
+                      f"{'/'.join(REF_HDIFF)} and {'/'.join(REF_VADV)}), run through the reference's own Benchmark "
+                      f"classes and timers, {threads} threads on {os.cpu_count()} host cores ({_cpu_model()})",
+        },
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_reference_port(args, hd, va, dist):
+    """The C restatement of the reference arithmetic on the host cores."""
     from oracle import cport
 
-    hd, va = make_inputs(seed=7)
     n_threads = cport.max_threads()
     for _ in range(args.warmup):
         cport.hdiff(hd["inp"], hd["coeff"], hd["out"], (NI, NJ, NK), HDIFF_HALO)
@@ -618,7 +826,7 @@ def run_reference(args, dist):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": elapsed / args.steps * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded PCG64, workload distributions)",
-        "config": {"workload": "hdiff+vadv fp64 512x512x80 (halo 2,2,0 / 1,1,0)", "l2": "inputs > L2"},
+        "config": dict(CONFIG),
         "cpu_baseline": {
             "value": value, "unit": UNIT, "cores": n_threads, "kind": "port",
             "sample": "every step is the full 512x512x80 hdiff+vadv fp64 step on the host cores "
@@ -665,9 +873,8 @@ def main(argv=None):
             "warmup": args.warmup, "ms_per_step": res["elapsed"] / args.steps * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded PCG64, workload distributions)",
-            "config": {"workload": "hdiff+vadv fp64 512x512x80 (halo 2,2,0 / 1,1,0)",
-                       "l2": "inputs > L2 (1.35 GB of fields per step), no flush",
-                       "device": res["info"]["name"], "sm_count": res["info"]["sm_count"]},
+            "config": dict(CONFIG),
+            "device": {"name": res["info"]["name"], "sm_count": res["info"]["sm_count"]},
             "gpu_launches": res["gpu_launches"],
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": res["h2d"],
                     "d2h_bytes_per_step": res["d2h"], "steps": res["e2e_steps"],
@@ -721,7 +928,19 @@ def main(argv=None):
         # serving first: its latencies are measured in a process that has not
         # yet created and torn down the autotuner's many batch objects
         if not args.no_served:
-            line["served"] = run_served()
+            batched = run_served()
+            plain = run_served(mode="plain")
+            sat_b = max(r["throughput_req_s"] for r in batched)
+            sat_p = max(r["throughput_req_s"] for r in plain)
+            line["served"] = {
+                "workload": "10,000 requests per rate, Poisson arrivals; hdiff/vadv 50/50, ni,nj log-uniform in "
+                            "[32,1024] rounded to 32, nk in [40,137], fp64/fp32/bf16-storage 20/60/20 %, 150 GB "
+                            "budget, fields generated on the device",
+                "batched": batched, "plain": plain,
+                "saturation_req_s": {"batched": sat_b, "plain": sat_p, "ratio": sat_b / sat_p},
+                "p99_ms_at_5k": {"batched": batched[1]["p99_ms"], "plain": plain[1]["p99_ms"]},
+                "error_vs_exact_fp64": served_precision_errors(),
+            }
             line["served_fast_f64"] = {
                 "what": "float64 requests with fixed-point hdiff and float-pair vadv (within 1e-12 / 1e-10 of "
                         "the field scale); float32 and bfloat16 requests unchanged",
@@ -730,6 +949,7 @@ def main(argv=None):
             line["batched"] = run_batched()
         if not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline_sample()
+            line["cpu_baseline"]["reference_backends"] = reference_backends()
         print(json.dumps(line), flush=True)
         return 0
     finally:

@@ -112,7 +112,12 @@ typedef struct sb_tune {
     int32_t tile_y;    /* hdiff: rows of j per CTA                              */
     int32_t k_per_cta; /* hdiff: k-planes per CTA                               */
     int32_t unroll;    /* STREAM: vectors per thread per iteration             */
-    int32_t flags;     /* STREAM: bit0 streaming (evict-first) stores          */
+    int32_t flags;     /* STREAM: bit0 streaming (evict-first) stores;
+                        * float64 hdiff TMA / vadv SLAB: bits 4-7 pick which
+                        * operations run as integer arithmetic instead of fp64
+                        * instructions (same bits either way; 0: the library's
+                        * default split, 1: all on the fp64 pipe, 2-8: other
+                        * splits)                                               */
     int32_t reserved;
 } sb_tune;
 
@@ -341,7 +346,12 @@ int sb_vadv_noalloc(int storage, int compute, const void* stage, const void* pos
 /* Throughput of dependent-free arithmetic on this device, in operations per
  * second (kind 0: f64 add, 1: f64 fma, 2: f32 fma, 3: f64->f32 conversion,
  * 4: f32->f64 conversion, 5: 32-bit integer shift/xor/multiply, 6: u32->f32
- * conversion, 7: s32->f32 conversion). */
+ * conversion, 7: s32->f32 conversion, 8: f64 add and 9: f64 multiply in
+ * integer arithmetic, bit-identical to the fp64 instructions; 10: f64 adds
+ * with independent 32-bit integer work beside them, 48 integer operations per
+ * add, counted as adds; 11: that integer work alone, counted the same way --
+ * 10 runs at the rate of 0 if the two pipes overlap, and at
+ * 1 / (1/rate(0) + 1/rate(11)) if they do not). */
 int sb_probe_arith_rate(int kind, double* ops_per_s);
 
 #ifdef __cplusplus

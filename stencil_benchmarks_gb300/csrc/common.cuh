@@ -9,8 +9,11 @@
 #include <cstdint>
 #include <cstdio>
 
+#include <type_traits>
+
 #include "../../include/sbgb300.h"
 #include "f32x2.cuh"
+#include "softf64.cuh"
 
 namespace sb {
 
@@ -226,6 +229,66 @@ struct Ar<double> {
     static __device__ __forceinline__ double neg_diff(double x, double a, double b) {
         if ((__double_as_longlong(x) << 1) == 0) return fp64_sub_cold(b, a);
         return -x;
+    }
+};
+
+// ---------------------------------------------------------------------------
+// binary64 operations on the integer pipe (softf64.cuh): bit-identical to the
+// fp64 instructions; the cases the integer path declines (NaN/inf operands,
+// subnormal or overflowing results) take the fp64 instruction out of line.
+// ---------------------------------------------------------------------------
+static __device__ __noinline__ double fp64_add_cold(double a, double b) { return __dadd_rn(a, b); }
+
+__device__ __forceinline__ double iadd(double a, double b) {
+    uint64_t r;
+    if (sf::add(sf::bits(a), sf::bits(b), r)) return sf::from_bits(r);
+    return fp64_add_cold(a, b);
+}
+__device__ __forceinline__ double isub(double a, double b) {
+    uint64_t r;
+    if (sf::sub(sf::bits(a), sf::bits(b), r)) return sf::from_bits(r);
+    return fp64_sub_cold(a, b);
+}
+__device__ __forceinline__ double imul(double a, double b) {
+    uint64_t r;
+    if (sf::mul(sf::bits(a), sf::bits(b), r)) return sf::from_bits(r);
+    return fp64_mul_cold(a, b);
+}
+
+// Arithmetic with a per-site choice of pipe.  A kernel numbers its operation
+// sites (site<K>); for float64 compute, bit K of the placement mask PL sends
+// site K to the integer pipe (iadd / isub / imul), the others use the fp64
+// instructions.  The results are the same bits either way; only the balance
+// between the two pipes changes.  Other compute types ignore the mask.
+template <int K>
+using site = std::integral_constant<int, K>;
+
+template <class C, uint32_t PL>
+struct Mix {
+    template <int K>
+    static __device__ __forceinline__ C add(C a, C b, site<K>) { return Ar<C>::add(a, b); }
+    template <int K>
+    static __device__ __forceinline__ C sub(C a, C b, site<K>) { return Ar<C>::sub(a, b); }
+    template <int K>
+    static __device__ __forceinline__ C mul(C a, C b, site<K>) { return Ar<C>::mul(a, b); }
+};
+
+template <uint32_t PL>
+struct Mix<double, PL> {
+    template <int K>
+    static __device__ __forceinline__ double add(double a, double b, site<K>) {
+        if constexpr (((PL >> K) & 1u) != 0u) return iadd(a, b);
+        else return __dadd_rn(a, b);
+    }
+    template <int K>
+    static __device__ __forceinline__ double sub(double a, double b, site<K>) {
+        if constexpr (((PL >> K) & 1u) != 0u) return isub(a, b);
+        else return __dsub_rn(a, b);
+    }
+    template <int K>
+    static __device__ __forceinline__ double mul(double a, double b, site<K>) {
+        if constexpr (((PL >> K) & 1u) != 0u) return imul(a, b);
+        else return __dmul_rn(a, b);
     }
 };
 

@@ -317,12 +317,13 @@ struct TmaSmem {
     }
 };
 
-template <class S, class C, int TX, int NTY>
+template <class S, class C, int TX, int NTY, uint32_t PL>
 __global__ void __launch_bounds__(TX* NTY)
     hdiff_tma_kernel(const __grid_constant__ CUtensorMap tmap, const S* __restrict__ coeff, S* __restrict__ out,
                      int ni, int nj, int nk, int64_t sj, int64_t sk, int TY, int kper, int off, int polls,
                      int* status) {
     using A = Ar<C>;
+    using X = Mix<C, PL>;  // sites 0-10 below
     using M = TmaSmem<S, C>;
     using T = typename std::conditional<M::CONV, C, S>::type;  // element type the stencil reads
     constexpr int BX = TX + M::PADX, WL = TX + 2, WF = TX + 1, WY = TX;
@@ -387,9 +388,10 @@ __global__ void __launch_bounds__(TX* NTY)
         for (int jj = ty; jj < TY + 2; jj += NTY) {
             for (int ii = tx; ii < WL; ii += TX) {
                 const T* c = s_in + (jj + 1) * BX + ii + 1;
-                const C sum = A::add(A::add(A::add(cvt<C, T>(c[1]), cvt<C, T>(c[-1])), cvt<C, T>(c[BX])),
-                                     cvt<C, T>(c[-BX]));
-                s_lap[jj * WL + ii] = A::sub(A::template scale2<2>(cvt<C, T>(c[0])), sum);
+                const C sum = X::add(X::add(X::add(cvt<C, T>(c[1]), cvt<C, T>(c[-1]), site<0>{}), cvt<C, T>(c[BX]),
+                                            site<1>{}),
+                                     cvt<C, T>(c[-BX]), site<2>{});
+                s_lap[jj * WL + ii] = X::sub(A::template scale2<2>(cvt<C, T>(c[0])), sum, site<3>{});
             }
         }
         if constexpr (M::CONV) {
@@ -403,14 +405,14 @@ __global__ void __launch_bounds__(TX* NTY)
             for (int ii = tx; ii < WF; ii += TX) {
                 const C* l = s_lap + (jj + 1) * WL + ii;
                 const T* x = s_in + (jj + 2) * BX + ii + 1;
-                s_flx[jj * WF + ii] = A::limit(A::sub(l[1], l[0]), cvt<C, T>(x[1]), cvt<C, T>(x[0]));
+                s_flx[jj * WF + ii] = A::limit(X::sub(l[1], l[0], site<4>{}), cvt<C, T>(x[1]), cvt<C, T>(x[0]));
             }
         }
         for (int jj = ty; jj < TY + 1; jj += NTY) {
             for (int ii = tx; ii < WY; ii += TX) {
                 const C* l = s_lap + jj * WL + ii + 1;
                 const T* x = s_in + (jj + 1) * BX + ii + 2;
-                s_fly[jj * WY + ii] = A::limit(A::sub(l[WL], l[0]), cvt<C, T>(x[BX]), cvt<C, T>(x[0]));
+                s_fly[jj * WY + ii] = A::limit(X::sub(l[WL], l[0], site<5>{}), cvt<C, T>(x[BX]), cvt<C, T>(x[0]));
             }
         }
         __syncthreads();
@@ -423,7 +425,8 @@ __global__ void __launch_bounds__(TX* NTY)
                 const C x = cvt<C, T>(s_in[(jj + 2) * BX + tx + 2]);
                 const int64_t o = (int64_t)k * sk + (int64_t)gi + (int64_t)gj * sj;
                 const C cf = ld<C, S>(coeff + o);
-                st<S, C>(out + o, A::sub(x, A::mul(cf, A::sub(A::add(A::sub(fx1, fx0), fy1), fy0))));
+                const C div = X::sub(X::add(X::sub(fx1, fx0, site<6>{}), fy1, site<7>{}), fy0, site<8>{});
+                st<S, C>(out + o, X::sub(x, X::mul(cf, div, site<9>{}), site<10>{}));
             }
         }
         __syncthreads();  // stage sidx and the lap/flux buffers are free again
@@ -459,7 +462,7 @@ CUtensorMapDataType tma_type() {
 // TMA launch if the layout qualifies (i unit-stride, j/k strides multiples
 // of 16 bytes, tile rows within the 256-row box limit); SB_ERR_UNSUPPORTED
 // (no error text) if not.
-template <class S, class C, int TX, int NTY>
+template <class S, class C, int TX, int NTY, uint32_t PL>
 int launch_tma(const void* inp, const void* coeff, void* out, int64_t ni, int64_t nj, int64_t nk, int64_t si,
                int64_t sj, int64_t sk, int ty, int kper, cudaStream_t stream, const DeviceProps* p) {
     constexpr int ES = (int)sizeof(S), PADX = TmaSmem<S, C>::PADX;
@@ -487,7 +490,7 @@ int launch_tma(const void* inp, const void* coeff, void* out, int64_t ni, int64_
     const size_t smem = TmaSmem<S, C>::bytes(TX, ty);
     SB_CHECK((int64_t)smem <= p->smem_optin, SB_ERR_INVALID, "hdiff TMA tile %dx%d needs %zu bytes of shared memory",
              TX, ty, smem);
-    auto kernel = hdiff_tma_kernel<S, C, TX, NTY>;
+    auto kernel = hdiff_tma_kernel<S, C, TX, NTY, PL>;
     if (smem > 48 * 1024) SB_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const int64_t gx = ceil_div(ni, TX), gy = ceil_div(nj, ty), gz = ceil_div(nk, kper);
     SB_CHECK(gy <= p->max_grid_y && gz <= p->max_grid_z, SB_ERR_INVALID, "hdiff grid too large");
@@ -500,6 +503,57 @@ int launch_tma(const void* inp, const void* coeff, void* out, int64_t ni, int64_
     return SB_OK;
 }
 
+// Integer-pipe placements of the float64 TMA tile's operation sites (bit K =
+// site K of hdiff_tma_kernel: 0-2 the Laplacian's neighbour sum, 3 its
+// 4*inp - sum, 4/5 the flux differences, 6-8 the flux divergence, 9 the
+// coefficient product, 10 the update).  sb_tune.flags bits 4-7 pick one:
+// 0 the default, 1 every site on the fp64 pipe, 2.. the mixes below; shapes
+// other than the 128 x 4 tile always use the default.
+constexpr uint32_t kTmaPlacements[] = {
+    0u,
+    0u,
+    1u << 9,
+    (1u << 9) | (1u << 6) | (1u << 7) | (1u << 8),
+    (1u << 9) | (1u << 6) | (1u << 7) | (1u << 8) | (1u << 10),
+    (1u << 9) | (1u << 0) | (1u << 1) | (1u << 2) | (1u << 3),
+    (1u << 9) | (1u << 0) | (1u << 1) | (1u << 6) | (1u << 7),
+    (1u << 9) | (1u << 0) | (1u << 1) | (1u << 2) | (1u << 6) | (1u << 7) | (1u << 8),
+    (1u << 9) | (1u << 0) | (1u << 1) | (1u << 2) | (1u << 3) | (1u << 6) | (1u << 7) | (1u << 8) | (1u << 10),
+};
+// Measured at 512x512x80 fp64: 561 us with every site on the fp64 pipe;
+// every mix above is slower (600-1269 us): the tile's phases are separated by
+// block barriers and each point's operations form one dependent chain, so the
+// long integer sequences do not overlap the fp64 work.  The default keeps
+// every site on the fp64 pipe.
+constexpr int kTmaPlacementDefault = 1;
+constexpr int kTmaPlacementCount = (int)(sizeof(kTmaPlacements) / sizeof(kTmaPlacements[0]));
+
+template <class S, class C, int TX, int NTY>
+int launch_tma_placed(int placement, const void* inp, const void* coeff, void* out, int64_t ni, int64_t nj,
+                      int64_t nk, int64_t si, int64_t sj, int64_t sk, int ty, int kper, cudaStream_t stream,
+                      const DeviceProps* p) {
+    SB_CHECK(placement >= 0 && placement < kTmaPlacementCount, SB_ERR_INVALID,
+             "hdiff TMA: placement preset %d out of range [0, %d)", placement, kTmaPlacementCount);
+    constexpr uint32_t kDefault = kTmaPlacements[kTmaPlacementDefault];
+    if constexpr (std::is_same<C, double>::value && TX == 128 && NTY == 4) {
+#define SB_TMA_PL(Q)                                                                                          \
+    if (placement == Q)                                                                                       \
+        return launch_tma<S, C, TX, NTY, kTmaPlacements[Q]>(inp, coeff, out, ni, nj, nk, si, sj, sk, ty, kper,   \
+                                                           stream, p);
+        SB_TMA_PL(1)
+        SB_TMA_PL(2)
+        SB_TMA_PL(3)
+        SB_TMA_PL(4)
+        SB_TMA_PL(5)
+        SB_TMA_PL(6)
+        SB_TMA_PL(7)
+        SB_TMA_PL(8)
+#undef SB_TMA_PL
+    }
+    return launch_tma<S, C, TX, NTY, std::is_same<C, double>::value ? kDefault : 0u>(
+        inp, coeff, out, ni, nj, nk, si, sj, sk, ty, kper, stream, p);
+}
+
 template <class S, class C>
 int launch_typed(const void* inp, const void* coeff, void* out, int64_t ni, int64_t nj, int64_t nk,
                  int64_t si, int64_t sj, int64_t sk, const sb_tune* tune, cudaStream_t stream) {
@@ -507,6 +561,7 @@ int launch_typed(const void* inp, const void* coeff, void* out, int64_t ni, int6
     int rc = device_props(&p);
     if (rc) return rc;
     int variant = tune ? tune->variant : SB_VARIANT_AUTO;
+    const int placement = tune ? (tune->flags >> 4) & 15 : 0;
     // fp64 compute is bound by the fp64 pipe: TILE computes every lap/flx/fly
     // once per tile (fewest fp64 operations); fp32 and float-pair compute are
     // bound by instruction issue: JSCAN (shuffles, no block barriers) is faster.
@@ -516,7 +571,8 @@ int launch_typed(const void* inp, const void* coeff, void* out, int64_t ni, int6
     const bool auto_tile = variant == SB_VARIANT_AUTO && std::is_same<C, double>::value;
     if constexpr (std::is_same<S, double>::value && std::is_same<C, double>::value) {
         if (variant == SB_VARIANT_AUTO) {
-            const int rc_tma = launch_tma<S, C, 128, 4>(inp, coeff, out, ni, nj, nk, si, sj, sk, 16, 2, stream, p);
+            const int rc_tma =
+                launch_tma_placed<S, C, 128, 4>(placement, inp, coeff, out, ni, nj, nk, si, sj, sk, 16, 2, stream, p);
             if (rc_tma != SB_ERR_UNSUPPORTED) return rc_tma;
         }
     }
@@ -554,7 +610,7 @@ int launch_typed(const void* inp, const void* coeff, void* out, int64_t ni, int6
             int rc2 = SB_ERR_UNSUPPORTED;
 #define SB_TMA_CASE(TXV, NTYV)                                                                               \
     if (bx == TXV && by == NTYV)                                                                              \
-        rc2 = launch_tma<S, C, TXV, NTYV>(inp, coeff, out, ni, nj, nk, si, sj, sk, ty, kper, stream, p);
+        rc2 = launch_tma_placed<S, C, TXV, NTYV>(placement, inp, coeff, out, ni, nj, nk, si, sj, sk, ty, kper, stream, p);
             SB_TMA_CASE(32, 8)
             SB_TMA_CASE(64, 4)
             SB_TMA_CASE(64, 8)

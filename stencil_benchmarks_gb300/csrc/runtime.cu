@@ -172,6 +172,40 @@ __global__ void arith_probe_kernel(double* out, int iters, double x) {
         float s = 0.f;
         for (int u = 0; u < 8; ++u) s += a[u];
         if (s == 12345.678f) out[0] = s;
+    } else if (KIND == 10 || KIND == 11) {  // f64 add chains beside 32-bit integer chains (10), or the integer chains alone (11)
+        double a[8];
+        unsigned b[8];
+        for (int u = 0; u < 8; ++u) {
+            a[u] = x + (double)(threadIdx.x + u);
+            b[u] = (unsigned)x + threadIdx.x + u;
+        }
+        const double c = 1e-3;
+        for (int it = 0; it < iters; ++it) {
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                if (KIND == 10) a[u] = __dadd_rn(a[u], c);
+#pragma unroll
+                for (int r = 0; r < 16; ++r) b[u] = (b[u] ^ (b[u] >> 15)) * 0x2C1B3C6Du;
+            }
+        }
+        double s = 0.0;
+        unsigned t = 0;
+        for (int u = 0; u < 8; ++u) {
+            s += a[u];
+            t += b[u];
+        }
+        if (s == 12345.678 || t == 12345u) out[0] = s;
+    } else if (KIND == 8 || KIND == 9) {  // binary64 add / mul on the integer pipe (softf64.cuh)
+        double a[8];
+        for (int u = 0; u < 8; ++u) a[u] = x + (double)(threadIdx.x + u);
+        const double m = 0.999, c = 1e-3;
+        for (int it = 0; it < iters; ++it) {
+#pragma unroll
+            for (int u = 0; u < 8; ++u) a[u] = KIND == 8 ? iadd(a[u], c) : imul(a[u], m);
+        }
+        double s = 0.0;
+        for (int u = 0; u < 8; ++u) s += a[u];
+        if (s == 12345.678) out[0] = s;
     } else {
         double a[8];
         for (int u = 0; u < 8; ++u) a[u] = x + (double)(threadIdx.x + u);
@@ -395,13 +429,14 @@ int sb_l2_flush(void* stream) {
 }
 
 int sb_probe_arith_rate(int kind, double* ops_per_s) {
-    SB_CHECK(kind >= 0 && kind <= 7 && ops_per_s, SB_ERR_INVALID, "bad probe arguments");
+    SB_CHECK(kind >= 0 && kind <= 11 && ops_per_s, SB_ERR_INVALID, "bad probe arguments");
     const DeviceProps* p;
     int rc = device_props(&p);
     if (rc) return rc;
     double* out = nullptr;
     SB_CUDA(cudaMalloc(&out, sizeof(double)));
-    const int blocks = p->sm_count * 8, threads = 256, iters = (kind == 2 || kind >= 5) ? 8192 : 512;
+    const int blocks = p->sm_count * 8, threads = 256,
+              iters = (kind == 2 || (kind >= 5 && kind <= 9)) ? 8192 : 512;
     auto launch = [&]() {
         if (kind == 0) arith_probe_kernel<0><<<blocks, threads>>>(out, iters, 0.5);
         if (kind == 1) arith_probe_kernel<1><<<blocks, threads>>>(out, iters, 0.5);
@@ -411,6 +446,10 @@ int sb_probe_arith_rate(int kind, double* ops_per_s) {
         if (kind == 5) arith_probe_kernel<5><<<blocks, threads>>>(out, iters, 0.5);
         if (kind == 6) arith_probe_kernel<6><<<blocks, threads>>>(out, iters, 0.5);
         if (kind == 7) arith_probe_kernel<7><<<blocks, threads>>>(out, iters, 0.5);
+        if (kind == 8) arith_probe_kernel<8><<<blocks, threads>>>(out, iters, 0.5);
+        if (kind == 9) arith_probe_kernel<9><<<blocks, threads>>>(out, iters, 0.5);
+        if (kind == 10) arith_probe_kernel<10><<<blocks, threads>>>(out, iters, 0.5);
+        if (kind == 11) arith_probe_kernel<11><<<blocks, threads>>>(out, iters, 0.5);
         return SB_OK;
     };
     double t = 0.0;

@@ -549,7 +549,8 @@ __device__ __forceinline__ C from_ring(T w, uint32_t sel) {
 //                 0 and 1 of a slot; needs ring entries of the compute size).
 // Every shared-memory address below is a per-thread base plus a
 // compile-time offset.
-template <class S, class C, int BT, int D, class IDX, bool SLAB = false, class P = C>
+// PL: integer-pipe placement mask over the operation sites 0-20 below (Mix).
+template <class S, class C, int BT, int D, class IDX, bool SLAB = false, class P = C, uint32_t PL = 0u>
 __device__ __forceinline__ void vadv_async_column(const S* __restrict__ stage, const S* __restrict__ pos,
                                                   const S* __restrict__ tens, const S* tensstage,
                                                   const S* __restrict__ wcon, S* out, IDX col, int nk, IDX sk,
@@ -557,6 +558,8 @@ __device__ __forceinline__ void vadv_async_column(const S* __restrict__ stage, c
                                                   int fs = 0) {
     using A = Ar<C>;
     using AP = Ar<P>;
+    using X = Mix<C, PL>;
+    using XP = Mix<P, PL>;
     using T = typename RingOf<S>::T;
     constexpr int R = D + 1;
     constexpr int B = sizeof(T);
@@ -615,17 +618,17 @@ __device__ __forceinline__ void vadv_async_column(const S* __restrict__ stage, c
             const C t0 = from_ring<C, S>(sl[4 * BT], sel_te ^ f), ts0 = from_ring<C, S>(sl[5 * BT], sel_ts ^ f);
             issue((u + D) % R, k + D);  // the slot of level k-1, already consumed
             const C as_ = A::template scale2<-1>(-gcv);
-            gcv = A::template scale2<-2>(A::add(w1, w0));
+            gcv = A::template scale2<-2>(X::add(w1, w0, site<0>{}));
             cs = A::template scale2<-1>(gcv);
             const C ddown = A::neg_diff(dup, scur, sprev);
-            dup = A::sub(snext, scur);
-            bcol = A::sub(A::sub(dtr, as_), cs);
-            corr = A::sub(A::mul(-as_, ddown), A::mul(cs, dup));
-            dv = A::add(A::add(A::add(A::mul(dtr, p0), t0), ts0), corr);
+            dup = X::sub(snext, scur, site<1>{});
+            bcol = X::sub(X::sub(dtr, as_, site<2>{}), cs, site<3>{});
+            corr = X::sub(X::mul(-as_, ddown, site<4>{}), X::mul(cs, dup, site<5>{}), site<6>{});
+            dv = X::add(X::add(X::add(X::mul(dtr, p0, site<7>{}), t0, site<8>{}), ts0, site<9>{}), corr, site<10>{});
             const P pas = to_p<P>(as_);
-            const P divided = AP::rcp(AP::sub(to_p<P>(bcol), AP::mul(cp, pas)));
-            cp = AP::mul(to_p<P>(cs), divided);
-            dp = AP::mul(AP::sub(to_p<P>(dv), AP::mul(dp, pas)), divided);
+            const P divided = AP::rcp(XP::sub(to_p<P>(bcol), XP::mul(cp, pas, site<11>{}), site<12>{}));
+            cp = XP::mul(to_p<P>(cs), divided, site<13>{});
+            dp = XP::mul(XP::sub(to_p<P>(dv), XP::mul(dp, pas, site<14>{}), site<15>{}), divided, site<16>{});
             sc[k * FS] = cp;
             sd[k * FS] = dp;
             sprev = scur;
@@ -681,8 +684,9 @@ __device__ __forceinline__ void vadv_async_column(const S* __restrict__ stage, c
                 dv_k = sd[k * BT];
             }
             issue_b((u + D) % R, k - D);
-            data = AP::sub(dv_k, AP::mul(cv, data));
-            st<S, C>(out + (col + (IDX)k * sk), A::mul(dtr, from_p<C>(AP::sub(data, to_p<P>(p0)))));
+            data = XP::sub(dv_k, XP::mul(cv, data, site<17>{}), site<18>{});
+            st<S, C>(out + (col + (IDX)k * sk),
+                     X::mul(dtr, from_p<C>(XP::sub(data, to_p<P>(p0), site<19>{})), site<20>{}));
         }
     }
     cp_async_wait<0>();

@@ -29,6 +29,7 @@
 //            same names), for columns too tall for shared memory.
 // The backward sweep reads them back in reverse order.
 #include <algorithm>
+#include <initializer_list>
 #include <type_traits>
 
 #include "stencil_core.cuh"
@@ -58,6 +59,44 @@ __global__ void __launch_bounds__(256)
         vadv_column<S, C, D>(stage, pos, tens, tensstage, wcon, out, col, nk, sk, wsh, fac);
     }
 }
+
+// Integer-pipe placements of float64 vadv's operation sites (bit K = site K
+// of vadv_async_column: 0 the wcon sum, 1 the stage difference, 2-3 bcol,
+// 4-6 the correction, 7-10 the right-hand side, 11-12 the pivot, 13 ccol,
+// 14-16 dcol, 17-18 the back substitution, 19-20 the output).  sb_tune.flags
+// bits 4-7 pick one for the SLAB form: 0 the default, 1 every site on the
+// fp64 pipe, 2.. the mixes below; SLAB shapes other than 32 threads x depth 4
+// and the SMEM-async form use the default.
+constexpr uint32_t vadv_sites(std::initializer_list<int> ks) {
+    uint32_t m = 0;
+    for (int k : ks) m |= 1u << k;
+    return m;
+}
+constexpr uint32_t kVadvMuls = vadv_sites({4, 5, 7, 11, 13, 14, 16, 17, 20});
+constexpr uint32_t kVadvPlacements[] = {
+    0u,
+    0u,
+    kVadvMuls,
+    vadv_sites({4, 5, 7, 14, 17, 20}),
+    vadv_sites({4, 5, 7, 14, 17, 20, 11}),
+    vadv_sites({4, 5, 7}),
+    vadv_sites({17, 20}),
+    vadv_sites({4, 5, 7, 11, 13, 14, 16}),
+    kVadvMuls | vadv_sites({0}),
+};
+// Measured at 512x512x80 (32-thread SLAB blocks, depth 4): every site on the
+// fp64 pipe 1171-1201 us whatever the blocks per SM; the nine products on the
+// integer pipe (preset 2) 980 us with 24 blocks per SM (1019 with 16, 1189
+// with 8: the integer sequences need more warps in flight); additions on the
+// integer pipe cost more than they save (a binary64 add in integer
+// arithmetic runs at 0.31 Tops/s against 0.52 for the fp64 instruction, a
+// multiply at 0.56).  The default SLAB form therefore runs the products on
+// the integer pipe with 24 blocks per SM.
+constexpr int kVadvPlacementDefault = 2;
+constexpr int kVadvSlabBlocksPerSm = 24;
+constexpr int kVadvPlacementCount = (int)(sizeof(kVadvPlacements) / sizeof(kVadvPlacements[0]));
+template <class C>
+constexpr uint32_t kVadvDefaultPlacement = std::is_same<C, double>::value ? kVadvPlacements[kVadvPlacementDefault] : 0u;
 
 // SMEM variant with asynchronous staging: the six
 // per-level inputs of the forward sweep (wcon at k+1 in both columns, stage
@@ -91,7 +130,7 @@ __global__ void __launch_bounds__(BT)
 // nslots * nk * 2 elements -- sized to stay in L2 -- rather than the whole
 // field.  Inputs and read-back factors are staged with cp.async
 // (vadv_async_column<..., SLAB = true>); the shared memory is the ring only.
-template <class S, class C, int BT, int D>
+template <class S, class C, int BT, int D, uint32_t PL>
 __global__ void __launch_bounds__(BT)
     vadv_slab_kernel(const S* __restrict__ stage, const S* __restrict__ pos, const S* __restrict__ tens,
                      const S* tensstage, const S* __restrict__ wcon, S* out, C* __restrict__ slab_c,
@@ -107,8 +146,8 @@ __global__ void __launch_bounds__(BT)
         const int i = (int)(g % gx) * BT + t;
         const int j = (int)(g / gx);
         if (i < ni) {
-            vadv_async_column<S, C, BT, D, int, true>(stage, pos, tens, tensstage, wcon, out, i * si + j * sj, nk, sk,
-                                                      wsh, slab_c + slot, slab_d + slot, ring, nslots);
+            vadv_async_column<S, C, BT, D, int, true, C, PL>(stage, pos, tens, tensstage, wcon, out, i * si + j * sj,
+                                                             nk, sk, wsh, slab_c + slot, slab_d + slot, ring, nslots);
         }
     }
 }
@@ -218,12 +257,12 @@ int launch_async(int bx, int by, int depth, const DeviceProps* p, cudaStream_t s
     }
 }
 
-template <class S, class C, int BT, int D>
+template <class S, class C, int BT, int D, uint32_t PL>
 int launch_slab_one(int blocks_per_sm, const DeviceProps* p, cudaStream_t stream, const void* stage,
                     const void* pos, const void* tens, const void* tensstage, const void* wcon, void* out,
                     void* ccol, void* dcol, int64_t ni, int64_t nj, int64_t nk, int64_t si, int64_t sj, int64_t sk,
                     int64_t wsh) {
-    auto kernel = vadv_slab_kernel<S, C, BT, D>;
+    auto kernel = vadv_slab_kernel<S, C, BT, D, PL>;
     const size_t smem = (size_t)(D + 1) * 6 * BT * sizeof(typename RingOf<S>::T);
     if (smem > 48 * 1024) SB_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int fit = 0;
@@ -231,6 +270,9 @@ int launch_slab_one(int blocks_per_sm, const DeviceProps* p, cudaStream_t stream
     int per_sm = std::max(1, fit);
     if (blocks_per_sm > 0) {
         per_sm = std::min(per_sm, blocks_per_sm);
+    } else if (PL != 0u) {
+        // integer-pipe products: more warps in flight beat an L2-resident slab
+        per_sm = std::min(per_sm, kVadvSlabBlocksPerSm);
     } else {
         // keep the factor slabs (2 * nk elements per thread) within half of L2
         const int64_t per_block = 2 * nk * (int64_t)sizeof(C) * BT * p->sm_count;
@@ -254,7 +296,7 @@ int launch_slab_one(int blocks_per_sm, const DeviceProps* p, cudaStream_t stream
 // compute size, positive strides, 32-bit offsets); SB_ERR_UNSUPPORTED (without
 // error text) otherwise.
 template <class S, class C>
-int launch_slab(int bx, int depth, int blocks_per_sm, const DeviceProps* p, cudaStream_t stream,
+int launch_slab(int bx, int depth, int blocks_per_sm, int placement, const DeviceProps* p, cudaStream_t stream,
                 const void* stage, const void* pos, const void* tens, const void* tensstage, const void* wcon,
                 void* out, void* ccol, void* dcol, int64_t ni, int64_t nj, int64_t nk, int64_t si, int64_t sj,
                 int64_t sk, int64_t wsh) {
@@ -264,10 +306,31 @@ int launch_slab(int bx, int depth, int blocks_per_sm, const DeviceProps* p, cuda
         if (!ccol || !dcol || si <= 0 || sj <= 0 || sk <= 0) return SB_ERR_UNSUPPORTED;
         const int64_t span = (ni + 1) * si + nj * sj + (nk + 1) * sk;
         if (span >= (1LL << 31) || (int64_t)ni * nj * nk >= (1LL << 31)) return SB_ERR_UNSUPPORTED;
-#define SB_VADV_SLAB_CASE(BTV, DV)                                                                              \
-    if (bx == BTV && depth == DV)                                                                               \
-        return launch_slab_one<S, C, BTV, DV>(blocks_per_sm, p, stream, stage, pos, tens, tensstage, wcon, out, \
-                                              ccol, dcol, ni, nj, nk, si, sj, sk, wsh);
+        SB_CHECK(placement >= 0 && placement < kVadvPlacementCount, SB_ERR_INVALID,
+                 "vadv SLAB: placement preset %d out of range [0, %d)", placement, kVadvPlacementCount);
+        if constexpr (std::is_same<C, double>::value) {
+            if (bx == 32 && depth == 4 && placement != 0) {
+#define SB_VADV_SLAB_PL(Q)                                                                                         \
+    if (placement == Q)                                                                                            \
+        return launch_slab_one<S, C, 32, 4, kVadvPlacements[Q]>(blocks_per_sm, p, stream, stage, pos, tens,        \
+                                                                tensstage, wcon, out, ccol, dcol, ni, nj, nk, si, \
+                                                                sj, sk, wsh);
+                SB_VADV_SLAB_PL(1)
+                SB_VADV_SLAB_PL(2)
+                SB_VADV_SLAB_PL(3)
+                SB_VADV_SLAB_PL(4)
+                SB_VADV_SLAB_PL(5)
+                SB_VADV_SLAB_PL(6)
+                SB_VADV_SLAB_PL(7)
+                SB_VADV_SLAB_PL(8)
+#undef SB_VADV_SLAB_PL
+            }
+        }
+#define SB_VADV_SLAB_CASE(BTV, DV)                                                                                 \
+    if (bx == BTV && depth == DV)                                                                                  \
+        return launch_slab_one<S, C, BTV, DV, kVadvDefaultPlacement<C>>(blocks_per_sm, p, stream, stage, pos,   \
+                                                                           tens, tensstage, wcon, out, ccol, dcol, \
+                                                                           ni, nj, nk, si, sj, sk, wsh);
         SB_VADV_SLAB_CASE(32, 2)
         SB_VADV_SLAB_CASE(32, 4)
         SB_VADV_SLAB_CASE(32, 8)
@@ -437,6 +500,7 @@ int launch_typed(const void* stage, const void* pos, const void* tens, const voi
     int rc = device_props(&p);
     if (rc) return rc;
     int variant = tune ? tune->variant : SB_VARIANT_AUTO;
+    const int placement = tune ? (tune->flags >> 4) & 15 : 0;
     int bx = (tune && tune->block_x > 0) ? tune->block_x : 32;
     int by = (tune && tune->block_y > 0) ? tune->block_y : 1;
     SB_CHECK(bx * by <= 256 && bx >= 1 && by >= 1, SB_ERR_INVALID, "vadv block (%d, %d) exceeds 256 threads", bx, by);
@@ -464,10 +528,11 @@ int launch_typed(const void* stage, const void* pos, const void* tens, const voi
                             ? launch_wslab<S, C>(32, 4, 0, p, stream, stage, pos, tens, tensstage, wcon, out, ccol,
                                                  dcol, ni, nj, nk, si, sj, sk, wsh)
                             : (std::is_same<C, double>::value
-                                   ? launch_slab<S, C>(32, 4, 8, p, stream, stage, pos, tens, tensstage, wcon, out,
-                                                       ccol, dcol, ni, nj, nk, si, sj, sk, wsh)
-                                   : launch_slab<S, C>(64, 2, 32, p, stream, stage, pos, tens, tensstage, wcon, out,
-                                                       ccol, dcol, ni, nj, nk, si, sj, sk, wsh));
+                                   ? launch_slab<S, C>(32, 4, kVadvSlabBlocksPerSm, placement, p, stream, stage, pos,
+                                                       tens, tensstage, wcon, out, ccol, dcol, ni, nj, nk, si, sj,
+                                                       sk, wsh)
+                                   : launch_slab<S, C>(64, 2, 32, placement, p, stream, stage, pos, tens, tensstage,
+                                                       wcon, out, ccol, dcol, ni, nj, nk, si, sj, sk, wsh));
         if (arc != SB_ERR_UNSUPPORTED) return arc;
     }
     if (variant == SB_VARIANT_AUTO) variant = ((int64_t)smem <= p->smem_optin) ? SB_VADV_SMEM : SB_VADV_GLOBAL;
@@ -499,8 +564,8 @@ int launch_typed(const void* stage, const void* pos, const void* tens, const voi
         SB_CHECK(ccol && dcol, SB_ERR_INVALID, "vadv SLAB variant needs ccol/dcol scratch fields");
         const int d = (tune && tune->unroll > 0) ? tune->unroll : 4;
         const int bpsm = tune ? tune->k_per_cta : 0;
-        const int rc2 = launch_slab<S, C>(bx, d, bpsm, p, stream, stage, pos, tens, tensstage, wcon, out, ccol, dcol,
-                                          ni, nj, nk, si, sj, sk, wsh);
+        const int rc2 = launch_slab<S, C>(bx, d, bpsm, placement, p, stream, stage, pos, tens, tensstage, wcon, out,
+                                          ccol, dcol, ni, nj, nk, si, sj, sk, wsh);
         SB_CHECK(rc2 != SB_ERR_UNSUPPORTED, SB_ERR_UNSUPPORTED,
                  "vadv SLAB variant: needs blocks of 32 or 64 threads, depth 2, 4 or 8, positive strides, "
                  "32-bit offsets and a compute type as wide as the storage ring entries");

@@ -25,6 +25,11 @@ device (continuous batching, not a queue in front of one launch at a time).
 Every result is computed by the same per-item arithmetic wherever and with
 whatever it is batched, so it is bit-identical alone and in a mix.
 
+``Server(mode="plain")`` is the comparison without batching: the same
+admission, fill, slots and streams, but every request is its own
+``sb_hdiff`` / ``sb_vadv`` launch (the library's default form for its size
+and precision) instead of a place in a batched graph replay.
+
 ``run_load`` drives a server with a Poisson arrival process in real time.
 """
 
@@ -41,7 +46,7 @@ from typing import Dict, List, Optional
 
 import numpy as np
 
-from . import _native
+from . import _native, kernels
 from .batching import Batch, HdiffDomain, VadvDomain
 from .device import DeviceBuffer, Event, Field, PinnedBuffer, Stream
 
@@ -208,22 +213,32 @@ class _Slot:
 class Server:
     def __init__(self, budget_bytes: float = 150e9, max_batch: int = 64, max_nk: int = 137, slots_per_form: int = 3,
                  keep_outputs: bool = False, batch_tune: Optional[dict] = None, fill_capacity: int = 4096,
-                 float64_compute: str = "float64"):
+                 float64_compute: str = "float64", mode: str = "batched", keep_inputs: bool = False):
         """``float64_compute`` picks how float64 requests are computed: "float64"
         (exact, bit-identical to the reference's numpy) or "fixed64" (fixed-point
         hdiff and float-pair vadv: errors within 1e-12 / 1e-10 of the field scale,
-        about 3x less device time)."""
+        about 3x less device time).  ``mode`` "batched" packs a slot's requests
+        into one graph replay of the persistent kernels; "plain" launches each
+        request's kernel on its own (the per-request baseline).  ``keep_outputs`` /
+        ``keep_inputs`` keep a completed request's output / input fields until
+        ``release``."""
         if float64_compute not in ("float64", "fixed64"):
             raise ValueError("float64_compute must be 'float64' or 'fixed64'")
+        if mode not in ("batched", "plain"):
+            raise ValueError("mode must be 'batched' or 'plain'")
+        self.mode = mode
         _native.call("sb_set_device", 0)
         self.pool = DevicePool(int(budget_bytes))
         self.max_batch, self.max_nk = max_batch, max_nk
         self.keep_outputs = keep_outputs
+        self.keep_inputs = keep_inputs
         self.float64_compute = float64_compute
         tune = dict(batch_tune or {})
         forms = dict(FORMS, float64=("float64", float64_compute))
+        self.computes = {form: c for form, (_, c) in forms.items()}
         self.slots = {
-            form: [_Slot(Batch(s, c, max_domains=max_batch, max_nk=max_nk, **tune), Stream(), Event())
+            form: [_Slot(Batch(s, c, max_domains=max_batch, max_nk=max_nk, **tune) if mode == "batched" else None,
+                         Stream(), Event())
                    for _ in range(slots_per_form)]
             for form, (s, c) in forms.items()
         }
@@ -271,10 +286,9 @@ class Server:
             self.step()
 
     def release(self, req: Request):
-        """Return a kept output field to the pool (keep_outputs=True)."""
-        out = req.fields.pop("out", None)
-        if out is not None:
-            self.pool.release(out.buffer)
+        """Return a completed request's kept fields to the pool."""
+        for name in list(req.fields):
+            self.pool.release(req.fields.pop(name).buffer)
 
     # -- scheduling -------------------------------------------------------------
 
@@ -289,7 +303,7 @@ class Server:
                 for req in slot.requests:
                     req.completed = now
                     for name in list(req.fields):
-                        if name == "out" and self.keep_outputs:
+                        if self.keep_outputs if name == "out" else self.keep_inputs:
                             continue
                         self.pool.release(req.fields.pop(name).buffer)
                     self.completed.append(req)
@@ -340,15 +354,29 @@ class Server:
                 if slot is None:
                     break
                 reqs = [queue.popleft() for _ in range(min(self.max_batch, len(queue)))]
-                slot.batch.set([r.domain() for r in reqs])
                 _wait(slot.stream, self.fill_done)
-                slot.batch.launch(slot.stream)
+                if self.mode == "batched":
+                    slot.batch.set([r.domain() for r in reqs])
+                    slot.batch.launch(slot.stream)
+                else:
+                    for r in reqs:
+                        self._launch_one(r, slot.stream)
                 slot.done.record(slot.stream)
                 now = time.perf_counter()
                 for r in reqs:
                     r.launched = now
                 slot.requests = reqs
                 slot.busy = True
+
+
+    def _launch_one(self, req: Request, stream: Stream):
+        f = req.fields
+        compute = self.computes[req.storage]
+        if req.op == "hdiff":
+            kernels.hdiff(f["inp"], f["coeff"], f["out"], compute=compute, stream=stream)
+        else:
+            kernels.vadv(f["stage"], f["pos"], f["tens"], f["tensstage"], f["wcon"], out=f["out"],
+                         compute="float32x2" if compute == "fixed64" else compute, stream=stream)
 
 
 # ---------------------------------------------------------------------------
@@ -382,6 +410,7 @@ def run_load(server: Server, requests: List[Request], rate: float, seed: int = 5
     gc.collect()
     gc_was_enabled = gc.isenabled()
     gc.disable()
+    busy_host = 0.0  # time spent in Server.step with requests waiting or ready (host-side scheduling work)
     try:
         t0 = time.perf_counter()
         nxt = 0
@@ -391,7 +420,11 @@ def run_load(server: Server, requests: List[Request], rate: float, seed: int = 5
                 requests[nxt].arrival = t0 + offsets[nxt]
                 server.submit(requests[nxt])
                 nxt += 1
+            pending = bool(server.waiting) or any(server.ready.values())
+            s0 = time.perf_counter()
             server.step()
+            if pending:
+                busy_host += time.perf_counter() - s0
     finally:
         if gc_was_enabled:
             gc.enable()
@@ -399,6 +432,12 @@ def run_load(server: Server, requests: List[Request], rate: float, seed: int = 5
     first = min(r.arrival for r in requests)
     last = max(r.completed for r in requests)
     points = sum(r.points for r in requests)
+    by_form = {}
+    for form in FORMS:
+        fl = [r.latency for r in requests if r.storage == form]
+        if fl:
+            by_form[form] = {"n": len(fl), "p50_ms": float(np.percentile(fl, 50) * 1e3),
+                             "p99_ms": float(np.percentile(fl, 99) * 1e3)}
     return {
         "rate_offered": rate,
         "requests": len(requests),
@@ -409,6 +448,8 @@ def run_load(server: Server, requests: List[Request], rate: float, seed: int = 5
         "gpoints_s": points / (last - first) / 1e9,
         "peak_pool_gb": server.pool.peak / 1e9,
         "max_waiting": server.max_waiting,
+        "host_step_fraction": busy_host / (last - first),
+        "by_precision": by_form,
     }
 
 
@@ -426,22 +467,16 @@ def main(argv=None):
     ap.add_argument("--seed", type=int, default=11)
     ap.add_argument("--float64-compute", choices=["float64", "fixed64"], default="float64",
                     help="float64 requests: exact (float64) or fixed-point hdiff / float-pair vadv (fixed64)")
+    ap.add_argument("--mode", choices=["batched", "plain"], default="batched",
+                    help="batched graph replays, or one kernel launch per request")
     args = ap.parse_args(argv)
     server = Server(budget_bytes=args.budget_gb * 1e9, max_batch=args.max_batch, slots_per_form=args.slots,
-                    float64_compute=args.float64_compute)
+                    float64_compute=args.float64_compute, mode=args.mode)
     warm = request_specs(1024, seed=args.seed + 1000)  # every slot launches (and captures its graph) once
     run_load(server, warm, rate=1e6)
     for rate in (float(r) for r in args.rates.split(",")):
         reqs = request_specs(args.requests, seed=args.seed)
-        stats = run_load(server, reqs, rate=rate)
-        by_form = {}
-        for form in FORMS:
-            lat = [r.latency for r in reqs if r.storage == form]
-            if lat:
-                by_form[form] = {"n": len(lat), "p50_ms": float(np.percentile(lat, 50) * 1e3),
-                                 "p99_ms": float(np.percentile(lat, 99) * 1e3)}
-        stats["by_precision"] = by_form
-        print(json.dumps(stats), flush=True)
+        print(json.dumps(run_load(server, reqs, rate=rate)), flush=True)
     return 0
 
 

@@ -140,3 +140,17 @@ def test_fast_float64_serving_within_tolerance(lib):
     alone.submit(twin)
     alone.drain()
     assert bits_equal(download_output(twin), download_output(probe))
+
+
+def test_plain_mode_serves_the_same_bits(lib):
+    """mode="plain" (one kernel launch per request, the baseline of the
+    batched server) gives every request the oracle's result too."""
+    reqs = _small_mix(16, 12)
+    srv = serving.Server(budget_bytes=8e9, max_batch=6, max_nk=48, slots_per_form=2, keep_outputs=True, mode="plain")
+    stats = serving.run_load(srv, reqs, rate=20000.0)
+    assert stats["requests"] == 16 and 0.0 <= stats["host_step_fraction"] <= 1.0
+    assert set(stats["by_precision"]) <= {"float64", "float32", "bfloat16"}
+    for r in reqs:
+        got, want = download_output(r), expected_output(r)
+        assert bits_equal(got, want), f"request {r}: " + mismatch_report(got, want)
+        srv.release(r)
