@@ -34,12 +34,14 @@ timed region and the maximum time over ranks is reported.
 from __future__ import annotations
 
 import argparse
+import contextlib
 import ctypes
 import json
 import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import threading
 import time
 from pathlib import Path
@@ -702,6 +704,14 @@ def reference_instances(hd, va):
     from stencil_benchmarks.benchmarks_collection.stencils.openmp import vertical_advection as ref_va
 
     out = {"hdiff": {}, "vadv": {}}
+    # the reference writes each generated source into ./benchmarks_source_code
+    # before compiling it: construct in a scratch directory, not the checkout
+    with tempfile.TemporaryDirectory() as scratch, contextlib.chdir(scratch):
+        _construct_reference(ref_hd, ref_va, hd, va, out)
+    return out
+
+
+def _construct_reference(ref_hd, ref_va, hd, va, out):
     for name in REF_HDIFF:
         b = getattr(ref_hd, name)(domain=(NI, NJ, NK), halo=HDIFF_HALO, dtype="float64", verify=False)
         for f in ("inp", "coeff"):
@@ -712,7 +722,6 @@ def reference_instances(hd, va):
         for f in ("ustage", "upos", "utens", "utensstage", "wcon"):
             getattr(b._data[0], f)[...] = va[f]
         out["vadv"][name] = b
-    return out
 
 
 def reference_backends(runs=3):

@@ -53,7 +53,7 @@ def test_reference_arm_under_torchrun():
     pytest.importorskip("torch")
     from oracle import cport
 
-    cport.build()  # the C restatement the reference arm times
+    cport.build()  # the C restatement, the reference arm's fallback
     cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2", "--master-addr",
            "127.0.0.1", "--master-port", str(_free_port()), str(ROOT / "bench.py"), "--impl", "reference",
            "--gpus", "2", "--steps", "1", "--warmup", "3"]
@@ -64,4 +64,11 @@ def test_reference_arm_under_torchrun():
     assert len(lines) == 1
     line = json.loads(lines[0])
     assert line["impl"] == "reference" and line["n_gpus"] == 2 and line["value"] > 0
-    assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["cpu_baseline"]["kind"] == "port"
+    assert line["e2e"]["h2d_bytes_per_step"] == 0
+    # the reference's own OpenMP backends when its package loads and compiles here, else the C port
+    from stencil_benchmarks_gb300 import host
+
+    assert line["cpu_baseline"]["kind"] == ("reference" if host.available() else "port")
+    assert line["config"] == {"workload": "hdiff+vadv fp64 512x512x80 (halo 2,2,0 / 1,1,0)",
+                              "l2": "inputs > L2 (1.35 GB of fields per step), no flush"}
+    assert not (ROOT / "benchmarks_source_code").exists(), "the reference's generated sources landed in the checkout"
