@@ -254,7 +254,9 @@ typedef struct sb_batch_tune {
     int32_t blocks_per_sm; /* persistent blocks per SM (0: 4)                      */
     int32_t hdiff_rows;    /* rows of j per hdiff item (0: 32)                     */
     int32_t hdiff_planes;  /* k-planes per hdiff item (0: 1)                       */
-    int32_t order;         /* reserved (vadv domains always run tallest-first)         */
+    int32_t order;         /* 0: the hdiff kernel enters the graph first; 1: the vadv
+                            * bucket kernels first (tallest bucket first), so their
+                            * blocks are resident before hdiff fills the SMs    */
     int32_t vadv_block;    /* threads (= columns) per vadv block: 32 or 64 (0: 32)   */
     int32_t vadv_blocks_per_sm; /* persistent vadv blocks per SM (0: as many as fit,
                                  * at most 8 with a factor workspace)              */

@@ -5,7 +5,7 @@ scripts/sbench_*_collection.py configurations).
 ``autotune_batch`` times every candidate launch shape -- threads per hdiff
 block, persistent hdiff blocks per SM (the rest of each SM is left to the
 vadv kernels running beside them), rows per hdiff work item, columns per vadv
-block -- on the batch it is given (a few graph replays each, CUDA events, median)
+block, and which kernels enter the graph first -- on the batch it is given (a few graph replays each, CUDA events, median)
 and returns the fastest.  Results are cached in a JSON file keyed by GPU
 name, storage/compute form and a coarse signature of the workload (number of
 hdiff and vadv domains, total points and the largest nk, each rounded to a
@@ -27,14 +27,16 @@ from . import _native
 from .batching import Batch, Domain, HdiffDomain
 
 DEFAULT_CANDIDATES: List[Dict[str, int]] = [
-    {"block": b, "blocks_per_sm": p, "hdiff_rows": r, "hdiff_planes": pl, "vadv_block": vb, "vadv_blocks_per_sm": vp}
+    {"block": b, "blocks_per_sm": p, "hdiff_rows": r, "hdiff_planes": pl, "vadv_block": vb, "vadv_blocks_per_sm": vp,
+     "order": o}
     for b in (128, 256)
     for p in (2, 4, 8)
     for r in (32, 64)
     for pl in (1, 2)
     for vb in (32, 64)
     for vp in (0, 2)
-    if b * p <= 2048
+    for o in (0, 1)
+    if b * p <= 2048 and (o == 0 or (vb == 32 and vp == 0 and p >= 4))
 ]
 
 

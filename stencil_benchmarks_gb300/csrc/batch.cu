@@ -390,10 +390,18 @@ int capture_graph(sb_batch* b) {
     cudaMemcpyAsync(b->dev_table, b->host_table, table_bytes(b->max_domains), cudaMemcpyHostToDevice, s0);
     cudaMemsetAsync(b->counters, 0, sizeof(unsigned long long) * (1 + kBuckets), s0);
     cudaEventRecord(b->fork, s0);
-    cudaStreamWaitEvent(b->streams[1], b->fork, 0);
-    k.hdiff(dim3(b->hdiff_grid), dim3(b->hdiff_block), b->streams[1], b->dev_table, b->counters);
-    cudaEventRecord(b->joins[0], b->streams[1]);
-    for (int q = 0; q < kBuckets; ++q) {
+    // order 0: hdiff first, then the vadv buckets; order 1: the vadv buckets
+    // first (tallest first), so their blocks are resident before the hdiff
+    // blocks take the remaining room of each SM
+    const bool vadv_first = b->tune.order == 1;
+    auto launch_hdiff = [&]() {
+        cudaStreamWaitEvent(b->streams[1], b->fork, 0);
+        k.hdiff(dim3(b->hdiff_grid), dim3(b->hdiff_block), b->streams[1], b->dev_table, b->counters);
+        cudaEventRecord(b->joins[0], b->streams[1]);
+    };
+    if (!vadv_first) launch_hdiff();
+    for (int qq = 0; qq < kBuckets; ++qq) {
+        const int q = vadv_first ? kBuckets - 1 - qq : qq;
         cudaStreamWaitEvent(b->streams[2 + q], b->fork, 0);
         if (b->use_tmem)
             k.vadv_tmem(dim3(b->vadv_tmem_grid), dim3(b->tmem_block[q]), b->tmem_smem, b->streams[2 + q],
@@ -403,6 +411,7 @@ int capture_graph(sb_batch* b) {
                      b->counters + 1 + q, q, b->cap[q], b->ring_offset[q], b->slab[q]);
         cudaEventRecord(b->joins[1 + q], b->streams[2 + q]);
     }
+    if (vadv_first) launch_hdiff();
     for (int q = 0; q < 1 + kBuckets; ++q) cudaStreamWaitEvent(s0, b->joins[q], 0);
     cudaGraph_t graph = nullptr;
     const cudaError_t ec = cudaStreamEndCapture(s0, &graph);
