@@ -317,6 +317,74 @@ int sb_arena_stats(sb_arena* arena, uint64_t* in_use, uint64_t* peak, uint64_t* 
                    uint64_t* free_blocks);
 int sb_arena_destroy(sb_arena* arena);
 
+/* ---- request server (continuous batching) -----------------------------------
+ * No counterpart in the reference (it runs one benchmark at a time).  A
+ * request is one hdiff or vadv (u component) solve on its own domain, with
+ * float64, float32 or bfloat16 storage (float32 compute for the latter two;
+ * float64 requests in float64, or with float64_compute = SB_FIX64 in the fast
+ * forms: fixed-point hdiff, float-pair vadv).  The server owns one device
+ * region of budget_bytes (allocated by sb_server_create), carves request
+ * fields from it, generates the inputs on the device (sb_fill_batch, seeds
+ * derived from the request seed) and runs requests as batched graph replays
+ * (mode 0) or one kernel launch each (mode 1), with slots_per_form batches of
+ * each precision in flight.  sb_server_step(now) polls completions, admits
+ * waiting requests in arrival order as the budget allows, and dispatches;
+ * `now` (any clock, seconds) stamps what happens in the step.  Completed
+ * requests are reported by sb_server_take_completed; with keep bit 0 (outputs)
+ * or bit 1 (inputs) set their fields stay allocated (sb_server_field gives
+ * the address of field q: hdiff inp, coeff, out; vadv stage, pos, tens,
+ * tensstage, wcon, out; i unit-stride, j stride ni + 2h, k stride
+ * (ni + 2h)(nj + 2h), halo h = 2 for hdiff, 1 for vadv) until
+ * sb_server_release; sb_server_query reports the times of a request the
+ * server still holds.  simulate = 1 makes no CUDA call (scheduling tests;
+ * sb_server_debug_complete finishes the in-flight slots, sb_server_debug_launches
+ * lists the launches as (storage, requests)).  One thread per server.        */
+typedef struct sb_server sb_server;
+typedef struct sb_server_config {
+    uint64_t budget_bytes;
+    int32_t max_batch;       /* requests per batch (0: 64)                       */
+    int32_t max_nk;          /* largest vadv nk accepted (0: 137)                */
+    int32_t slots_per_form;  /* batches in flight per precision (0: 3)           */
+    int32_t float64_compute; /* SB_F64 (0 also) or SB_FIX64                      */
+    int32_t mode;            /* 0 batched graph replays, 1 one launch per request */
+    int32_t keep;            /* bit 0 outputs, bit 1 inputs: kept until released */
+    int32_t fill_capacity;   /* fill descriptors per step (0: 4096)              */
+    int32_t simulate;
+    sb_batch_tune tune;      /* batch launch shape (zeros: defaults)             */
+} sb_server_config;
+typedef struct sb_request {
+    int64_t id;              /* unique among the requests the server holds       */
+    int32_t op;              /* SB_OP_HDIFF or SB_OP_VADV                        */
+    int32_t storage;         /* SB_F64, SB_F32 or SB_BF16                        */
+    int64_t ni, nj, nk;
+    uint64_t seed;
+    double arrival;          /* caller's clock, copied into the completion       */
+} sb_request;
+typedef struct sb_completion {
+    int64_t id;
+    double arrival, admitted, launched, completed;
+} sb_completion;
+typedef struct sb_server_state {
+    uint64_t budget_bytes, in_use_bytes, peak_bytes;
+    int64_t waiting, ready, inflight, max_waiting, busy_slots;
+    double work_seconds;     /* host time in steps that retired, admitted or launched */
+} sb_server_state;
+typedef struct sb_server_launch {
+    int32_t storage, requests;
+} sb_server_launch;
+int sb_server_create(sb_server** server, const sb_server_config* config);
+int sb_server_destroy(sb_server* server);
+int sb_server_submit(sb_server* server, const sb_request* request);
+int sb_server_step(sb_server* server, double now, int* busy);
+int sb_server_take_completed(sb_server* server, sb_completion* out, int capacity, int* n);
+int sb_server_field(sb_server* server, int64_t id, int field, void** ptr);
+/* times of a request the server still holds (-1: not yet) */
+int sb_server_query(sb_server* server, int64_t id, sb_completion* record);
+int sb_server_release(sb_server* server, int64_t id);
+int sb_server_stats(sb_server* server, sb_server_state* stats);
+int sb_server_debug_complete(sb_server* server);
+int sb_server_debug_launches(sb_server* server, sb_server_launch* out, int capacity, int* n);
+
 /* ---- vertical advection without device allocation -------------------------
  * No counterpart in the reference.  For callers that cannot call cudaMalloc:
  * code embedded in a host framework that owns every device allocation (fixed

@@ -3,20 +3,21 @@
 A request is one stencil solve (hdiff, or vadv u component) on its own domain
 with a storage precision tag (float64, float32, or bfloat16 storage with
 float32 compute).  Its fields live on the device from admission to
-completion: the server allocates them from a budget-capped pool and creates
-the inputs in place with the library's seeded generator (``sb_fill_batch``),
-so request data never crosses the host link; the output stays on the device
-for the client.
+completion: the server allocates them from a budget-capped region and
+creates the inputs in place with the library's seeded generator
+(``sb_fill_batch``), so request data never crosses the host link; the output
+stays on the device for the client.
 
-Scheduling (``Server.step``), repeated by the caller's loop:
+The scheduler is native (``csrc/server.cu``, ``sb_server_*``); ``Server`` is
+its Python face.  ``Server.step`` runs, in the library:
 
 1. poll: batches whose completion event has fired retire their requests
-   (latency = completion seen - arrival) and return their memory to the pool;
-2. admit: waiting requests, in arrival order, get their fields if the pool's
+   (latency = completion seen - arrival) and return their memory;
+2. admit: waiting requests, in arrival order, get their fields if the
    budget allows (150 GB by default); one ``sb_fill_batch`` launch creates the
    inputs of everything admitted in this step;
 3. dispatch: for every precision form with admitted requests and a free slot,
-   up to ``max_batch`` of them are packed into that slot's ``Batch`` and
+   up to ``max_batch`` of them are packed into that slot's batch and
    launched (one graph replay) on the slot's stream, after the fill.
 
 Several slots per form are in flight at once, so requests that arrive while
@@ -35,10 +36,10 @@ and precision) instead of a place in a batched graph replay.
 
 from __future__ import annotations
 
-import collections
 import ctypes
-import math
 import gc
+import itertools
+import math
 import time
 import weakref
 from dataclasses import dataclass, field
@@ -46,12 +47,11 @@ from typing import Dict, List, Optional
 
 import numpy as np
 
-from . import _native, kernels
-from .batching import Batch, HdiffDomain, VadvDomain
-from .device import DeviceBuffer, Event, Field, PinnedBuffer, Stream
+from . import _native
+from .batching import SbBatchTune
+from .device import DeviceBuffer, Field, Stream
 
 ALIGN = 256  # field allocations start on 256-byte boundaries
-FILL_DEPTH = 8  # page-locked staging slots for fill descriptors
 
 FORMS = {"float64": ("float64", "float64"), "float32": ("float32", "float32"), "bfloat16": ("bfloat16", "float32")}
 ITEMSIZE = {"float64": 8, "float32": 4, "bfloat16": 2}
@@ -108,11 +108,6 @@ class Request:
         n = len(HDIFF_FIELDS if self.op == "hdiff" else VADV_FIELDS)
         return n * _round(math.prod(shape) * ITEMSIZE[self.storage])
 
-    def domain(self):
-        f = self.fields
-        if self.op == "hdiff":
-            return HdiffDomain(f["inp"], f["coeff"], f["out"])
-        return VadvDomain(f["stage"], f["pos"], f["tens"], f["tensstage"], f["wcon"], out=f["out"])
 
 
 def _round(nbytes: int) -> int:
@@ -175,15 +170,6 @@ class DevicePool:
         return self.stats()["peak"]
 
 
-def _event_done(event: Event) -> bool:
-    rc = _native.lib().sb_event_query(ctypes.c_void_p(event.handle))
-    if rc == _native.SB_NOT_READY:
-        return False
-    if rc != _native.SB_OK:
-        raise _native.SbError("sb_event_query", rc, _native.last_error())
-    return True
-
-
 def _fill(descs, scratch: DeviceBuffer, stream: Stream, staging: Optional[int] = None):
     """Generate the fields ``descs`` describe on ``stream``.  With ``staging``
     (page-locked host memory for ``len(descs)`` descriptors, left untouched
@@ -197,186 +183,201 @@ def _fill(descs, scratch: DeviceBuffer, stream: Stream, staging: Optional[int] =
     _native.call("sb_fill_batch", ctypes.c_void_p(src), len(descs), ctypes.c_void_p(scratch.ptr), stream.as_parameter)
 
 
-def _wait(stream: Stream, event: Event):
-    _native.call("sb_stream_wait_event", stream.as_parameter, ctypes.c_void_p(event.handle))
+class SbServerConfig(ctypes.Structure):
+    _fields_ = [("budget_bytes", ctypes.c_uint64), ("max_batch", ctypes.c_int32), ("max_nk", ctypes.c_int32),
+                ("slots_per_form", ctypes.c_int32), ("float64_compute", ctypes.c_int32), ("mode", ctypes.c_int32),
+                ("keep", ctypes.c_int32), ("fill_capacity", ctypes.c_int32), ("simulate", ctypes.c_int32),
+                ("tune", SbBatchTune)]
 
 
-@dataclass
-class _Slot:
-    batch: Batch
-    stream: Stream
-    done: Event
-    requests: List[Request] = field(default_factory=list)
-    busy: bool = False
+class SbRequest(ctypes.Structure):
+    _fields_ = [("id", ctypes.c_int64), ("op", ctypes.c_int32), ("storage", ctypes.c_int32), ("ni", ctypes.c_int64),
+                ("nj", ctypes.c_int64), ("nk", ctypes.c_int64), ("seed", ctypes.c_uint64), ("arrival", ctypes.c_double)]
+
+
+class SbCompletion(ctypes.Structure):
+    _fields_ = [("id", ctypes.c_int64), ("arrival", ctypes.c_double), ("admitted", ctypes.c_double),
+                ("launched", ctypes.c_double), ("completed", ctypes.c_double)]
+
+
+class SbServerState(ctypes.Structure):
+    _fields_ = [("budget_bytes", ctypes.c_uint64), ("in_use_bytes", ctypes.c_uint64), ("peak_bytes", ctypes.c_uint64),
+                ("waiting", ctypes.c_int64), ("ready", ctypes.c_int64), ("inflight", ctypes.c_int64),
+                ("max_waiting", ctypes.c_int64), ("busy_slots", ctypes.c_int64), ("work_seconds", ctypes.c_double)]
+
+
+class SbServerLaunch(ctypes.Structure):
+    _fields_ = [("storage", ctypes.c_int32), ("requests", ctypes.c_int32)]
+
+
+_STORAGE_NAME = {_native.DTYPE_CODES[f]: f for f in FORMS}
+
+
+class _PoolView:
+    """Memory counters of a server's region (bytes)."""
+
+    def __init__(self, server):
+        self._server = server
+
+    @property
+    def budget(self) -> int:
+        return self._server.state().budget_bytes
+
+    @property
+    def in_use(self) -> int:
+        return self._server.state().in_use_bytes
+
+    @property
+    def peak(self) -> int:
+        return self._server.state().peak_bytes
 
 
 class Server:
+    """The native continuous-batching server (sb_server_*), driven from Python.
+
+    Per request Python makes one call (``submit``); ``step`` runs the native
+    poll / admit / dispatch and hands back the completed requests.  The
+    Request objects given to ``submit`` get their ``admitted`` /
+    ``launched`` / ``completed`` times (on ``time.perf_counter``'s clock) when
+    they complete, and their kept fields (``keep_outputs`` / ``keep_inputs``)
+    as ``Field`` objects in ``fields`` until ``release``."""
+
     def __init__(self, budget_bytes: float = 150e9, max_batch: int = 64, max_nk: int = 137, slots_per_form: int = 3,
                  keep_outputs: bool = False, batch_tune: Optional[dict] = None, fill_capacity: int = 4096,
-                 float64_compute: str = "float64", mode: str = "batched", keep_inputs: bool = False):
+                 float64_compute: str = "float64", mode: str = "batched", keep_inputs: bool = False,
+                 simulate: bool = False):
         """``float64_compute`` picks how float64 requests are computed: "float64"
         (exact, bit-identical to the reference's numpy) or "fixed64" (fixed-point
         hdiff and float-pair vadv: errors within 1e-12 / 1e-10 of the field scale,
         about 3x less device time).  ``mode`` "batched" packs a slot's requests
         into one graph replay of the persistent kernels; "plain" launches each
-        request's kernel on its own (the per-request baseline).  ``keep_outputs`` /
-        ``keep_inputs`` keep a completed request's output / input fields until
-        ``release``."""
+        request's kernel on its own (the per-request baseline).  ``simulate``
+        runs the scheduling without any device work (tests)."""
         if float64_compute not in ("float64", "fixed64"):
             raise ValueError("float64_compute must be 'float64' or 'fixed64'")
         if mode not in ("batched", "plain"):
             raise ValueError("mode must be 'batched' or 'plain'")
         self.mode = mode
-        _native.call("sb_set_device", 0)
-        self.pool = DevicePool(int(budget_bytes))
-        self.max_batch, self.max_nk = max_batch, max_nk
-        self.keep_outputs = keep_outputs
-        self.keep_inputs = keep_inputs
-        self.float64_compute = float64_compute
-        tune = dict(batch_tune or {})
-        forms = dict(FORMS, float64=("float64", float64_compute))
-        self.computes = {form: c for form, (_, c) in forms.items()}
-        self.slots = {
-            form: [_Slot(Batch(s, c, max_domains=max_batch, max_nk=max_nk, **tune) if mode == "batched" else None,
-                         Stream(), Event())
-                   for _ in range(slots_per_form)]
-            for form, (s, c) in forms.items()
-        }
-        self.waiting: collections.deque = collections.deque()
-        self.ready = {form: collections.deque() for form in FORMS}
+        self.max_nk = max_nk
+        self._lib = _native.lib()
+        cfg = SbServerConfig(budget_bytes=int(budget_bytes), max_batch=max_batch, max_nk=max_nk,
+                             slots_per_form=slots_per_form,
+                             float64_compute=_native.DTYPE_CODES["fixed64" if float64_compute == "fixed64" else "float64"],
+                             mode=0 if mode == "batched" else 1, keep=(1 if keep_outputs else 0) | (2 if keep_inputs else 0),
+                             fill_capacity=fill_capacity, simulate=1 if simulate else 0)
+        for k, v in (batch_tune or {}).items():
+            setattr(cfg.tune, k, int(v))
+        handle = ctypes.c_void_p()
+        self._check("sb_server_create", self._lib.sb_server_create(ctypes.byref(handle), ctypes.byref(cfg)))
+        self._handle = handle
+        self._finalizer = weakref.finalize(self, self._lib.sb_server_destroy, handle)
+        self.pool = _PoolView(self)
         self.completed: List[Request] = []
-        # fills go out on their own stream; their descriptors are staged in a
-        # page-locked ring of FILL_DEPTH slots, each reused once the fill that
-        # last read it has run (its event)
-        self.fill_stream = Stream()
-        self.fill_capacity = fill_capacity
-        self.fill_scratch = DeviceBuffer(ctypes.sizeof(SbFillDesc) * fill_capacity)
-        self.fill_staging = PinnedBuffer(ctypes.sizeof(SbFillDesc) * fill_capacity * FILL_DEPTH)
-        self.fill_events = [Event() for _ in range(FILL_DEPTH)]
-        self._fill_used = [False] * FILL_DEPTH
-        self._fill_next = 0
-        self.fill_done = self.fill_events[0]
-        self.max_waiting = 0
+        self._held: Dict[int, Request] = {}
+        self._ids = itertools.count()
+        self._done = (SbCompletion * 1024)()
+        self._busy = ctypes.c_int(0)
+        self._req = SbRequest()
+
+    @staticmethod
+    def _check(name, rc):
+        if rc != _native.SB_OK:
+            raise _native.SbError(name, rc, _native.last_error())
 
     # -- client side ------------------------------------------------------------
 
     def submit(self, req: Request):
         if req.storage not in FORMS:
             raise ValueError(f"unknown precision {req.storage!r}")
-        if req.op == "vadv" and req.nk > self.max_nk:
-            raise ValueError(f"nk = {req.nk} exceeds the server's max_nk {self.max_nk}")
-        if req.footprint() > self.pool.budget:
-            raise ValueError("request larger than the whole memory budget")
         if req.arrival is None:
             req.arrival = time.perf_counter()
-        self.waiting.append(req)
-        self.max_waiting = max(self.max_waiting, len(self.waiting))
+        key = next(self._ids)
+        r = self._req
+        r.id, r.op, r.storage = key, 0 if req.op == "hdiff" else 1, _native.DTYPE_CODES[req.storage]
+        r.ni, r.nj, r.nk, r.seed, r.arrival = req.ni, req.nj, req.nk, req.seed % (1 << 64), req.arrival
+        rc = self._lib.sb_server_submit(self._handle, ctypes.byref(r))
+        if rc == _native.SB_ERR_INVALID:
+            raise ValueError(_native.last_error())
+        self._check("sb_server_submit", rc)
+        req._key = key
+        self._held[key] = req
+
+    def step(self, now: Optional[float] = None) -> bool:
+        """One poll / admit / dispatch; True while requests are waiting, queued
+        or on the device."""
+        self._check("sb_server_step", self._lib.sb_server_step(self._handle, ctypes.c_double(
+            time.perf_counter() if now is None else now), ctypes.byref(self._busy)))
+        self._collect()
+        return bool(self._busy.value)
 
     def busy(self) -> bool:
-        return bool(self.waiting) or any(self.ready.values()) or any(
-            s.busy for slots in self.slots.values() for s in slots)
-
-    def step(self):
-        self._poll()
-        self._admit()
-        self._dispatch()
+        st = self.state()
+        return bool(st.waiting or st.ready or st.inflight)
 
     def drain(self):
-        while self.busy():
-            self.step()
+        while self.step():
+            pass
 
     def release(self, req: Request):
         """Return a completed request's kept fields to the pool."""
-        for name in list(req.fields):
-            self.pool.release(req.fields.pop(name).buffer)
+        if req.fields:
+            self._check("sb_server_release", self._lib.sb_server_release(self._handle, ctypes.c_int64(req._key)))
+        req.fields.clear()
 
-    # -- scheduling -------------------------------------------------------------
+    def query(self, req: Request) -> Request:
+        """Refresh the times of a request the server still holds."""
+        rec = SbCompletion()
+        if self._lib.sb_server_query(self._handle, ctypes.c_int64(req._key), ctypes.byref(rec)) == _native.SB_OK:
+            req.admitted, req.launched, req.completed = (v if v >= 0.0 else None
+                                                         for v in (rec.admitted, rec.launched, rec.completed))
+        return req
 
-    def _poll(self):
-        for slots in self.slots.values():
-            for slot in slots:
-                if not slot.busy:
-                    continue
-                if not _event_done(slot.done):
-                    continue
-                now = time.perf_counter()
-                for req in slot.requests:
-                    req.completed = now
-                    for name in list(req.fields):
-                        if self.keep_outputs if name == "out" else self.keep_inputs:
-                            continue
-                        self.pool.release(req.fields.pop(name).buffer)
-                    self.completed.append(req)
-                slot.requests = []
-                slot.busy = False
+    def state(self) -> SbServerState:
+        st = SbServerState()
+        self._check("sb_server_stats", self._lib.sb_server_stats(self._handle, ctypes.byref(st)))
+        return st
 
-    def _admit(self):
-        descs = []
-        now = time.perf_counter()
-        while self.waiting and len(descs) + 6 <= self.fill_capacity:
-            req = self.waiting[0]
-            specs = HDIFF_FIELDS if req.op == "hdiff" else VADV_FIELDS
-            shape, strides, halo = field_layout(req.op, req.ni, req.nj, req.nk)
-            count = math.prod(shape)
-            bufs = []
-            for _ in specs:
-                buf = self.pool.try_alloc(count * ITEMSIZE[req.storage])
-                if buf is None:
-                    break
-                bufs.append(buf)
-            if len(bufs) < len(specs):  # budget exhausted: wait for completions (FIFO order kept)
-                for buf in bufs:
-                    self.pool.release(buf)
-                break
-            self.waiting.popleft()
-            code = _native.storage_code(req.storage)
-            for q, ((name, lo, hi), buf) in enumerate(zip(specs, bufs)):
-                req.fields[name] = Field(buf, shape, strides, req.storage, halo)
-                if lo is not None:
-                    descs.append(SbFillDesc(buf.ptr, count, field_seed(req.seed, q), lo, hi, code, 0))
-            req.admitted = now
-            self.ready[req.storage].append(req)
-        if descs:
-            k = self._fill_next
-            self._fill_next = (k + 1) % FILL_DEPTH
-            if self._fill_used[k]:
-                self.fill_events[k].synchronize()  # normally long done
-            staging = self.fill_staging.ptr + k * self.fill_capacity * ctypes.sizeof(SbFillDesc)
-            _fill(descs, self.fill_scratch, self.fill_stream, staging)
-            self.fill_events[k].record(self.fill_stream)
-            self._fill_used[k] = True
-            self.fill_done = self.fill_events[k]
+    @property
+    def max_waiting(self) -> int:
+        return self.state().max_waiting
 
-    def _dispatch(self):
-        for form, queue in self.ready.items():
-            while queue:
-                slot = next((s for s in self.slots[form] if not s.busy), None)
-                if slot is None:
-                    break
-                reqs = [queue.popleft() for _ in range(min(self.max_batch, len(queue)))]
-                _wait(slot.stream, self.fill_done)
-                if self.mode == "batched":
-                    slot.batch.set([r.domain() for r in reqs])
-                    slot.batch.launch(slot.stream)
-                else:
-                    for r in reqs:
-                        self._launch_one(r, slot.stream)
-                slot.done.record(slot.stream)
-                now = time.perf_counter()
-                for r in reqs:
-                    r.launched = now
-                slot.requests = reqs
-                slot.busy = True
+    def debug_complete(self):
+        """Simulating server: finish every batch in flight."""
+        self._check("sb_server_debug_complete", self._lib.sb_server_debug_complete(self._handle))
 
+    def launches(self):
+        """Simulating server: the launches so far, as (storage, requests)."""
+        n = ctypes.c_int(0)
+        self._lib.sb_server_debug_launches(self._handle, None, 0, ctypes.byref(n))
+        out = (SbServerLaunch * max(1, n.value))()
+        self._check("sb_server_debug_launches",
+                    self._lib.sb_server_debug_launches(self._handle, out, n.value, ctypes.byref(n)))
+        return [(_STORAGE_NAME[out[q].storage], out[q].requests) for q in range(n.value)]
 
-    def _launch_one(self, req: Request, stream: Stream):
-        f = req.fields
-        compute = self.computes[req.storage]
-        if req.op == "hdiff":
-            kernels.hdiff(f["inp"], f["coeff"], f["out"], compute=compute, stream=stream)
-        else:
-            kernels.vadv(f["stage"], f["pos"], f["tens"], f["tensstage"], f["wcon"], out=f["out"],
-                         compute="float32x2" if compute == "fixed64" else compute, stream=stream)
+    # -- completions --------------------------------------------------------------
+
+    def _collect(self):
+        n = ctypes.c_int(0)
+        while True:
+            self._check("sb_server_take_completed",
+                        self._lib.sb_server_take_completed(self._handle, self._done, len(self._done), ctypes.byref(n)))
+            for q in range(n.value):
+                rec = self._done[q]
+                req = self._held.pop(rec.id)
+                req.admitted, req.launched, req.completed = rec.admitted, rec.launched, rec.completed
+                self._attach_kept(req)
+                self.completed.append(req)
+            if n.value < len(self._done):
+                return
+
+    def _attach_kept(self, req: Request):
+        specs = HDIFF_FIELDS if req.op == "hdiff" else VADV_FIELDS
+        shape, strides, halo = field_layout(req.op, req.ni, req.nj, req.nk)
+        nbytes = math.prod(shape) * ITEMSIZE[req.storage]
+        ptr = ctypes.c_void_p()
+        for q, (name, _, _) in enumerate(specs):
+            if self._lib.sb_server_field(self._handle, ctypes.c_int64(req._key), q, ctypes.byref(ptr)) == _native.SB_OK:
+                req.fields[name] = Field(Block(ptr.value, nbytes), shape, strides, req.storage, halo)
 
 
 # ---------------------------------------------------------------------------
@@ -410,21 +411,18 @@ def run_load(server: Server, requests: List[Request], rate: float, seed: int = 5
     gc.collect()
     gc_was_enabled = gc.isenabled()
     gc.disable()
-    busy_host = 0.0  # time spent in Server.step with requests waiting or ready (host-side scheduling work)
+    work0 = server.state().work_seconds
     try:
         t0 = time.perf_counter()
         nxt = 0
-        while nxt < len(requests) or server.busy():
+        busy = True
+        while nxt < len(requests) or busy:
             now = time.perf_counter() - t0
             while nxt < len(requests) and offsets[nxt] <= now:
                 requests[nxt].arrival = t0 + offsets[nxt]
                 server.submit(requests[nxt])
                 nxt += 1
-            pending = bool(server.waiting) or any(server.ready.values())
-            s0 = time.perf_counter()
-            server.step()
-            if pending:
-                busy_host += time.perf_counter() - s0
+            busy = server.step()
     finally:
         if gc_was_enabled:
             gc.enable()
@@ -448,7 +446,7 @@ def run_load(server: Server, requests: List[Request], rate: float, seed: int = 5
         "gpoints_s": points / (last - first) / 1e9,
         "peak_pool_gb": server.pool.peak / 1e9,
         "max_waiting": server.max_waiting,
-        "host_step_fraction": busy_host / (last - first),
+        "host_step_fraction": (server.state().work_seconds - work0) / (last - first),
         "by_precision": by_form,
     }
 

@@ -1,6 +1,8 @@
-"""Scheduling logic of the server on the CPU: admission by memory budget in
-arrival order, continuous batching over several in-flight slots, pool reuse.
-The device is replaced by fakes (no GPU work happens here)."""
+"""Scheduling logic of the native server on the CPU: admission by memory
+budget in arrival order, continuous batching over several in-flight slots,
+forms, kept fields.  The server runs in its simulating mode (no CUDA call:
+launches are recorded, in-flight work completes on request), so no GPU work
+happens here; the arena tests use a fake device region."""
 
 from __future__ import annotations
 
@@ -18,137 +20,110 @@ class FakeBuffer:
     def __init__(self, nbytes):
         self.nbytes = int(nbytes)
         self.ptr = next(FakeBuffer._ptrs)
-        self.freed = False
-
-    def free(self):
-        self.freed = True
-
-
-class FakeBatch:
-    launches = []
-
-    def __init__(self, storage, compute, max_domains, max_nk, **kw):
-        self.storage, self.max_domains = storage, max_domains
-        self.domains = []
-
-    def set(self, domains):
-        assert len(domains) <= self.max_domains
-        self.domains = list(domains)
-
-    def launch(self, stream=None, timed=False):
-        FakeBatch.launches.append((self.storage, len(self.domains)))
-
-
-class FakeHandle:
-    def __init__(self):
-        self.handle = id(self)
-        self.as_parameter = None
-
-    def record(self, stream=None):
-        pass
-
-    def synchronize(self):
-        pass
 
 
 @pytest.fixture(scope="module", autouse=True)
 def _library_built():
-    """The pool's arena is host code in the native library (no GPU needed)."""
+    """The scheduler and the arena are host code in the native library (no GPU needed)."""
     from stencil_benchmarks_gb300 import build
 
     build.build()
 
 
 @pytest.fixture
-def fake_device(monkeypatch):
-    done = set()
+def fake_region(monkeypatch):
     monkeypatch.setattr(serving, "DeviceBuffer", FakeBuffer)
-    monkeypatch.setattr(serving, "Batch", FakeBatch)
-    monkeypatch.setattr(serving, "Stream", FakeHandle)
-    monkeypatch.setattr(serving, "Event", FakeHandle)
-    monkeypatch.setattr(serving, "_fill", lambda descs, scratch, stream, staging=None: None)
-    monkeypatch.setattr(serving, "_wait", lambda stream, event: None)
-    monkeypatch.setattr(serving, "_event_done", lambda ev: id(ev) in done)
-    monkeypatch.setattr(serving._native, "call", lambda *a, **k: 0)
-    FakeBatch.launches = []
-    return done
 
 
 def _req(rid, op="hdiff", n=64, nk=10, storage="float32"):
     return serving.Request(rid, op, n, n, nk, storage, seed=rid)
 
 
-def _complete_all(server, done):
-    for slots in server.slots.values():
-        for s in slots:
-            if s.busy:
-                done.add(id(s.done))
+def _server(**kw):
+    return serving.Server(simulate=True, **kw)
 
 
-def test_admission_respects_budget_in_arrival_order(fake_device):
+def _run_out(server):
+    while server.step():
+        server.debug_complete()
+
+
+def test_admission_respects_budget_in_arrival_order():
     one = _req(0).footprint()
-    server = serving.Server(budget_bytes=2 * one, max_batch=8, slots_per_form=2)
+    server = _server(budget_bytes=2 * one, max_batch=8, slots_per_form=2)
     reqs = [_req(i) for i in range(5)]
     for r in reqs:
         server.submit(r)
     server.step()
-    assert [r.admitted is not None for r in reqs] == [True, True, False, False, False]
+    assert [server.query(r).admitted is not None for r in reqs] == [True, True, False, False, False]
     assert server.pool.in_use <= server.pool.budget
-    _complete_all(server, fake_device)
+    server.debug_complete()
     server.step()  # retire 0, 1; admit 2, 3
     assert reqs[0].completed and reqs[1].completed
-    assert [r.admitted is not None for r in reqs] == [True] * 4 + [False]
-    while server.busy():
-        _complete_all(server, fake_device)
-        server.step()
-    assert all(r.completed for r in reqs)
+    assert [server.query(r).admitted is not None for r in reqs] == [True] * 4 + [False]
+    _run_out(server)
+    assert all(r.completed for r in reqs) and len(server.completed) == 5
+    assert all(r.arrival <= r.admitted <= r.launched <= r.completed for r in reqs)
     assert server.pool.peak <= server.pool.budget
     assert server.pool.in_use == 0
 
 
-def test_continuous_batching_overlaps_slots(fake_device):
-    server = serving.Server(budget_bytes=1e12, max_batch=4, slots_per_form=3)
+def test_continuous_batching_overlaps_slots():
+    server = _server(budget_bytes=1e12, max_batch=4, slots_per_form=3)
     first = [_req(i) for i in range(4)]
     for r in first:
         server.submit(r)
     server.step()
-    assert FakeBatch.launches == [("float32", 4)]
+    assert server.launches() == [("float32", 4)]
     # new arrivals while the first batch still runs go out in a second slot
     late = [_req(10 + i) for i in range(3)]
     for r in late:
         server.submit(r)
     server.step()
-    assert FakeBatch.launches == [("float32", 4), ("float32", 3)]
-    busy = sum(s.busy for s in server.slots["float32"])
-    assert busy == 2
-    _complete_all(server, fake_device)
+    assert server.launches() == [("float32", 4), ("float32", 3)]
+    assert server.state().busy_slots == 2
+    server.debug_complete()
     server.step()
     assert all(r.completed for r in first + late)
 
 
-def test_forms_go_to_their_own_batches(fake_device):
-    server = serving.Server(budget_bytes=1e12, max_batch=8, slots_per_form=1)
+def test_forms_go_to_their_own_batches():
+    server = _server(budget_bytes=1e12, max_batch=8, slots_per_form=1)
     for i, st in enumerate(["float64", "float32", "bfloat16", "float32"]):
         server.submit(_req(i, op="vadv" if i % 2 else "hdiff", storage=st))
     server.step()
-    assert sorted(FakeBatch.launches) == [("bfloat16", 1), ("float32", 2), ("float64", 1)]
+    assert sorted(server.launches()) == [("bfloat16", 1), ("float32", 2), ("float64", 1)]
 
 
-def test_slots_limit_in_flight_batches(fake_device):
-    server = serving.Server(budget_bytes=1e12, max_batch=2, slots_per_form=2)
+def test_slots_limit_in_flight_batches():
+    server = _server(budget_bytes=1e12, max_batch=2, slots_per_form=2)
     reqs = [_req(i) for i in range(9)]
     for r in reqs:
         server.submit(r)
     server.step()
-    assert len(FakeBatch.launches) == 2  # two slots, two requests each
-    assert len(server.ready["float32"]) == 5
-    while server.busy():
-        _complete_all(server, fake_device)
-        server.step()
-    assert sum(n for _, n in FakeBatch.launches) == 9
+    assert len(server.launches()) == 2  # two slots, two requests each
+    assert server.state().ready == 5
+    _run_out(server)
+    assert sum(n for _, n in server.launches()) == 9 and all(r.completed for r in reqs)
 
 
-def test_pool_arena_best_fit_and_coalescing(fake_device):
+def test_many_requests_under_a_tight_budget_all_complete():
+    rng = np.random.Generator(np.random.PCG64(5))
+    reqs = [_req(i, op=("hdiff", "vadv")[i % 2], n=int(rng.integers(8, 200)), nk=int(rng.integers(2, 60)),
+                 storage=("float64", "float32", "bfloat16")[i % 3]) for i in range(300)]
+    budget = 3 * max(r.footprint() for r in reqs)
+    server = _server(budget_bytes=budget, max_batch=5, slots_per_form=2, max_nk=60)
+    for r in reqs[:150]:
+        server.submit(r)
+    server.step()
+    for r in reqs[150:]:
+        server.submit(r)
+    _run_out(server)
+    assert len(server.completed) == 300 and server.pool.in_use == 0
+    assert server.pool.peak <= budget and server.max_waiting >= 150
+
+
+def test_pool_arena_best_fit_and_coalescing(fake_region):
     A = serving.ALIGN
     pool = serving.DevicePool(budget_bytes=100 * A)
     base = pool.region.ptr
@@ -173,7 +148,7 @@ def test_pool_arena_best_fit_and_coalescing(fake_device):
         pool.release(c)  # double free is an error, not silent corruption
 
 
-def test_pool_random_churn_keeps_invariants(fake_device):
+def test_pool_random_churn_keeps_invariants(fake_region):
     A = serving.ALIGN
     pool = serving.DevicePool(budget_bytes=4096 * A)
     base = pool.region.ptr
@@ -195,27 +170,40 @@ def test_pool_random_churn_keeps_invariants(fake_device):
     assert pool.stats()["free_blocks"] == 1 and pool.in_use == 0
 
 
-def test_invalid_requests_rejected(fake_device):
-    server = serving.Server(budget_bytes=1e9, max_nk=50)
+def test_invalid_requests_rejected():
+    server = _server(budget_bytes=1e9, max_nk=50)
     with pytest.raises(ValueError):
         server.submit(_req(0, storage="float16"))
-    with pytest.raises(ValueError):
+    with pytest.raises(ValueError, match="max_nk"):
         server.submit(_req(1, op="vadv", nk=51))
-    with pytest.raises(ValueError):
-        server.submit(_req(2, n=4096, nk=100))  # larger than the budget
+    with pytest.raises(ValueError, match="budget"):
+        server.submit(_req(2, n=4096, nk=100))  # larger than the whole budget
 
 
-def test_keep_outputs_and_release(fake_device):
-    server = serving.Server(budget_bytes=1e12, keep_outputs=True)
+def test_keep_outputs_and_release():
+    server = _server(budget_bytes=1e12, keep_outputs=True)
     r = _req(0)
     server.submit(r)
     server.step()
-    _complete_all(server, fake_device)
+    server.debug_complete()
     server.step()
     assert set(r.fields) == {"out"}
+    assert r.fields["out"].shape == (68, 68, 10) and r.fields["out"].strides == (1, 68, 68 * 68)
     before = server.pool.in_use
     server.release(r)
     assert server.pool.in_use < before and not r.fields
+
+
+def test_keep_inputs_too():
+    server = _server(budget_bytes=1e12, keep_outputs=True, keep_inputs=True)
+    r = _req(0, op="vadv")
+    server.submit(r)
+    server.step()
+    server.debug_complete()
+    server.step()
+    assert set(r.fields) == {"stage", "pos", "tens", "tensstage", "wcon", "out"}
+    server.release(r)
+    assert server.pool.in_use == 0
 
 
 def test_request_specs_distribution():
