@@ -138,6 +138,18 @@ SIGNATURES = {
     "sb_arena_free": [_vp, ctypes.c_uint64],
     "sb_arena_stats": [_vp] + [ctypes.POINTER(ctypes.c_uint64)] * 4,
     "sb_arena_destroy": [_vp],
+    # server entry points take struct pointers (serving.py passes ctypes structures)
+    "sb_server_create": [ctypes.POINTER(_vp), _vp],
+    "sb_server_destroy": [_vp],
+    "sb_server_submit": [_vp, _vp],
+    "sb_server_step": [_vp, _dbl, ctypes.POINTER(_int)],
+    "sb_server_take_completed": [_vp, _vp, _int, ctypes.POINTER(_int)],
+    "sb_server_field": [_vp, _i64, _int, ctypes.POINTER(_vp)],
+    "sb_server_query": [_vp, _i64, _vp],
+    "sb_server_release": [_vp, _i64],
+    "sb_server_stats": [_vp, _vp],
+    "sb_server_debug_complete": [_vp],
+    "sb_server_debug_launches": [_vp, _vp, _int, ctypes.POINTER(_int)],
     "sb_probe_arith_rate": [_int, _dp],
 }
 _RESTYPES = {"sb_last_error": ctypes.c_char_p}
