@@ -609,7 +609,7 @@ def run_served(n_requests=10000, rates=SERVE_RATES, seed=11, float64_compute="fl
         stats = serving.run_load(server, serving.request_specs(n_requests, seed=seed), rate=rate)
         stats["gpu_util_pct"] = util.stop()
         out.append(stats)
-    del server
+    server.close()
     return out
 
 
@@ -658,6 +658,7 @@ def served_precision_errors(n=12, seed=97):
             p99s.append(float(np.percentile(np.abs(got - want)[big] / np.abs(want)[big], 99)))
             server.release(r)
         errors[form] = {"requests": n, "max_abs_over_scale": worst, "p99_pointwise_rel": max(p99s) if p99s else 0.0}
+    server.close()
     return errors
 
 

@@ -271,7 +271,6 @@ class Server:
         self._check("sb_server_create", self._lib.sb_server_create(ctypes.byref(handle), ctypes.byref(cfg)))
         self._handle = handle
         self._finalizer = weakref.finalize(self, self._lib.sb_server_destroy, handle)
-        self.pool = _PoolView(self)
         self.completed: List[Request] = []
         self._held: Dict[int, Request] = {}
         self._ids = itertools.count()
@@ -283,6 +282,14 @@ class Server:
     def _check(name, rc):
         if rc != _native.SB_OK:
             raise _native.SbError(name, rc, _native.last_error())
+
+    @property
+    def pool(self) -> _PoolView:
+        return _PoolView(self)
+
+    def close(self):
+        """Wait for the device work and free the server's region now."""
+        self._finalizer()
 
     # -- client side ------------------------------------------------------------
 
