@@ -2,7 +2,8 @@
 
     python profile_cases.py [--warmup W] [--launches L] CASE...
 
-CASE is ``<stencil>-<form>[:<variant>]`` with stencil in hdiff, vadv, triad, copy, lap and
+CASE is ``<stencil>-<form>[:<variant>[@<placement>]]`` with stencil in hdiff, vadv, vadv3 (all
+three components, one launch each on a shared wcon), triad, copy, lap and
 form in f64, f32, bf16 (bf16 = bfloat16 storage, f32 compute), f32x2
 (float64 storage, float-pair compute) and fix64 (float64 storage, hdiff only,
 fixed-point sums); ``all`` runs every hdiff/vadv form plus triad-f64.  Stencil cases use the 512 x 512 x 80
@@ -14,7 +15,8 @@ library, except vadv-f64 and vadv-f32x2, which use the caller-scratch
 (GLOBAL) variant as ``bench.py`` does.  ``:<variant>`` picks another one
 (hdiff: tile, jscan, tma, vscan -- tma with rows padded to 64 bytes so that the
 j/k strides suit the tensor copies; vadv: smem, global, slab, wslab, tmem -- global,
-slab and wslab with ccol/dcol scratch fields).
+slab and wslab with ccol/dcol scratch fields); ``@<placement>`` sets the float64
+integer-pipe placement preset (sb_tune.flags bits 4-7) of tma and slab.
 """
 
 from __future__ import annotations
@@ -59,6 +61,8 @@ VARIANTS = {"tile": _native.HDIFF_TILE, "jscan": _native.HDIFF_JSCAN, "tma": _na
 
 def run_case(name, warmup, launches, rng):
     name, _, variant = name.partition(":")
+    variant, _, placement = variant.partition("@")
+    flags = int(placement) << 4 if placement else 0
     stencil, form = name.split("-")
     if stencil == "triad":
         n = 1 << 27
@@ -74,7 +78,7 @@ def run_case(name, warmup, launches, rng):
             align = 64 if variant == "tma" else 0
             f = [_field(rng, storage, (2, 2, 0), 0.0, 1.0, align) for _ in range(3)]
 
-            htune = _native.tune(variant=VARIANTS[variant]) if variant else None
+            htune = _native.tune(variant=VARIANTS[variant], flags=flags) if variant else None
 
             def launch(timed):
                 return kernels.hdiff(*f, compute=compute, tune=htune, timed=timed)
@@ -89,8 +93,9 @@ def run_case(name, warmup, launches, rng):
                 scratch = {"ccol": _field(rng, scratch_storage, (1, 1, 0), 0.0, 0.0),
                            "dcol": _field(rng, scratch_storage, (1, 1, 0), 0.0, 0.0)}
             if variant == "slab":  # the bench's tunings for f64 and f32x2
-                slab = {"f64": (32, 4, 8), "f32x2": (64, 2, 32)}.get(form, (64, 4, 16))
-                tune = _native.tune(variant=_native.VADV_SLAB, block_x=slab[0], unroll=slab[1], k_per_cta=slab[2])
+                slab = {"f64": (32, 4, 24), "f32x2": (64, 2, 32)}.get(form, (64, 4, 16))
+                tune = _native.tune(variant=_native.VADV_SLAB, block_x=slab[0], unroll=slab[1], k_per_cta=slab[2],
+                                    flags=flags)
             elif variant:
                 tune = _native.tune(variant=VARIANTS[variant])
             elif form in ("f64", "f32x2"):
@@ -99,6 +104,17 @@ def run_case(name, warmup, launches, rng):
 
             def launch(timed):
                 return kernels.vadv(*f, out=out, compute=compute, tune=tune, timed=timed, **scratch)
+        elif stencil == "vadv3":  # all components: u, v, w on one wcon field, three launches
+            comps = [[_field(rng, storage, (1, 1, 1), -1.0, 1.0) for _ in range(4)] for _ in range(3)]
+            wcon = _field(rng, storage, (1, 1, 1), -0.5, 0.5)
+            outs = [_field(rng, storage, (1, 1, 1), 0.0, 0.0) for _ in range(3)]
+
+            def launch(timed):
+                total = 0.0
+                for f, o, shift in zip(comps, outs, ((1, 0), (0, 1), (0, 0))):
+                    t = kernels.vadv(*f, wcon, shift, out=o, compute=compute, timed=timed)
+                    total += t or 0.0
+                return total
         elif stencil in ("copy", "lap"):
             f = [_field(rng, storage, (1, 1, 1), 0.0, 1.0) for _ in range(2)]
 
