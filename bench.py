@@ -460,8 +460,12 @@ def run_gpu(args, dist):
         sl = tuple(slice(h, h + n) for h, n in zip(halo, (NI, NJ, NK)))
         a, b = a[sl], b[sl]
         scale = float(np.max(np.abs(a)))
+        big = np.abs(a) >= 1e-2 * np.sqrt(np.mean(a * a))
+        pointwise = np.abs(a - b)[big] / np.abs(a)[big]
         fast["err_" + name] = {"max_abs_over_scale": float(np.max(np.abs(a - b))) / scale,
-                               "rms_rel": float(np.sqrt(np.mean((a - b) ** 2)) / np.sqrt(np.mean(a * a)))}
+                               "rms_rel": float(np.sqrt(np.mean((a - b) ** 2)) / np.sqrt(np.mean(a * a))),
+                               "p99_pointwise_rel": float(np.percentile(pointwise, 99)),
+                               "p999_pointwise_rel": float(np.percentile(pointwise, 99.9))}
 
     # ---- STREAM triad calibration (outside the timed region)
     triad = None
@@ -920,7 +924,10 @@ def main(argv=None):
         fh, fv = statistics.mean(fast["t_hdiff"]), statistics.mean(fast["t_vadv"])
         line["fast_f64"] = {
             "what": "same step and inputs; hdiff fixed-point sums + one fp64 FMA (fp64 rounding level), vadv "
-                    "float-pair arithmetic (~48-bit significand); not bit-identical to the reference",
+                    "float-pair arithmetic (~48-bit significand); not bit-identical to the reference, and the "
+                    "float-pair vadv is not held to 1e-10 of the field scale in near-singular columns (errors "
+                    "against the exact step: max |err| / max |exact| and pointwise relative p99 / p99.9 over "
+                    "|exact| >= 1e-2 rms)",
             "value": 2 * POINTS * args.steps * dist.world / fast["elapsed"] / 1e9, "unit": UNIT,
             "ms_per_step": fast["elapsed"] / args.steps * 1e3,
             "hdiff": {"compute": FAST_HDIFF_COMPUTE, "ms": fh * 1e3, "gpoints_s": POINTS / fh / 1e9,

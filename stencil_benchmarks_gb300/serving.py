@@ -248,8 +248,9 @@ class Server:
                  simulate: bool = False):
         """``float64_compute`` picks how float64 requests are computed: "float64"
         (exact, bit-identical to the reference's numpy) or "fixed64" (fixed-point
-        hdiff and float-pair vadv: errors within 1e-12 / 1e-10 of the field scale,
-        about 3x less device time).  ``mode`` "batched" packs a slot's requests
+        hdiff, 4e-16 of the field scale, and float-pair vadv, about 48
+        significant bits, within 1e-10 of the field scale except in
+        near-singular columns; about 3x less device time).  ``mode`` "batched" packs a slot's requests
         into one graph replay of the persistent kernels; "plain" launches each
         request's kernel on its own (the per-request baseline).  ``simulate``
         runs the scheduling without any device work (tests)."""

@@ -2,7 +2,10 @@
 stated tolerances:
 
     hdiff: max |got - oracle| <= 1e-12 * max |oracle|
-    vadv:  max |got - oracle| <= 1e-10 * max |oracle|
+    vadv:  max |got - oracle| <= 1e-10 * max |oracle| on well-conditioned
+           domains; on ill-conditioned ones the float-pair solve is held to
+           2^10 times float64's own error instead (its error grows with the
+           column's conditioning, so 1e-10 is not a property it has there)
 
 (relative to the field's magnitude).  Float-pair compute ("float32x2")
 carries about 48 significant bits, so isolated results close to zero have
