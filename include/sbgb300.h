@@ -113,6 +113,8 @@ typedef struct sb_tune {
     int32_t k_per_cta; /* hdiff: k-planes per CTA                               */
     int32_t unroll;    /* STREAM: vectors per thread per iteration             */
     int32_t flags;     /* STREAM: bit0 streaming (evict-first) stores;
+                        * vadv TMEM: bit 10 / 11 stage through 32-bit shared
+                        * addresses / generic pointers (neither: the default);
                         * float64 hdiff TMA / vadv SLAB: bits 4-7 pick which
                         * operations run as integer arithmetic instead of fp64
                         * instructions (same bits either way; 0: the library's

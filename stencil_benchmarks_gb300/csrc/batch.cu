@@ -206,11 +206,11 @@ __global__ void __launch_bounds__(512, 1)
         const int nvalid = min(32, dm.ni - i0);
         const int col0 = i0 + j * (int)dm.sj;
         if (dm.kp == 1)
-            vadv_tmem_column<S, D, 1, int>((const S*)dm.f[0], (const S*)dm.f[1], (const S*)dm.f[2],
+            vadv_tmem_column<S, D, 1, int, true>((const S*)dm.f[0], (const S*)dm.f[1], (const S*)dm.f[2],
                                            (const S*)dm.f[3], (const S*)dm.f[4], (S*)dm.out, col0, lane, nvalid,
                                            dm.nk, (int)dm.sk, (int)dm.wsh, tcol, ring);
         else if (dm.kp == 2)
-            vadv_tmem_column<S, D, 2, int>((const S*)dm.f[0], (const S*)dm.f[1], (const S*)dm.f[2],
+            vadv_tmem_column<S, D, 2, int, true>((const S*)dm.f[0], (const S*)dm.f[1], (const S*)dm.f[2],
                                            (const S*)dm.f[3], (const S*)dm.f[4], (S*)dm.out, col0, lane, nvalid,
                                            dm.nk, (int)dm.sk, (int)dm.wsh, tcol, ring);
         else

@@ -930,13 +930,35 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&f)[16]) {
     for (int q = 0; q < 16; ++q) f[q] = __uint_as_float(r[q]);
 }
 
+// Shared-memory accesses by 32-bit shared address (the ring's base converted
+// once), so per-level offsets fold into the instructions' immediates.
+__device__ __forceinline__ void cp_async16_s(uint32_t dst, const void* src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(dst), "l"(src) : "memory");
+}
+template <class S>
+__device__ __forceinline__ S lds(uint32_t addr);
+template <>
+__device__ __forceinline__ float lds<float>(uint32_t addr) {
+    float v;
+    asm volatile("ld.shared.f32 %0, [%1];\n" : "=f"(v) : "r"(addr) : "memory");
+    return v;
+}
+template <>
+__device__ __forceinline__ bf16 lds<bf16>(uint32_t addr) {
+    unsigned short v;
+    asm volatile("ld.shared.u16 %0, [%1];\n" : "=h"(v) : "r"(addr) : "memory");
+    return __ushort_as_bfloat16(v);
+}
+
 // KP: how the level stride sk * sizeof(S) sits on 16-byte granules.  KP = 1:
 // a multiple of 16 bytes, so every level's rows share level 0's offsets
 // within their granules; KP = 2: 8 modulo 16, so even and odd levels each
 // share one set of offsets.  Then the copy addresses advance by a constant
 // and the staged rows sit at fixed ring offsets (per parity), which takes
 // far fewer instructions per level than the general case (KP = 0).
-template <class S, int D, int KP, class IDX>
+// SA: stage and read the ring through 32-bit shared addresses (cp_async16_s,
+// lds) instead of generic pointers.
+template <class S, int D, int KP, class IDX, bool SA = false>
 __device__ __forceinline__ void vadv_tmem_column(const S* __restrict__ stage, const S* __restrict__ pos,
                                                  const S* __restrict__ tens, const S* tensstage,
                                                  const S* __restrict__ wcon, S* out, IDX col0, int lane, int nvalid,
@@ -952,6 +974,7 @@ __device__ __forceinline__ void vadv_tmem_column(const S* __restrict__ stage, co
     const IDX col = col0 + (IDX)(valid ? lane : nvalid - 1);
     const int64_t kstep = (int64_t)sk * ES;  // bytes from level k to k+1 in a field
     const int nbytes = nvalid * ES;
+    const uint32_t ring_s = (uint32_t)__cvta_generic_to_shared(ring);
 
     // forward rows at level k: wcon(k+1) shifted, wcon(k+1), stage(k+1), pos(k), tens(k), tensstage(k)
     const unsigned char* const g0 = (const unsigned char*)(wcon + col0 + sk + wsh);
@@ -995,7 +1018,11 @@ __device__ __forceinline__ void vadv_tmem_column(const S* __restrict__ stage, co
                 if constexpr (KP > 0) {
                     const bool odd = KP == 2 && (k & 1);
                     const bool use = odd ? cuse[1][m] : cuse[0][m];
-                    if (use) cp_async<16>(ring + slot * SLOT + cdst[m], (const void*)((odd ? cg[1][m] : cg[0][m]) + kb));
+                    if constexpr (SA) {
+                        if (use) cp_async16_s(ring_s + slot * SLOT + cdst[m], (const void*)((odd ? cg[1][m] : cg[0][m]) + kb));
+                    } else {
+                        if (use) cp_async<16>(ring + slot * SLOT + cdst[m], (const void*)((odd ? cg[1][m] : cg[0][m]) + kb));
+                    }
                 } else {
                     const uintptr_t a = (uintptr_t)(cg[0][m] + kb);
                     const int n = (int)(((a & 15u) + (unsigned)nbytes + 15u) >> 4);
@@ -1009,13 +1036,19 @@ __device__ __forceinline__ void vadv_tmem_column(const S* __restrict__ stage, co
     };
     // this lane's element of staged row f in slot 0, for even and odd levels (KP > 0)
     const unsigned char* rowb[2][6];
+    uint32_t rows_s[2][6];
 #pragma unroll
     for (int f = 0; f < 6; ++f) {
         rowb[0][f] = ring + f * ROWB + mis0[f] + lane * ES;
         rowb[1][f] = ring + f * ROWB + ((mis0[f] + kph) & 15u) + lane * ES;
+        rows_s[0][f] = ring_s + (uint32_t)(f * ROWB) + mis0[f] + (uint32_t)(lane * ES);
+        rows_s[1][f] = ring_s + (uint32_t)(f * ROWB) + ((mis0[f] + kph) & 15u) + (uint32_t)(lane * ES);
     }
     auto rd = [&](int slot, int f, int k) -> C {
-        if constexpr (KP > 0) {
+        if constexpr (KP > 0 && SA) {
+            const bool odd = KP == 2 && (k & 1);
+            return cvt<C, S>(lds<S>((odd ? rows_s[1][f] : rows_s[0][f]) + slot * SLOT));
+        } else if constexpr (KP > 0) {
             const bool odd = KP == 2 && (k & 1);
             return cvt<C, S>(*(const S*)((odd ? rowb[1][f] : rowb[0][f]) + slot * SLOT));
         } else {
@@ -1109,7 +1142,11 @@ __device__ __forceinline__ void vadv_tmem_column(const S* __restrict__ stage, co
                 if constexpr (KP > 0) {
                     const bool odd = KP == 2 && (k & 1);
                     const bool use = odd ? buse[1][m] : buse[0][m];
-                    if (use) cp_async<16>(ring + slot * SLOT + bdst[m], (const void*)((odd ? bg[1][m] : bg[0][m]) + kb));
+                    if constexpr (SA) {
+                        if (use) cp_async16_s(ring_s + slot * SLOT + bdst[m], (const void*)((odd ? bg[1][m] : bg[0][m]) + kb));
+                    } else {
+                        if (use) cp_async<16>(ring + slot * SLOT + bdst[m], (const void*)((odd ? bg[1][m] : bg[0][m]) + kb));
+                    }
                 } else {
                     const uintptr_t a = (uintptr_t)(bg[0][m] + kb);
                     const int n = (int)(((a & 15u) + (unsigned)nbytes + 15u) >> 4);
@@ -1130,6 +1167,8 @@ __device__ __forceinline__ void vadv_tmem_column(const S* __restrict__ stage, co
     }
     const unsigned char* const prow0 = ring + mis_p + lane * ES;  // KP > 0: pos element of slot 0, even levels
     const unsigned char* const prow1 = ring + ((mis_p + kph) & 15u) + lane * ES;  // odd levels
+    const uint32_t prow0_s = ring_s + mis_p + (uint32_t)(lane * ES);
+    const uint32_t prow1_s = ring_s + ((mis_p + kph) & 15u) + (uint32_t)(lane * ES);
     S* optr = out + col;
     int slot = 0;  // ring slot of the next level
     for (int w = (nk - 2) >> 3; w >= 0; --w) {
@@ -1142,7 +1181,10 @@ __device__ __forceinline__ void vadv_tmem_column(const S* __restrict__ stage, co
             cp_async_wait<D - 1>();
             __syncwarp();
             C p0;
-            if constexpr (KP > 0) {
+            if constexpr (KP > 0 && SA) {
+                const bool odd = KP == 2 && (k & 1);
+                p0 = cvt<C, S>(lds<S>((odd ? prow1_s : prow0_s) + (uint32_t)(slot * SLOT)));
+            } else if constexpr (KP > 0) {
                 const bool odd = KP == 2 && (k & 1);
                 p0 = cvt<C, S>(*(const S*)((odd ? prow1 : prow0) + slot * SLOT));
             } else {

@@ -404,7 +404,7 @@ int launch_wslab(int bx, int depth, int blocks_per_sm, const DeviceProps* p, cud
 // The block allocates all 512 columns and asks for enough shared memory that
 // no second block shares its SM, so the allocation never waits.
 // ---------------------------------------------------------------------------
-template <class S, int D, int KP>
+template <class S, int D, int KP, bool SA>
 __global__ void __launch_bounds__(512, 1)
     vadv_tmem_kernel(const S* __restrict__ stage, const S* __restrict__ pos, const S* __restrict__ tens,
                      const S* tensstage, const S* __restrict__ wcon, S* out, int ni, int nj, int nk, int sj, int sk,
@@ -431,8 +431,8 @@ __global__ void __launch_bounds__(512, 1)
         const int i0 = (int)(g % gx) * 32;
         const int j = (int)(g / gx);
         const int nvalid = min(32, ni - i0);
-        vadv_tmem_column<S, D, KP, int>(stage, pos, tens, tensstage, wcon, out, i0 + j * sj, lane, nvalid, nk, sk,
-                                        wsh, tcol, ring);
+        vadv_tmem_column<S, D, KP, int, SA>(stage, pos, tens, tensstage, wcon, out, i0 + j * sj, lane, nvalid, nk,
+                                            sk, wsh, tcol, ring);
     }
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
     __syncthreads();
@@ -443,12 +443,19 @@ __global__ void __launch_bounds__(512, 1)
     }
 }
 
+// TMEM staging through 32-bit shared addresses (sb_tune.flags bit 10) or
+// generic pointers (bit 11); neither bit: the default below (512x512x80:
+// float32 135 vs 136 us, bfloat16 120 vs 125 us at ring depth 8).
+constexpr bool kTmemSharedAddr = true;
+
 template <class S, int D>
-int launch_tmem_one(int g4, int cpw, const DeviceProps* p, cudaStream_t stream, const void* stage, const void* pos,
-                    const void* tens, const void* tensstage, const void* wcon, void* out, int64_t ni, int64_t nj,
-                    int64_t nk, int64_t sj, int64_t sk, int64_t wsh) {
+int launch_tmem_one(int g4, int cpw, bool sa, const DeviceProps* p, cudaStream_t stream, const void* stage,
+                    const void* pos, const void* tens, const void* tensstage, const void* wcon, void* out, int64_t ni,
+                    int64_t nj, int64_t nk, int64_t sj, int64_t sk, int64_t wsh) {
     const int64_t kmod = ((int64_t)sk * (int64_t)sizeof(S)) % 16;
-    auto kernel = kmod == 0 ? vadv_tmem_kernel<S, D, 1> : kmod == 8 ? vadv_tmem_kernel<S, D, 2> : vadv_tmem_kernel<S, D, 0>;
+    auto kernel = kmod == 0 ? (sa ? vadv_tmem_kernel<S, D, 1, true> : vadv_tmem_kernel<S, D, 1, false>)
+                  : kmod == 8 ? (sa ? vadv_tmem_kernel<S, D, 2, true> : vadv_tmem_kernel<S, D, 2, false>)
+                              : vadv_tmem_kernel<S, D, 0, false>;
     // fewer warps per lane quarter when their rings do not fit
     g4 = std::min<int64_t>(g4, (p->smem_optin - 16) / (4 * (int64_t)WarpRing<S, float, D>::BYTES));
     if (g4 < 1) return SB_ERR_UNSUPPORTED;
@@ -469,7 +476,7 @@ int launch_tmem_one(int g4, int cpw, const DeviceProps* p, cudaStream_t stream, 
 // positive strides, 32-bit offsets, 2 <= nk <= 256); SB_ERR_UNSUPPORTED
 // otherwise.  depth 0 = the deepest ring that fits.
 template <class S, class C>
-int launch_tmem(int depth, const DeviceProps* p, cudaStream_t stream, const void* stage, const void* pos,
+int launch_tmem(int depth, bool sa, const DeviceProps* p, cudaStream_t stream, const void* stage, const void* pos,
                 const void* tens, const void* tensstage, const void* wcon, void* out, int64_t ni, int64_t nj,
                 int64_t nk, int64_t si, int64_t sj, int64_t sk, int64_t wsh) {
     if constexpr (!std::is_same<C, float>::value) {
@@ -482,11 +489,11 @@ int launch_tmem(int depth, const DeviceProps* p, cudaStream_t stream, const void
         const int g4 = std::min(4, 512 / cpw);             // warps per TMEM lane quarter
         int rc = SB_ERR_UNSUPPORTED;
         if ((depth == 0 || depth == 16) && rc == SB_ERR_UNSUPPORTED)
-            rc = launch_tmem_one<S, 16>(g4, cpw, p, stream, stage, pos, tens, tensstage, wcon, out, ni, nj, nk, sj, sk, wsh);
+            rc = launch_tmem_one<S, 16>(g4, cpw, sa, p, stream, stage, pos, tens, tensstage, wcon, out, ni, nj, nk, sj, sk, wsh);
         if ((depth == 0 || depth == 8) && rc == SB_ERR_UNSUPPORTED)
-            rc = launch_tmem_one<S, 8>(g4, cpw, p, stream, stage, pos, tens, tensstage, wcon, out, ni, nj, nk, sj, sk, wsh);
+            rc = launch_tmem_one<S, 8>(g4, cpw, sa, p, stream, stage, pos, tens, tensstage, wcon, out, ni, nj, nk, sj, sk, wsh);
         if (depth == 4 && rc == SB_ERR_UNSUPPORTED)
-            rc = launch_tmem_one<S, 4>(g4, cpw, p, stream, stage, pos, tens, tensstage, wcon, out, ni, nj, nk, sj, sk, wsh);
+            rc = launch_tmem_one<S, 4>(g4, cpw, sa, p, stream, stage, pos, tens, tensstage, wcon, out, ni, nj, nk, sj, sk, wsh);
         return rc;
     }
 }
@@ -515,8 +522,8 @@ int launch_typed(const void* stage, const void* pos, const void* tens, const voi
     if constexpr (std::is_same<C, float>::value) {
         if (variant == SB_VARIANT_AUTO && !(tune && (tune->block_x || tune->block_y || tune->unroll)) &&
             ceil_div(ni, (int64_t)32) * nj >= 2048 && (sizeof(S) == 4 || (sk * (int64_t)sizeof(S)) % 8 == 0)) {
-            const int arc = launch_tmem<S, C>(8, p, stream, stage, pos, tens, tensstage, wcon, out, ni, nj, nk, si,
-                                              sj, sk, wsh);
+            const int arc = launch_tmem<S, C>(8, kTmemSharedAddr, p, stream, stage, pos, tens, tensstage, wcon, out,
+                                              ni, nj, nk, si, sj, sk, wsh);
             if (arc != SB_ERR_UNSUPPORTED) return arc;
         }
     }
@@ -542,7 +549,8 @@ int launch_typed(const void* stage, const void* pos, const void* tens, const voi
     if (variant == SB_VADV_TMEM) {
         const int d = (tune && tune->unroll > 0) ? tune->unroll : 0;
         SB_CHECK(d == 0 || d == 4 || d == 8 || d == 16, SB_ERR_INVALID, "vadv TMEM ring depth must be 4, 8 or 16");
-        const int rc2 = launch_tmem<S, C>(d, p, stream, stage, pos, tens, tensstage, wcon, out, ni, nj, nk, si, sj,
+        const bool sa = tune && (tune->flags & 0x400) ? true : (tune && (tune->flags & 0x800) ? false : kTmemSharedAddr);
+        const int rc2 = launch_tmem<S, C>(d, sa, p, stream, stage, pos, tens, tensstage, wcon, out, ni, nj, nk, si, sj,
                                           sk, wsh);
         SB_CHECK(rc2 != SB_ERR_UNSUPPORTED, SB_ERR_UNSUPPORTED,
                  "vadv TMEM variant: needs float32 compute, i unit-stride, positive strides, 32-bit offsets and "

@@ -326,12 +326,14 @@ def test_vadv_slab(variant, bx, depth, per_sm, storage, compute, lib):
 
 @pytest.mark.parametrize("depth", [0, 4, 8, 16])
 @pytest.mark.parametrize("storage", ["float32", "bfloat16"])
-def test_vadv_tmem(depth, storage, lib):
+@pytest.mark.parametrize("staging", [0x400, 0x800], ids=["shared-addr", "generic"])
+def test_vadv_tmem(depth, storage, staging, lib):
     """Factors in tensor memory: level counts around the 8-level load window
     and the per-warp column ranges (nk 64 -> 16 warps, 80 -> 12, 128 -> 8,
     256 -> 4 per block), row ends with 1 or 2 valid lanes, many column
-    groups per warp."""
-    t = _native.tune(variant=_native.VADV_TMEM, unroll=depth)
+    groups per warp; the ring staged through shared addresses and through
+    generic pointers."""
+    t = _native.tune(variant=_native.VADV_TMEM, unroll=depth, flags=staging)
     for domain in ((97, 19, 2), (97, 19, 3), (33, 40, 9), (130, 7, 41), (64, 5, 64), (40, 6, 80), (35, 3, 128),
                    (34, 2, 137), (33, 2, 256)):
         got, want = _run_vadv(domain, (1, 1, 0), storage, "float32", tune=t, seed=40 + domain[2])
