@@ -106,7 +106,7 @@ __global__ void __launch_bounds__(256)
 // factors live in the bucket's slab workspace instead (level k of thread slot
 // q at slab[k * nslots + q], dcol after cap * nslots ccol entries) and the
 // shared memory is the ring only, so many more blocks fit per SM.
-template <class S, class C, int BT, int D, class IDX, class P = C, bool SLAB = false>
+template <class S, class C, int BT, int D, class IDX, class P = C, bool SLAB = false, uint32_t PL = 0u>
 __global__ void __launch_bounds__(BT)
     batch_vadv_kernel(const DevTable* __restrict__ tab, unsigned long long* __restrict__ counter, int bucket,
                       int cap, int ring_offset, P* __restrict__ slab) {
@@ -145,7 +145,7 @@ __global__ void __launch_bounds__(BT)
         if (i < dm.ni) {
             const IDX col = (IDX)i * (IDX)dm.si + (IDX)j * (IDX)dm.sj;
             if constexpr (SLAB) {
-                vadv_async_column<S, C, BT, D, IDX, true, P>((const S*)dm.f[0], (const S*)dm.f[1],
+                vadv_async_column<S, C, BT, D, IDX, true, P, PL>((const S*)dm.f[0], (const S*)dm.f[1],
                                                              (const S*)dm.f[2], (const S*)dm.f[3],
                                                              (const S*)dm.f[4], (S*)dm.out, col, dm.nk,
                                                              (IDX)dm.sk, (IDX)dm.wsh, sc, sc + (int64_t)cap * nslots,
@@ -236,6 +236,7 @@ struct Kinds {
     const void* vadv32_fn;
     const void* vadv64_fn;
     int storage_bytes, compute_bytes;
+    bool int_products;  // float64 slab buckets run their products in integer arithmetic
     // float32 vadv with factors in tensor memory (nullptr for other compute types)
     void (*vadv_tmem)(dim3, dim3, size_t, cudaStream_t, const DevTable*, unsigned long long*, int, int);
     const void* vadv_tmem_fn;
@@ -246,11 +247,11 @@ template <class S, class C, int U, class IDX>
 void run_hdiff(dim3 g, dim3 b, cudaStream_t s, const DevTable* t, unsigned long long* c) {
     batch_hdiff_kernel<S, C, U, IDX><<<g, b, 0, s>>>(t, c);
 }
-template <class S, class C, int BT, class IDX, class P, bool SLAB>
+template <class S, class C, int BT, class IDX, class P, bool SLAB, uint32_t PL>
 void run_vadv(dim3 g, dim3 b, size_t smem, cudaStream_t s, const DevTable* t, unsigned long long* c, int bucket,
               int cap, int ring_offset, void* slab) {
-    batch_vadv_kernel<S, C, BT, kVadvDepth, IDX, P, SLAB><<<g, b, smem, s>>>(t, c, bucket, cap, ring_offset,
-                                                                             (P*)slab);
+    batch_vadv_kernel<S, C, BT, kVadvDepth, IDX, P, SLAB, PL><<<g, b, smem, s>>>(t, c, bucket, cap, ring_offset,
+                                                                                 (P*)slab);
 }
 
 template <class S>
@@ -269,10 +270,15 @@ Kinds kinds_for() {
                           !(std::is_same<S, float>::value && std::is_same<P, float>::value);
     k.slab = SLAB;
     k.hdiff = &run_hdiff<S, HC, U, IDX>;
-    k.vadv32 = &run_vadv<S, VC, 32, IDX, P, SLAB>;
-    k.vadv64 = &run_vadv<S, VC, 64, IDX, P, SLAB>;
-    k.vadv32_fn = (const void*)&batch_vadv_kernel<S, VC, 32, kVadvDepth, IDX, P, SLAB>;
-    k.vadv64_fn = (const void*)&batch_vadv_kernel<S, VC, 64, kVadvDepth, IDX, P, SLAB>;
+    // float64 slab buckets: the products on the integer pipe (more blocks per SM, below)
+    constexpr uint32_t PL = SLAB && std::is_same<P, double>::value && std::is_same<VC, double>::value
+                                ? kVadvProductSites
+                                : 0u;
+    k.int_products = PL != 0u;
+    k.vadv32 = &run_vadv<S, VC, 32, IDX, P, SLAB, PL>;
+    k.vadv64 = &run_vadv<S, VC, 64, IDX, P, SLAB, PL>;
+    k.vadv32_fn = (const void*)&batch_vadv_kernel<S, VC, 32, kVadvDepth, IDX, P, SLAB, PL>;
+    k.vadv64_fn = (const void*)&batch_vadv_kernel<S, VC, 64, kVadvDepth, IDX, P, SLAB, PL>;
     k.storage_bytes = sizeof(typename RingOf<S>::T);  // ring entry
     k.compute_bytes = sizeof(P);                      // factor entry
     if constexpr (std::is_same<VC, float>::value && std::is_same<P, float>::value && std::is_same<IDX, int>::value) {
@@ -475,9 +481,11 @@ int sb_batch_create(sb_batch** out, int storage, int compute, int max_domains, i
                         "use a smaller max_nk or vadv block",
                         (long long)max_nk, need, p->smem_optin);
         }
-        const int fit = (int)std::min<int64_t>(16, (p->smem_optin + 1024) / (int64_t)(b->vadv_smem[q] + 1024));
-        // slab mode: 8 blocks per SM by default (the slabs grow with the grid)
-        const int vdef = k.slab ? std::min(fit, 8) : fit;
+        const int fit = (int)std::min<int64_t>(k.int_products ? 24 : 16,
+                                               (p->smem_optin + 1024) / (int64_t)(b->vadv_smem[q] + 1024));
+        // slab mode: 8 blocks per SM by default (the slabs grow with the grid);
+        // 16 with the products in integer arithmetic, which need more warps in flight
+        const int vdef = k.slab ? std::min(fit, k.int_products ? 16 : 8) : fit;
         const int vper = b->tune.vadv_blocks_per_sm > 0 ? std::min(b->tune.vadv_blocks_per_sm, fit) : vdef;
         b->vadv_grid[q] = p->sm_count * std::max(1, vper);
     }

@@ -549,6 +549,11 @@ __device__ __forceinline__ C from_ring(T w, uint32_t sel) {
 //                 0 and 1 of a slot; needs ring entries of the compute size).
 // Every shared-memory address below is a per-thread base plus a
 // compile-time offset.
+// The nine products of a vadv level (sites 4, 5, 7, 11, 13, 14, 16, 17, 20 of
+// vadv_async_column): the placement that pays on the integer pipe.
+constexpr uint32_t kVadvProductSites = (1u << 4) | (1u << 5) | (1u << 7) | (1u << 11) | (1u << 13) | (1u << 14) |
+                                       (1u << 16) | (1u << 17) | (1u << 20);
+
 // PL: integer-pipe placement mask over the operation sites 0-20 below (Mix).
 template <class S, class C, int BT, int D, class IDX, bool SLAB = false, class P = C, uint32_t PL = 0u>
 __device__ __forceinline__ void vadv_async_column(const S* __restrict__ stage, const S* __restrict__ pos,

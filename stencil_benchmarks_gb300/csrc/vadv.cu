@@ -72,7 +72,8 @@ constexpr uint32_t vadv_sites(std::initializer_list<int> ks) {
     for (int k : ks) m |= 1u << k;
     return m;
 }
-constexpr uint32_t kVadvMuls = vadv_sites({4, 5, 7, 11, 13, 14, 16, 17, 20});
+constexpr uint32_t kVadvMuls = kVadvProductSites;
+static_assert(kVadvMuls == vadv_sites({4, 5, 7, 11, 13, 14, 16, 17, 20}), "the nine products");
 constexpr uint32_t kVadvPlacements[] = {
     0u,
     0u,
