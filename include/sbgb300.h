@@ -186,6 +186,14 @@ int sb_l2_flush(void* stream);
 #define SB_STREAM_SCALE 2
 #define SB_STREAM_ADD 3
 #define SB_STREAM_TRIAD 4
+/* tune->variant picks the grid: SB_STREAM_GRID_STRIDE, a few blocks per SM
+ * striding over the arrays (block_x <= 512, default 512 threads x 4 vectors);
+ * SB_STREAM_GRID_CHUNK, one block per block_x * unroll 16-byte vectors
+ * (block_x <= 1024, default 1024 x 2); 0: the library's choice (chunks;
+ * 2^29-element float64 arrays: 7.2-7.3 TB/s against 6.8-6.9 striding).  tune->flags
+ * bit0: streaming (evict-first) stores.                                    */
+#define SB_STREAM_GRID_STRIDE 1
+#define SB_STREAM_GRID_CHUNK 2
 int sb_stream_op(int op, int dtype, void* a, void* b, void* c, double scalar, int64_t n,
                  const sb_tune* tune, void* stream, double* time_s);
 
@@ -194,7 +202,17 @@ int sb_stream_op(int op, int dtype, void* a, void* b, void* c, double scalar, in
 int sb_copy(int storage, const void* inp, void* out, int64_t ni, int64_t nj, int64_t nk,
             int64_t si, int64_t sj, int64_t sk, const sb_tune* tune, void* stream,
             double* time_s);
-/* along_mask: bit0 x, bit1 y, bit2 z (LaplacianStencil along_x/y/z) */
+/* along_mask: bit0 x, bit1 y, bit2 z (LaplacianStencil along_x/y/z).
+ * tune->variant: SB_BASIC_POINT, one thread per point and 4 k-planes
+ * (block_x x block_y threads, default 128 x 2); SB_BASIC_MARCH, lanes along i,
+ * each thread holding a strip of tile_y rows of j for k_per_cta k-planes in
+ * registers (4 or 8 rows x 2 planes; default 4 x 2) with block_y warps per
+ * block (default 4); float64 along x and y: flags bits 4-7 pick which
+ * subtractions run as integer arithmetic (0: the library's default, 1: all
+ * fp64, 2-4: other splits); variant 0: the library's choice (the strips;
+ * along_mask 0 always runs the point kernel).  Same bits from every variant. */
+#define SB_BASIC_POINT 1
+#define SB_BASIC_MARCH 2
 int sb_laplacian(int storage, int compute, const void* inp, void* out, int64_t ni, int64_t nj,
                  int64_t nk, int64_t si, int64_t sj, int64_t sk, int along_mask,
                  const sb_tune* tune, void* stream, double* time_s);

@@ -1,0 +1,292 @@
+"""The reference's own CUDA kernels and this package's kernels, timed on the
+same GPU through the same Benchmark API.
+
+    python reference_gpu.py [--dtypes float64,float32] [--runs 5] [--only hdiff,vadv,basic,stream]
+
+Reference side: the cuda_hip backend exactly as the reference ships it -- each
+class renders its template and compiles it with nvcc (`-arch sm_103a`) in
+`setup`, allocates device copies and times one launch with CUDA events after
+`dry_runs` untimed ones (stencils/cuda_hip/mixin.py:60-175,
+templates/base.j2:68-193); launch shapes are the ones the reference's own
+tuned collection uses (scripts/sbench_h100_collection.py:59-152).  This side:
+the gb300 classes with their library defaults, same domain, halo, alignment,
+seeded inputs and timer rule (one launch after one dry run).  Every case's
+first run is verified by the reference's own `verify_stencil`; the median of
+the remaining runs is reported, and a side's best case is its fastest
+verified one (its fastest unverified one, marked so, when none passed).
+
+Cases left out or resized, from reading their kernels:
+  * hdiff JScanOtfIncache: its halo threads return before a __syncthreads
+    (horizontal_diffusion_jscanotfincache.j2:72-75); not run.
+  * hdiff JScanShuffle: where ni is not a multiple of 28 the threads past the
+    edge return before the warp's full-mask shuffles
+    (horizontal_diffusion_jscanshuffle.j2:50-51); run on 504 x 512 x 80
+    (18 blocks of 28 columns), where none returns.
+  * vadv SharedMem in float64 with 64-thread blocks needs 80 KB of static
+    shared memory; float64 runs it with 32-thread blocks.
+  * vadv reads and writes utensstage, so a dry run before the timed launch
+    changes the input that verification assumes: the vadv cases (both sides)
+    run without dry runs; every run after the first is warm all the same.
+
+Prints one JSON line per case and a final summary line.  Needs the
+reference package importable (baseline/_ref or $SBGB300_REFERENCE), jinja2,
+nvcc and libcudart.so on the loader path.
+"""
+from __future__ import annotations
+
+import argparse
+import contextlib
+import ctypes
+import gc
+import glob
+import json
+import os
+import shutil
+import statistics
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+DOMAIN = (512, 512, 80)
+HALO = (3, 3, 3)  # the reference's default halo
+BASIC_HALO = (1, 1, 1)
+ALIGNMENT = 128
+SHUFFLE_DOMAIN = (504, 512, 80)
+STREAM_N = 2 ** 29
+
+# (class name, kwargs) per reference cuda_hip module, from the reference's tuned collection
+REF_HDIFF = [
+    ("Classic", {"block_size": (32, 12, 1)}),
+    ("OnTheFly", {"block_size": (32, 16, 1), "loop": "3D"}),
+    ("OnTheFlyIncache", {"block_size": (32, 8, 1)}),
+    ("JScanSharedMem", {"block_size": (256, 32, 1)}),
+    ("JScanOtf", {"block_size": (128, 4, 1)}),
+    ("JScanShuffleIncache", {"block_size": (28, 8, 2)}),
+    ("JScanShuffleSystolic", {"block_size": (28, 4, 3)}),
+    ("JScanShuffle", {"block_size": (28, 8, 2), "domain": SHUFFLE_DOMAIN}),
+]
+REF_VADV = [
+    ("Classic", {"block_size": (128, 1), "unroll_factor": 8}),
+    ("LocalMem", {"block_size": (128, 1), "unroll_factor": 28}),
+    ("SharedMem", {"block_size": (64, 1), "unroll_factor": 0}),
+    ("LocalMemMerged", {"block_size": (128, 1), "unroll_factor": 2}),
+]
+REF_BASIC = [
+    ("Copy", {}),
+    ("Laplacian", {"along_x": True, "along_y": True, "along_z": False}),
+    ("OnesidedAverage", {"axis": 0}),
+    ("SymmetricAverage", {"axis": 1}),
+]
+OURS_HDIFF = [("TmaTile", {}), ("VectorScan", {}), ("JScan", {}), ("Tile", {})]
+OURS_VADV = [("Slab", {}), ("SharedMem", {}), ("GlobalScratch", {}), ("TensorMem", {})]
+
+
+def _ensure_cudart():
+    """The reference loads "libcudart.so" by name (stencils/cuda_hip/api.py:101-104):
+    re-run this script with the CUDA library folder on the loader path if the
+    name does not resolve."""
+    try:
+        ctypes.CDLL("libcudart.so")
+        return
+    except OSError:
+        pass
+    if os.environ.get("SBGB300_CUDART_RETRY"):
+        raise SystemExit("libcudart.so not found on the loader path")
+    roots = [os.environ.get("CUDA_HOME", ""), "/usr/local/cuda"]
+    dirs = [d for r in roots if r for d in (os.path.join(r, "lib64"), *glob.glob(os.path.join(r, "targets/*/lib")))
+            if os.path.exists(os.path.join(d, "libcudart.so"))]
+    if not dirs:
+        raise SystemExit("libcudart.so not found")
+    env = dict(os.environ, SBGB300_CUDART_RETRY="1",
+               LD_LIBRARY_PATH=os.pathsep.join([dirs[0], os.environ.get("LD_LIBRARY_PATH", "")]).rstrip(os.pathsep))
+    os.execve(sys.executable, [sys.executable] + sys.argv, env)
+
+
+def _nvcc():
+    path = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not os.path.exists(path):
+        raise SystemExit("nvcc not found")
+    return path
+
+
+def _seed_fields(bench, seed):
+    """Overwrite the benchmark's host fields with seeded uniform values (the
+    reference fills them unseeded)."""
+    rng = np.random.default_rng(seed)
+    for data in bench._data:
+        for field in data:
+            field[...] = rng.random(field.shape).astype(field.dtype)
+
+
+def time_stencil(cls, kwargs, runs, seed):
+    """Construct, verify on the first run, then the median time of `runs` runs."""
+    t0 = time.perf_counter()
+    bench = cls(**kwargs)
+    setup_s = time.perf_counter() - t0
+    _seed_fields(bench, seed)
+    verified = True
+    try:
+        bench.run()  # verify=True: the reference's verify_stencil
+    except Exception as err:  # noqa: BLE001 - reported per case
+        verified = f"{type(err).__name__}: {str(err)[:200]}"
+    bench.verify = False
+    times = [bench.run()["time"] for _ in range(runs)]
+    t = statistics.median(times)
+    points = float(np.prod(bench.domain))
+    out = {"ms": 1e3 * t, "gpoints_per_s": points / t / 1e9, "data_gbs": bench.data_size / t / 1e9,
+           "verified": verified, "setup_s": round(setup_s, 1), "domain": list(bench.domain)}
+    del bench
+    gc.collect()
+    return out
+
+
+def run_case(rows, stencil, dtype, impl, name, cls, kwargs, runs, seed):
+    row = {"stencil": stencil, "dtype": dtype, "impl": impl, "class": name,
+           "params": {k: v for k, v in kwargs.items() if k not in ("dtype", "verify", "halo", "alignment",
+                                                                  "dry_runs", "compiler", "gpu_architecture")}}
+    try:
+        row.update(time_stencil(cls, kwargs, runs, seed))
+    except Exception as err:  # noqa: BLE001 - a case that does not build or run is reported
+        row["error"] = f"{type(err).__name__}: {str(err)[:300]}"
+    print(json.dumps(row), flush=True)
+    rows.append(row)
+
+
+def stencil_cases(rows, dtypes, runs, only):
+    from stencil_benchmarks.benchmarks_collection.stencils.cuda_hip import basic as rbasic
+    from stencil_benchmarks.benchmarks_collection.stencils.cuda_hip import horizontal_diffusion as rhd
+    from stencil_benchmarks.benchmarks_collection.stencils.cuda_hip import vertical_advection as rva
+
+    from stencil_benchmarks_gb300.benchmarks_collection.stencils.gb300 import basic as obasic
+    from stencil_benchmarks_gb300.benchmarks_collection.stencils.gb300 import horizontal_diffusion as ohd
+    from stencil_benchmarks_gb300.benchmarks_collection.stencils.gb300 import vertical_advection as ova
+
+    nvcc = _nvcc()
+    ref_common = {"compiler": nvcc, "gpu_architecture": "sm_103a", "dry_runs": 1, "alignment": ALIGNMENT,
+                  "verify": True}
+    ours_common = {"dry_runs": 1, "alignment": ALIGNMENT, "verify": True}
+    groups = [("hdiff", rhd, REF_HDIFF, ohd, OURS_HDIFF, HALO),
+              ("vadv", rva, REF_VADV, ova, OURS_VADV, HALO),
+              ("basic", rbasic, REF_BASIC, obasic, [(n, dict(k)) for n, k in REF_BASIC], BASIC_HALO)]
+    for dtype in dtypes:
+        for seed, (stencil, rmod, rcases, omod, ocases, halo) in enumerate(groups):
+            if stencil not in only:
+                continue
+            for name, kw in rcases:
+                kw = dict(kw)
+                if stencil == "vadv" and name == "SharedMem" and dtype == "float64":
+                    kw["block_size"] = (32, 1)
+                if stencil == "basic":
+                    kw.update(loop="3D", block_size=(128, 2, 1))
+                args = dict(ref_common, domain=kw.pop("domain", DOMAIN), halo=halo, dtype=dtype, **kw)
+                if stencil == "vadv":
+                    args["dry_runs"] = 0  # utensstage is read and written: a dry run changes the verified input
+                run_case(rows, f"{stencil}" if stencil != "basic" else name, dtype, "reference cuda_hip", name,
+                         getattr(rmod, name), args, runs, seed)
+            for name, kw in ocases:
+                if name == "TensorMem" and dtype == "float64":
+                    continue
+                args = dict(ours_common, domain=DOMAIN, halo=halo, dtype=dtype, **kw)
+                if stencil == "vadv":
+                    args["dry_runs"] = 0
+                run_case(rows, f"{stencil}" if stencil != "basic" else name, dtype, "gb300", name,
+                         getattr(omod, name), args, runs, seed)
+
+
+def stream_cases(rows, dtypes, runs):
+    from stencil_benchmarks.benchmarks_collection.stream import cuda_hip as rstream
+
+    from stencil_benchmarks_gb300.benchmarks_collection.stream import gb300 as ostream
+
+    nvcc = _nvcc()
+    for dtype in dtypes:
+        cases = [("reference cuda_hip", rstream.Native,
+                  {"array_size": STREAM_N, "ntimes": 10, "dtype": dtype, "compiler": nvcc,
+                   "compiler_flags": "-arch sm_103a", "vector_size": v, "block_size": 1024})
+                 for v in (1, 2)]
+        cases.append(("gb300", ostream.Native, {"array_size": STREAM_N, "ntimes": 10, "dtype": dtype}))
+        for impl, cls, kw in cases:
+            row = {"stencil": "stream", "dtype": dtype, "impl": impl, "class": "Native",
+                   "params": {k: v for k, v in kw.items() if k not in ("compiler", "dtype")}}
+            try:
+                bench = cls(**kw)
+                best = {}
+                for _ in range(max(1, runs // 2)):
+                    for r in bench.run():
+                        best[r["name"]] = max(best.get(r["name"], 0.0), r["bandwidth"] / 1e3)
+                row["gbs"] = best
+                row["verified"] = True  # both classes raise when their self-check fails
+                del bench
+                gc.collect()
+            except Exception as err:  # noqa: BLE001
+                row["error"] = f"{type(err).__name__}: {str(err)[:300]}"
+            print(json.dumps(row), flush=True)
+            rows.append(row)
+
+
+def summary(rows):
+    best = {}
+    for r in rows:
+        if "error" in r:
+            continue
+        key = (r["stencil"], r["dtype"])
+        side = "reference" if r["impl"].startswith("reference") else "gb300"
+        if r["stencil"] == "stream":
+            val = r["gbs"].get("triad", 0.0)
+            better = val > best.get(key, {}).get(side, {}).get("triad_gbs", -1)
+            if better:
+                best.setdefault(key, {})[side] = {"class": r["class"], "params": r["params"], "triad_gbs": val}
+            continue
+        ok = r["verified"] is True
+        cur = best.setdefault(key, {}).get(side)
+        # a verified case beats any unverified one; among equals the faster wins
+        if cur is None or (ok, r["gpoints_per_s"]) > (cur["verified"], cur["gpoints_per_s"]):
+            best[key][side] = {"class": r["class"], "ms": r["ms"], "gpoints_per_s": r["gpoints_per_s"],
+                               "domain": r["domain"], "verified": ok}
+    out = []
+    for (stencil, dtype), sides in best.items():
+        entry = {"stencil": stencil, "dtype": dtype, **sides}
+        if "reference" in sides and "gb300" in sides:
+            unit = "triad_gbs" if stencil == "stream" else "gpoints_per_s"
+            entry["speedup"] = sides["gb300"][unit] / sides["reference"][unit]
+        out.append(entry)
+    return out
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
+    ap.add_argument("--dtypes", default="float64,float32")
+    ap.add_argument("--runs", type=int, default=5)
+    ap.add_argument("--only", default="hdiff,vadv,basic,stream")
+    args = ap.parse_args(argv)
+    _ensure_cudart()
+    from stencil_benchmarks_gb300 import host
+
+    host.load()
+    dtypes = [d for d in args.dtypes.split(",") if d]
+    only = set(args.only.split(","))
+    rows = []
+    # the reference writes each generated source into ./benchmarks_source_code
+    with tempfile.TemporaryDirectory() as scratch, contextlib.chdir(scratch):
+        stencil_cases(rows, dtypes, args.runs, only)
+        if "stream" in only:
+            stream_cases(rows, dtypes, args.runs)
+    print(json.dumps({"summary": summary(rows), "gpu": _gpu_name(),
+                      "workload": f"{DOMAIN[0]}x{DOMAIN[1]}x{DOMAIN[2]} halo {HALO} (basic {BASIC_HALO}), "
+                                  f"alignment {ALIGNMENT}, one timed launch after one dry run, "
+                                  f"median of {args.runs}; STREAM 2^29 elements, best of 10"}), flush=True)
+
+
+def _gpu_name():
+    from stencil_benchmarks_gb300 import _native
+
+    try:
+        return _native.device_info(0).get("name", "unknown")
+    except Exception:  # noqa: BLE001
+        return "unknown"
+
+
+if __name__ == "__main__":
+    main()

@@ -34,6 +34,8 @@ SB_FIX64 = 4  # compute only (hdiff): 64-bit fixed-point sums with float64 stora
 H2H, H2D, D2H, D2D = 0, 1, 2, 3
 
 STREAM_INIT, STREAM_COPY, STREAM_SCALE, STREAM_ADD, STREAM_TRIAD = range(5)
+STREAM_GRID_STRIDE, STREAM_GRID_CHUNK = 1, 2
+BASIC_POINT, BASIC_MARCH = 1, 2
 
 VARIANT_AUTO = 0
 HDIFF_TILE, HDIFF_JSCAN, HDIFF_TMA, HDIFF_VSCAN = 1, 2, 3, 4

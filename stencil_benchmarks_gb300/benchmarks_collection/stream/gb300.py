@@ -27,10 +27,14 @@ from ...device import DeviceBuffer, copy_to_host
 class Native(Benchmark):
     array_size = Parameter("number of elements in arrays", 10000000)
     ntimes = Parameter("number of runs", 10)
-    block_size = Parameter("threads per block", 512)
+    block_size = Parameter("threads per block (0: the grid shape's default)", 0)
+    grid = Parameter("grid shape: a few blocks per SM striding over the arrays, one block per chunk of "
+                     "block_size x unroll_factor vectors, or the library's choice", "auto",
+                     choices=["auto", "stride", "chunk"])
     dtype = Parameter("data type in NumPy format, e.g. float32 or float64", "float64",
                       choices=["float32", "float64"])
-    unroll_factor = Parameter("16-byte vectors per thread per iteration (1, 2, 4, 8)", 4, choices=[1, 2, 4, 8])
+    unroll_factor = Parameter("16-byte vectors per thread per iteration (0: the grid shape's default)", 0,
+                              choices=[0, 1, 2, 4, 8])
     streaming_stores = Parameter("use streaming (evict-first) store instructions", False)
     verify = Parameter("verify results", True)
     device = Parameter("CUDA device index", 0)
@@ -39,8 +43,9 @@ class Native(Benchmark):
         super().setup()
         if self.ntimes < 2:
             raise ParameterError("ntimes must be at least 2 (the first round is dropped)")
-        if self.array_size < 1 or self.block_size % 32 or not 32 <= self.block_size <= 512:
-            raise ParameterError("array_size >= 1 and block_size a multiple of 32 in [32, 512] required")
+        limit = 1024 if self.grid == "chunk" else 512
+        if self.array_size < 1 or self.block_size % 32 or not 0 <= self.block_size <= limit:
+            raise ParameterError(f"array_size >= 1 and block_size 0 or a multiple of 32 up to {limit} required")
         try:
             ndev = _native.device_count()
         except _native.NativeLibraryError as err:
@@ -50,7 +55,8 @@ class Native(Benchmark):
         _native.call("sb_set_device", self.device)
         itemsize = np.dtype(self.dtype).itemsize
         self._bufs = [DeviceBuffer(self.array_size * itemsize) for _ in range(3)]
-        self._tune = _native.tune(block_x=self.block_size, unroll=self.unroll_factor,
+        grid = {"auto": 0, "stride": _native.STREAM_GRID_STRIDE, "chunk": _native.STREAM_GRID_CHUNK}[self.grid]
+        self._tune = _native.tune(variant=grid, block_x=self.block_size, unroll=self.unroll_factor,
                                   flags=1 if self.streaming_stores else 0)
 
     def run(self):

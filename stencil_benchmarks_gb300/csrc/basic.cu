@@ -13,6 +13,12 @@ namespace sb {
 namespace {
 
 constexpr int kBasicPK = 4;
+// Laplacian march defaults: rows per strip, warps per block, k-planes per thread
+constexpr int kLapRows = 4;
+constexpr int kLapWarps = 4;
+constexpr int kLapPlanes = 2;
+// which Laplacian kernel runs when the tune names none
+constexpr int kLapDefaultVariant = SB_BASIC_MARCH;
 
 enum BasicOp { OP_COPY = 0, OP_LAP = 1, OP_AVG1 = 2, OP_AVG2 = 3 };
 
@@ -73,6 +79,142 @@ __global__ void __launch_bounds__(256) basic_kernel(const S* __restrict__ inp, S
     }
 }
 
+// Laplacian by row strips: lanes along i, warps of a block along k; each
+// thread takes a strip of R rows of j for PK k-planes, loads the strip's rows
+// (and, along j, the row before and after it) into registers at once so that
+// all its loads are in flight together, then computes the R rows.  Each input
+// row is read once per strip plus the two rows beyond it; the i-neighbours are
+// loads of rows already fetched (L1 hits).  Same operations in the same order
+// as basic_point; PL places the float64 subtractions/additions (sites 0-7) on
+// the integer pipe.
+template <int MASK, class S, class C, int R, int PK, uint32_t PL>
+__global__ void __launch_bounds__(256) lap_march_kernel(const S* __restrict__ inp, S* __restrict__ out, int ni,
+                                                        int nj, int nk, int64_t si, int64_t sj, int64_t sk) {
+    constexpr bool JN = (MASK & 2) != 0;
+    using A = Ar<C>;
+    using X = Mix<C, PL>;
+    constexpr int NR = JN ? R + 2 : R;  // rows held: j0-1 .. j0+R along j, else j0 .. j0+R-1
+    constexpr int R0 = JN ? 1 : 0;      // index of row j0 in v[]
+    const int i = blockIdx.x * 32 + threadIdx.x;
+    const int j0 = blockIdx.y * R;
+    const int kb = (blockIdx.z * blockDim.y + threadIdx.y) * PK;
+    if (i >= ni || kb >= nk) return;
+    const int nrow = min(R, nj - j0);  // rows of this strip inside the domain
+    const S* col = inp + (int64_t)i * si + (int64_t)kb * sk + (int64_t)j0 * sj;
+    S* ocol = out + (int64_t)i * si + (int64_t)kb * sk + (int64_t)j0 * sj;
+    C v[PK][NR];
+#pragma unroll
+    for (int q = 0; q < PK; ++q) {
+#pragma unroll
+        for (int r = 0; r < NR; ++r) {
+            // rows j0 - R0 + r up to j0 + nrow (the row after the strip, halo at the edge)
+            v[q][r] = (kb + q < nk && r - R0 <= nrow - (JN ? 0 : 1))
+                          ? ld<C, S>(col + (int64_t)(r - R0) * sj + (int64_t)q * sk)
+                          : C(0);
+        }
+    }
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        if (r < nrow) {
+#pragma unroll
+            for (int q = 0; q < PK; ++q) {
+                if (kb + q < nk) {
+                    const S* p = col + (int64_t)r * sj + (int64_t)q * sk;
+                    const C two_x = A::template scale2<1>(v[q][r + R0]);
+                    C acc = C(0);
+                    bool first = true;
+                    if (MASK & 1) {
+                        const C t = X::sub(X::sub(two_x, ld<C, S>(p + si), site<0>{}), ld<C, S>(p - si), site<1>{});
+                        acc = plus_zero<C>(t);
+                        first = false;
+                    }
+                    if (MASK & 2) {
+                        const C t = X::sub(X::sub(two_x, v[q][r + 2], site<2>{}), v[q][r], site<3>{});
+                        acc = first ? plus_zero<C>(t) : X::add(acc, t, site<4>{});
+                        first = false;
+                    }
+                    if (MASK & 4) {
+                        const C t = X::sub(X::sub(two_x, ld<C, S>(p + sk), site<5>{}), ld<C, S>(p - sk), site<6>{});
+                        acc = first ? plus_zero<C>(t) : X::add(acc, t, site<7>{});
+                    }
+                    st<S, C>(ocol + (int64_t)r * sj + (int64_t)q * sk, acc);
+                }
+            }
+        }
+    }
+}
+
+// float64 placements of the along-x-and-y strips (sites 0-4), by preset: 1 all
+// fp64, 2 the closing addition, 3 the second subtraction of each axis, 4 both
+// of those and the addition (0 selects the default preset)
+constexpr uint32_t kLapPlacements[] = {0u, 0u, 0x10u, 0x0Au, 0x1Au};
+constexpr int kLapPlacementDefault = 1;
+
+template <int MASK, class S, class C, int R, int PK>
+int launch_lap_march_pl(int placement, const S* inp, S* out, int64_t ni, int64_t nj, int64_t nk, int64_t si,
+                        int64_t sj, int64_t sk, int warps, cudaStream_t stream) {
+    const dim3 block(32, warps);
+    const int64_t gz = ceil_div(nk, (int64_t)warps * PK);
+    const dim3 grid((unsigned)ceil_div(ni, (int64_t)32), (unsigned)ceil_div(nj, (int64_t)R), (unsigned)gz);
+    auto go = [&](auto kernel) {
+        kernel<<<grid, block, 0, stream>>>(inp, out, (int)ni, (int)nj, (int)nk, si, sj, sk);
+        return SB_OK;
+    };
+    if constexpr (MASK == 3 && std::is_same<C, double>::value) {
+        switch (placement) {
+            case 2: return go(lap_march_kernel<MASK, S, C, R, PK, kLapPlacements[2]>);
+            case 3: return go(lap_march_kernel<MASK, S, C, R, PK, kLapPlacements[3]>);
+            case 4: return go(lap_march_kernel<MASK, S, C, R, PK, kLapPlacements[4]>);
+            default: break;
+        }
+    }
+    return go(lap_march_kernel<MASK, S, C, R, PK, 0u>);
+}
+
+template <int MASK, class S, class C>
+int launch_lap_march_shape(int rows, int pk, int placement, const S* inp, S* out, int64_t ni, int64_t nj,
+                           int64_t nk, int64_t si, int64_t sj, int64_t sk, int warps, cudaStream_t stream) {
+    if (pk == 2 && rows == 4)
+        return launch_lap_march_pl<MASK, S, C, 4, 2>(placement, inp, out, ni, nj, nk, si, sj, sk, warps, stream);
+    if (pk == 2 && rows == 8)
+        return launch_lap_march_pl<MASK, S, C, 8, 2>(placement, inp, out, ni, nj, nk, si, sj, sk, warps, stream);
+    return fail(SB_ERR_INVALID, "Laplacian strips: 4 or 8 rows x 2 k-planes per thread (got %d x %d)", rows, pk);
+}
+
+template <class S, class C>
+int launch_lap_march(const void* inp, void* out, int64_t ni, int64_t nj, int64_t nk, int64_t si, int64_t sj,
+                     int64_t sk, int mask, const sb_tune* tune, cudaStream_t stream) {
+    const DeviceProps* p;
+    int rc = device_props(&p);
+    if (rc) return rc;
+    const int rows = (tune && tune->tile_y > 0) ? tune->tile_y : kLapRows;
+    const int warps = (tune && tune->block_y > 0) ? tune->block_y : kLapWarps;
+    const int pk = (tune && tune->k_per_cta > 0) ? tune->k_per_cta : kLapPlanes;
+    const int placement = tune ? ((tune->flags >> 4) & 15) : 0;
+    SB_CHECK(warps >= 1 && warps <= 8, SB_ERR_INVALID, "Laplacian strips: 1 to 8 warps per block (got %d)", warps);
+    SB_CHECK(placement >= 0 && placement < (int)(sizeof(kLapPlacements) / sizeof(kLapPlacements[0])),
+             SB_ERR_INVALID, "Laplacian placement preset %d out of range", placement);
+    SB_CHECK(ceil_div(nj, (int64_t)rows) <= p->max_grid_y &&
+                 ceil_div(nk, (int64_t)warps * pk) <= p->max_grid_z,
+             SB_ERR_INVALID, "domain too large for the Laplacian strip grid");
+    const S* in = (const S*)inp;
+    S* o = (S*)out;
+    const int pl = placement == 0 ? kLapPlacementDefault : placement;
+    switch (mask) {
+#define SB_LAP_MASK(M) \
+    case M: return launch_lap_march_shape<M, S, C>(rows, pk, pl, in, o, ni, nj, nk, si, sj, sk, warps, stream);
+        SB_LAP_MASK(1)
+        SB_LAP_MASK(2)
+        SB_LAP_MASK(3)
+        SB_LAP_MASK(4)
+        SB_LAP_MASK(5)
+        SB_LAP_MASK(6)
+        SB_LAP_MASK(7)
+#undef SB_LAP_MASK
+    }
+    return fail(SB_ERR_INVALID, "along_mask must be in [1, 7] for the Laplacian strips");
+}
+
 template <int OP, class S, class C>
 int launch_basic(const void* inp, void* out, int64_t ni, int64_t nj, int64_t nk, int64_t si,
                  int64_t sj, int64_t sk, int mask, int64_t ds, const sb_tune* tune,
@@ -97,6 +239,22 @@ template <int OP>
 int dispatch_basic(int storage, int compute, const void* inp, void* out, int64_t ni, int64_t nj,
                    int64_t nk, int64_t si, int64_t sj, int64_t sk, int mask, int64_t ds,
                    const sb_tune* tune, cudaStream_t stream) {
+    if constexpr (OP == OP_LAP) {
+        const int variant = (tune && tune->variant > 0) ? tune->variant : kLapDefaultVariant;
+        SB_CHECK(variant == SB_BASIC_POINT || variant == SB_BASIC_MARCH, SB_ERR_INVALID,
+                 "Laplacian variant must be %d (point) or %d (row march)", SB_BASIC_POINT, SB_BASIC_MARCH);
+        if (variant == SB_BASIC_MARCH && mask != 0) {
+            if (storage == SB_F64 && compute == SB_F64)
+                return launch_lap_march<double, double>(inp, out, ni, nj, nk, si, sj, sk, mask, tune, stream);
+            if (storage == SB_F32 && compute == SB_F32)
+                return launch_lap_march<float, float>(inp, out, ni, nj, nk, si, sj, sk, mask, tune, stream);
+            if (storage == SB_F32 && compute == SB_F64)
+                return launch_lap_march<float, double>(inp, out, ni, nj, nk, si, sj, sk, mask, tune, stream);
+            if (storage == SB_BF16 && compute == SB_F32)
+                return launch_lap_march<bf16, float>(inp, out, ni, nj, nk, si, sj, sk, mask, tune, stream);
+            return fail(SB_ERR_UNSUPPORTED, "unsupported storage/compute combination (%d, %d)", storage, compute);
+        }
+    }
     if (storage == SB_F64 && compute == SB_F64)
         return launch_basic<OP, double, double>(inp, out, ni, nj, nk, si, sj, sk, mask, ds, tune, stream);
     if (storage == SB_F32 && compute == SB_F32)

@@ -79,6 +79,33 @@ __global__ void __launch_bounds__(512) stream_vec_kernel(typename Vec16<T>::type
     }
 }
 
+// dst = OP(x, y) with one block per `blockDim.x * UNROLL` vectors (no stride
+// loop): thread t of block b handles vectors b * blockDim.x * UNROLL + t +
+// u * blockDim.x, u < UNROLL, so each block streams one contiguous chunk and
+// the hardware block scheduler balances the SMs.
+template <int OP, class T, int UNROLL>
+__global__ void __launch_bounds__(1024) stream_chunk_kernel(typename Vec16<T>::type* __restrict__ dst,
+                                                            const typename Vec16<T>::type* __restrict__ x,
+                                                            const typename Vec16<T>::type* __restrict__ y,
+                                                            T s, int64_t nvec, bool streaming) {
+    using V = typename Vec16<T>::type;
+    const int64_t base = (int64_t)blockIdx.x * blockDim.x * UNROLL + threadIdx.x;
+    V vx[UNROLL], vy[UNROLL];
+#pragma unroll
+    for (int u = 0; u < UNROLL; ++u) {
+        const int64_t i = base + (int64_t)u * blockDim.x;
+        if (i < nvec) {
+            vx[u] = __ldg(x + i);
+            vy[u] = (OP == SB_STREAM_ADD || OP == SB_STREAM_TRIAD) ? __ldg(y + i) : vx[u];
+        }
+    }
+#pragma unroll
+    for (int u = 0; u < UNROLL; ++u) {
+        const int64_t i = base + (int64_t)u * blockDim.x;
+        if (i < nvec) vstore(dst + i, vop<OP>(vx[u], vy[u], s), streaming);
+    }
+}
+
 // scalar kernel for the tail and for pointers that are not 16-byte aligned
 template <int OP, class T>
 __global__ void stream_scalar_kernel(T* __restrict__ dst, const T* __restrict__ x,
@@ -100,19 +127,52 @@ __global__ void stream_init_kernel(T* __restrict__ a, T* __restrict__ b, T* __re
     }
 }
 
+// grid shape when the tune gives none, and the chunk shape's defaults
+constexpr int kStreamDefaultGrid = SB_STREAM_GRID_CHUNK;
+constexpr int kStreamChunkThreads = 1024;
+constexpr int kStreamChunkUnroll = 2;
+
 template <int OP, class T>
 int launch_op(T* dst, const T* x, const T* y, T s, int64_t n, const sb_tune* tune,
               cudaStream_t stream, const DeviceProps* p) {
     using V = typename Vec16<T>::type;
     constexpr int W = Vec16<T>::width;
     const bool streaming = tune && (tune->flags & 1);
-    const int threads = (tune && tune->block_x > 0) ? tune->block_x : 512;
-    const int unroll = (tune && tune->unroll > 0) ? tune->unroll : 4;
-    if (threads > 512 || threads % 32) return fail(SB_ERR_INVALID, "STREAM block size must be a multiple of 32 <= 512");
+    const int grid_mode = (tune && tune->variant > 0) ? tune->variant : kStreamDefaultGrid;
+    SB_CHECK(grid_mode == SB_STREAM_GRID_STRIDE || grid_mode == SB_STREAM_GRID_CHUNK, SB_ERR_INVALID,
+             "STREAM grid mode must be %d (stride) or %d (chunks)", SB_STREAM_GRID_STRIDE, SB_STREAM_GRID_CHUNK);
+    const bool chunks = grid_mode == SB_STREAM_GRID_CHUNK;
+    const int threads = (tune && tune->block_x > 0) ? tune->block_x : (chunks ? kStreamChunkThreads : 512);
+    const int unroll = (tune && tune->unroll > 0) ? tune->unroll : (chunks ? kStreamChunkUnroll : 4);
+    if (threads > (chunks ? 1024 : 512) || threads % 32)
+        return fail(SB_ERR_INVALID, "STREAM block size must be a multiple of 32 <= %d", chunks ? 1024 : 512);
     const bool aligned = ((uintptr_t)dst % 16 == 0) && ((uintptr_t)x % 16 == 0) &&
                          (y == nullptr || (uintptr_t)y % 16 == 0);
     int64_t done = 0;
-    if (aligned) {
+    if (aligned && chunks) {
+        const int64_t nvec = n / W;
+        if (nvec > 0) {
+            const int64_t blocks = ceil_div(nvec, (int64_t)threads * unroll);
+            SB_CHECK(blocks < (1LL << 31), SB_ERR_INVALID, "STREAM array too large for one chunk per block");
+            switch (unroll) {
+                case 1:
+                    stream_chunk_kernel<OP, T, 1><<<(unsigned)blocks, threads, 0, stream>>>((V*)dst, (const V*)x, (const V*)y, s, nvec, streaming);
+                    break;
+                case 2:
+                    stream_chunk_kernel<OP, T, 2><<<(unsigned)blocks, threads, 0, stream>>>((V*)dst, (const V*)x, (const V*)y, s, nvec, streaming);
+                    break;
+                case 4:
+                    stream_chunk_kernel<OP, T, 4><<<(unsigned)blocks, threads, 0, stream>>>((V*)dst, (const V*)x, (const V*)y, s, nvec, streaming);
+                    break;
+                case 8:
+                    stream_chunk_kernel<OP, T, 8><<<(unsigned)blocks, threads, 0, stream>>>((V*)dst, (const V*)x, (const V*)y, s, nvec, streaming);
+                    break;
+                default:
+                    return fail(SB_ERR_INVALID, "STREAM unroll must be 1, 2, 4 or 8 (got %d)", unroll);
+            }
+            done = nvec * W;
+        }
+    } else if (aligned) {
         const int64_t nvec = n / W;
         if (nvec > 0) {
             const int64_t want = ceil_div(nvec, (int64_t)threads * unroll);

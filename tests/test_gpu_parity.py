@@ -414,6 +414,67 @@ def test_laplacian_forms(storage, compute, along, lib):
     _assert_bits(got, want, f"laplacian {along} {storage}/{compute}")
 
 
+LAP_SHAPES = [
+    {"variant": _native.BASIC_POINT},
+    {"variant": _native.BASIC_MARCH},
+    {"variant": _native.BASIC_MARCH, "tile_y": 4, "block_y": 2},
+    {"variant": _native.BASIC_MARCH, "tile_y": 8, "block_y": 8},
+    {"variant": _native.BASIC_MARCH, "tile_y": 8, "k_per_cta": 2, "block_y": 1},
+]
+
+
+@pytest.mark.parametrize("storage,compute", FORMS)
+@pytest.mark.parametrize("mask", range(1, 8))
+@pytest.mark.parametrize("shape", range(len(LAP_SHAPES)))
+def test_laplacian_variants(storage, compute, mask, shape, lib):
+    """Every Laplacian kernel shape, every axis set, a ragged domain (partial
+    warps along i, a partial strip along j, partial k-plane groups): bit-identical
+    to the oracle."""
+    along = tuple(bool(mask >> a & 1) for a in range(3))
+    domain, halo = (37, 19, 7), (1, 1, 1)
+    shape_ = tuple(d + 2 * h for d, h in zip(domain, halo))
+    vals = rng_fields(40 + mask, shape_, ("inp", "out"), {})
+    hosts = {n: host_field(v, storage, halo=halo) for n, v in vals.items()}
+    dev = {n: to_device(h, storage, halo) for n, h in hosts.items()}
+    kernels.laplacian(dev["inp"], dev["out"], along, compute=compute, tune=_native.tune(**LAP_SHAPES[shape]))
+    got = interior(download_like(dev["out"], hosts["out"]), domain, halo)
+    want = round_to_storage(ora.laplacian(compute_view(hosts["inp"], storage, compute), domain, halo, along), storage)
+    _assert_bits(got, want, f"laplacian {LAP_SHAPES[shape]} {along} {storage}/{compute}")
+
+
+@pytest.mark.parametrize("storage", ["float64", "float32"])
+@pytest.mark.parametrize("preset", [1, 2, 3, 4])
+def test_laplacian_float64_placements(storage, preset, lib):
+    """float64 Laplacian strips with their subtractions/addition split between
+    the fp64 and the integer pipes: the same bits as the oracle, signed zeros
+    and cancellations included."""
+    domain, halo = (64, 33, 5), (1, 1, 1)
+    shape_ = tuple(d + 2 * h for d, h in zip(domain, halo))
+    vals = rng_fields(77, shape_, ("inp", "out"), {})
+    vals["inp"][::3, ::2, :] = 0.0  # exact cancellations and zero sums
+    vals["inp"][1::5, :, ::2] *= -1.0
+    hosts = {n: host_field(v, storage, halo=halo) for n, v in vals.items()}
+    dev = {n: to_device(h, storage, halo) for n, h in hosts.items()}
+    t = _native.tune(variant=_native.BASIC_MARCH, flags=preset << 4)
+    kernels.laplacian(dev["inp"], dev["out"], (True, True, False), compute="float64", tune=t)
+    got = interior(download_like(dev["out"], hosts["out"]), domain, halo)
+    want = round_to_storage(ora.laplacian(compute_view(hosts["inp"], storage, "float64"), domain, halo,
+                                          (True, True, False)), storage)
+    _assert_bits(got, want, f"laplacian placement {preset} {storage}")
+
+
+def test_laplacian_rejects_bad_strip(lib):
+    domain, halo = (8, 8, 4), (1, 1, 1)
+    shape_ = tuple(d + 2 * h for d, h in zip(domain, halo))
+    vals = rng_fields(3, shape_, ("inp", "out"), {})
+    hosts = {n: host_field(v, "float32", halo=halo) for n, v in vals.items()}
+    dev = {n: to_device(h, "float32", halo) for n, h in hosts.items()}
+    for bad in ({"tile_y": 5}, {"tile_y": 16}, {"k_per_cta": 4}, {"block_y": 9}, {"flags": 9 << 4}):
+        with pytest.raises(_native.SbError) as err:
+            kernels.laplacian(dev["inp"], dev["out"], tune=_native.tune(variant=_native.BASIC_MARCH, **bad))
+        assert err.value.code == _native.SB_ERR_INVALID
+
+
 @pytest.mark.parametrize("storage", ["float64", "float32", "bfloat16"])
 def test_copy_storage(storage, lib):
     domain, halo = (50, 7, 9), (3, 3, 3)
