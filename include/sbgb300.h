@@ -442,8 +442,15 @@ int sb_vadv_noalloc(int storage, int compute, const void* stage, const void* pos
  * with independent 32-bit integer work beside them, 48 integer operations per
  * add, counted as adds; 11: that integer work alone, counted the same way --
  * 10 runs at the rate of 0 if the two pipes overlap, and at
- * 1 / (1/rate(0) + 1/rate(11)) if they do not). */
+ * 1 / (1/rate(0) + 1/rate(11)) if they do not; 12: f64 reciprocal in integer
+ * arithmetic, 13: the f64 reciprocal instruction sequence, __drcp_rn). */
 int sb_probe_arith_rate(int kind, double* ops_per_s);
+/* The binary64 operations the kernels can run in integer arithmetic, applied
+ * element-wise on the device to n doubles (op 0: a + b, 1: a - b, 2: a * b,
+ * 3: 1 / a, b unused), asynchronously on `stream`: for checking them against
+ * IEEE arithmetic.  Operands the integer path declines take the fp64
+ * instruction, as in the kernels. */
+int sb_debug_soft_f64(int op, const void* a, const void* b, void* out, int64_t n, void* stream);
 
 #ifdef __cplusplus
 }

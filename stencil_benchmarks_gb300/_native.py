@@ -153,6 +153,7 @@ SIGNATURES = {
     "sb_server_debug_complete": [_vp],
     "sb_server_debug_launches": [_vp, _vp, _int, ctypes.POINTER(_int)],
     "sb_probe_arith_rate": [_int, _dp],
+    "sb_debug_soft_f64": [_int, _vp, _vp, _vp, _i64, _vp],
 }
 _RESTYPES = {"sb_last_error": ctypes.c_char_p}
 

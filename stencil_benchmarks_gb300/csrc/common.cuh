@@ -254,10 +254,16 @@ __device__ __forceinline__ double imul(double a, double b) {
     if (sf::mul(sf::bits(a), sf::bits(b), r)) return sf::from_bits(r);
     return fp64_mul_cold(a, b);
 }
+static __device__ __noinline__ double fp64_rcp_cold(double a) { return __drcp_rn(a); }
+__device__ __forceinline__ double ircp(double a) {
+    uint64_t r;
+    if (sf::rcp(sf::bits(a), r)) return sf::from_bits(r);
+    return fp64_rcp_cold(a);
+}
 
 // Arithmetic with a per-site choice of pipe.  A kernel numbers its operation
 // sites (site<K>); for float64 compute, bit K of the placement mask PL sends
-// site K to the integer pipe (iadd / isub / imul), the others use the fp64
+// site K to the integer pipe (iadd / isub / imul / ircp), the others use the fp64
 // instructions.  The results are the same bits either way; only the balance
 // between the two pipes changes.  Other compute types ignore the mask.
 template <int K>
@@ -271,6 +277,8 @@ struct Mix {
     static __device__ __forceinline__ C sub(C a, C b, site<K>) { return Ar<C>::sub(a, b); }
     template <int K>
     static __device__ __forceinline__ C mul(C a, C b, site<K>) { return Ar<C>::mul(a, b); }
+    template <int K>
+    static __device__ __forceinline__ C rcp(C a, site<K>) { return Ar<C>::rcp(a); }
 };
 
 template <uint32_t PL>
@@ -289,6 +297,11 @@ struct Mix<double, PL> {
     static __device__ __forceinline__ double mul(double a, double b, site<K>) {
         if constexpr (((PL >> K) & 1u) != 0u) return imul(a, b);
         else return __dmul_rn(a, b);
+    }
+    template <int K>
+    static __device__ __forceinline__ double rcp(double a, site<K>) {
+        if constexpr (((PL >> K) & 1u) != 0u) return ircp(a);
+        else return __drcp_rn(a);
     }
 };
 

@@ -1,5 +1,6 @@
 // Library plumbing behind the C ABI: error strings, device queries, memory,
 // streams/events, L2 flush and the arithmetic-rate probe.
+#include <algorithm>
 #include <atomic>
 #include <cstdarg>
 #include <cstring>
@@ -195,6 +196,16 @@ __global__ void arith_probe_kernel(double* out, int iters, double x) {
             t += b[u];
         }
         if (s == 12345.678 || t == 12345u) out[0] = s;
+    } else if (KIND == 12 || KIND == 13) {  // binary64 reciprocal: integer pipe (12), __drcp_rn (13)
+        double a[8];
+        for (int u = 0; u < 8; ++u) a[u] = x + (double)(threadIdx.x + u);
+        for (int it = 0; it < iters; ++it) {
+#pragma unroll
+            for (int u = 0; u < 8; ++u) a[u] = KIND == 12 ? ircp(a[u]) : __drcp_rn(a[u]);
+        }
+        double s = 0.0;
+        for (int u = 0; u < 8; ++u) s += a[u];
+        if (s == 12345.678) out[0] = s;
     } else if (KIND == 8 || KIND == 9) {  // binary64 add / mul on the integer pipe (softf64.cuh)
         double a[8];
         for (int u = 0; u < 8; ++u) a[u] = x + (double)(threadIdx.x + u);
@@ -217,6 +228,15 @@ __global__ void arith_probe_kernel(double* out, int iters, double x) {
         double s = 0.0;
         for (int u = 0; u < 8; ++u) s += a[u];
         if (s == 12345.678) out[0] = s;
+    }
+}
+// The integer-arithmetic binary64 operations (softf64.cuh) element-wise, for
+// checking the device build against the host's IEEE arithmetic.
+__global__ void soft_f64_kernel(int op, const double* __restrict__ a, const double* __restrict__ b,
+                                double* __restrict__ out, int64_t n) {
+    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
+        const double x = a[q];
+        out[q] = op == 0 ? iadd(x, b[q]) : op == 1 ? isub(x, b[q]) : op == 2 ? imul(x, b[q]) : ircp(x);
     }
 }
 }  // namespace
@@ -428,15 +448,29 @@ int sb_l2_flush(void* stream) {
     return SB_OK;
 }
 
+int sb_debug_soft_f64(int op, const void* a, const void* b, void* out, int64_t n, void* stream) {
+    clear_error();
+    SB_CHECK(op >= 0 && op <= 3, SB_ERR_INVALID, "op must be 0 (add), 1 (sub), 2 (mul) or 3 (reciprocal)");
+    SB_CHECK(n >= 0 && a && out && (op == 3 || b), SB_ERR_INVALID, "bad arguments");
+    if (n == 0) return SB_OK;
+    const DeviceProps* p;
+    int rc = device_props(&p);
+    if (rc) return rc;
+    const int blocks = (int)std::min<int64_t>(ceil_div(n, (int64_t)256), (int64_t)p->sm_count * 16);
+    soft_f64_kernel<<<blocks, 256, 0, (cudaStream_t)stream>>>(op, (const double*)a, (const double*)b, (double*)out, n);
+    SB_CUDA(cudaGetLastError());
+    return SB_OK;
+}
+
 int sb_probe_arith_rate(int kind, double* ops_per_s) {
-    SB_CHECK(kind >= 0 && kind <= 11 && ops_per_s, SB_ERR_INVALID, "bad probe arguments");
+    SB_CHECK(kind >= 0 && kind <= 13 && ops_per_s, SB_ERR_INVALID, "bad probe arguments");
     const DeviceProps* p;
     int rc = device_props(&p);
     if (rc) return rc;
     double* out = nullptr;
     SB_CUDA(cudaMalloc(&out, sizeof(double)));
     const int blocks = p->sm_count * 8, threads = 256,
-              iters = (kind == 2 || (kind >= 5 && kind <= 9)) ? 8192 : 512;
+              iters = (kind == 2 || (kind >= 5 && kind <= 9)) ? 8192 : (kind >= 12 ? 2048 : 512);
     auto launch = [&]() {
         if (kind == 0) arith_probe_kernel<0><<<blocks, threads>>>(out, iters, 0.5);
         if (kind == 1) arith_probe_kernel<1><<<blocks, threads>>>(out, iters, 0.5);
@@ -450,6 +484,8 @@ int sb_probe_arith_rate(int kind, double* ops_per_s) {
         if (kind == 9) arith_probe_kernel<9><<<blocks, threads>>>(out, iters, 0.5);
         if (kind == 10) arith_probe_kernel<10><<<blocks, threads>>>(out, iters, 0.5);
         if (kind == 11) arith_probe_kernel<11><<<blocks, threads>>>(out, iters, 0.5);
+        if (kind == 12) arith_probe_kernel<12><<<blocks, threads>>>(out, iters, 0.5);
+        if (kind == 13) arith_probe_kernel<13><<<blocks, threads>>>(out, iters, 0.5);
         return SB_OK;
     };
     double t = 0.0;

@@ -1,7 +1,7 @@
-// Binary64 addition, subtraction and multiplication in integer arithmetic,
-// correctly rounded to nearest-even: bit-identical to the hardware's
-// __dadd_rn / __dsub_rn / __dmul_rn (and to numpy) for every input the fast
-// paths accept.
+// Binary64 addition, subtraction, multiplication and reciprocal in integer
+// arithmetic, correctly rounded to nearest-even: bit-identical to the
+// hardware's __dadd_rn / __dsub_rn / __dmul_rn / __drcp_rn (and to numpy) for
+// every input the fast paths accept.
 //
 // Why: GB300 executes fp64 arithmetic at 0.52 Tops/s, 1/57 of its 32-bit
 // integer rate, so the exact fp64 stencils are bound by the fp64 pipe while
@@ -163,6 +163,101 @@ SB_SF_HD bool mul(uint64_t a, uint64_t b, uint64_t& r) {
     const int e = (int)(ea + eb) - 1023 - n;
     if ((unsigned)e > 2045u) return false;
     r = round_pack<11>(sign, (uint32_t)e, hi << n);
+    return true;
+}
+
+#if !defined(__CUDA_ARCH__)
+// Host builds: ulps added to the seed reciprocal (a test knob that stands in
+// for the device's approximate reciprocal instruction; 0 by default).
+inline int& rcp_seed_perturb() {
+    static int ulps = 0;
+    return ulps;
+}
+#endif
+
+// float approximation of 1 / x for x in [2^23, 2^24): the device's
+// rcp.approx (relative error below 2^-22); on the host the correctly rounded
+// quotient, moved by rcp_seed_perturb() ulps.
+SB_SF_HD float rcp_seed(float x) {
+#if defined(__CUDA_ARCH__)
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+#else
+    float r = 1.0f / x;
+    uint32_t b;
+    std::memcpy(&b, &r, sizeof b);
+    b = (uint32_t)((int32_t)b + rcp_seed_perturb());
+    std::memcpy(&r, &b, sizeof r);
+    return r;
+#endif
+}
+
+// One Newton step towards u = 2^126 / d (d in (2^63, 2^64)) from y ~ u:
+// y + y * E / 2^126, with E = 2^126 - d*y computed exactly in 128 bits and
+// shifted right by SE bits so that it fits a signed 64-bit word e; then
+// y * E / 2^126 = mulhi(y, e) / 2^(62 - SE).
+template <int SE>
+SB_SF_HD uint64_t rcp_step(uint64_t d, uint64_t y) {
+    constexpr int SC = 62 - SE;
+    const uint64_t plo = d * y, phi = mulhi64(d, y);
+    const uint64_t elo = 0ull - plo;
+    const uint64_t ehi = (1ull << 62) - phi - (uint64_t)(plo != 0);
+    const int64_t e = (int64_t)((ehi << (64 - SE)) | (elo >> SE));
+    const uint64_t mag = e < 0 ? 0ull - (uint64_t)e : (uint64_t)e;
+    const uint64_t c = mulhi64(y, mag) >> SC;
+    return e < 0 ? y - c : y + c;
+}
+
+// 1 / a, correctly rounded to nearest (bit-identical to __drcp_rn and to
+// numpy's 1.0 / a).  Returns false where the hardware must compute it: a
+// zero, subnormal, NaN or infinite operand, or |a| >= 2^1022 (a result at or
+// below the bottom of the normal range).
+//
+// Method (restated from the Newton-Raphson reciprocal iteration with an exact
+// remainder correction; Muller et al., Handbook of Floating-Point Arithmetic,
+// 2nd ed., sec. 4.7 and ch. 8 on division):  with the significand M in
+// (2^52, 2^53) (a power of two is exact), the rounded significand of 1/a is
+// S = round(2^105 / M) = (floor(2^106 / M) + 1) >> 1 (2^105 / M is never a
+// tie).  With d = M << 11, floor(2^106 / M) = floor(2^117 / d) =
+// floor(u / 2^9), u = 2^126 / d in (2^62, 2^63):
+//   * seed: the float reciprocal of d's top 32 bits (relative error below
+//     2^-20);
+//   * a Newton step y <- y (2 - dh y) in 32 x 32-bit products on those top
+//     bits (relative error below 2^-30, set by the dropped low bits of d),
+//     then one on the full d in 64-bit products, y <- y (2 - d y / 2^126),
+//     which squares it: |y2 - u| <= 4;
+//   * q = y2 >> 9 is floor(2^117 / d) or one off; the exact remainder
+//     2^117 - q d (128-bit) decides the +-1 correction.
+SB_SF_HD bool rcp(uint64_t a, uint64_t& r) {
+    const uint32_t ea = (uint32_t)(a >> 52) & 0x7ffu;
+    if (ea - 1u >= 2044u) return false;  // zero / subnormal (0), exponent >= 2045, inf / NaN
+    const uint64_t sign = a & kSign;
+    const uint64_t frac = a & kMant;
+    if (frac == 0) {
+        r = sign | ((uint64_t)(2046u - ea) << 52);
+        return true;
+    }
+    const uint64_t d = (frac | kImplicit) << 11;
+    // first step on d's top 32 bits: y0 ~ 2^62 / dh (31 bits), E = 2^62 - dh y0
+    // (|E| < 2^43), y1 = y0 2^32 + y0 E / 2^30 ~ 2^94 / dh = u (1 + eta),
+    // |eta| < 2^-30 (the truncation of d dominates the squared seed error)
+    const uint32_t dh = (uint32_t)(d >> 32);
+    const uint32_t y0 = (uint32_t)(rcp_seed((float)dh) * 0x1p62f);
+    const int64_t e0 = (int64_t)((1ull << 62) - (uint64_t)dh * y0);
+    const uint64_t c0 = ((uint64_t)y0 * ((e0 < 0 ? 0ull - (uint64_t)e0 : (uint64_t)e0) >> 10)) >> 20;
+    const uint64_t y1 = e0 < 0 ? ((uint64_t)y0 << 32) - c0 : ((uint64_t)y0 << 32) + c0;
+    const uint64_t y2 = rcp_step<34>(d, y1);  // |E| < 2^96: e = E >> 34 fits
+    uint64_t q = y2 >> 9;
+    const uint64_t plo = q * d, phi = mulhi64(q, d);
+    const uint64_t rlo = 0ull - plo;
+    const int64_t rhi = (int64_t)((1ull << 53) - phi - (uint64_t)(plo != 0));
+    if (rhi < 0) {
+        q -= 1;
+    } else if (rhi > 0 || rlo >= d) {
+        q += 1;
+    }
+    r = sign | (((uint64_t)(2044u - ea) << 52) + ((q + 1) >> 1));
     return true;
 }
 

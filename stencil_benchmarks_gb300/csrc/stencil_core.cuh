@@ -553,8 +553,10 @@ __device__ __forceinline__ C from_ring(T w, uint32_t sel) {
 // vadv_async_column): the placement that pays on the integer pipe.
 constexpr uint32_t kVadvProductSites = (1u << 4) | (1u << 5) | (1u << 7) | (1u << 11) | (1u << 13) | (1u << 14) |
                                        (1u << 16) | (1u << 17) | (1u << 20);
+// The level's reciprocal (site 21).
+constexpr uint32_t kVadvRcpSite = 1u << 21;
 
-// PL: integer-pipe placement mask over the operation sites 0-20 below (Mix).
+// PL: integer-pipe placement mask over the operation sites 0-21 below (Mix).
 template <class S, class C, int BT, int D, class IDX, bool SLAB = false, class P = C, uint32_t PL = 0u>
 __device__ __forceinline__ void vadv_async_column(const S* __restrict__ stage, const S* __restrict__ pos,
                                                   const S* __restrict__ tens, const S* tensstage,
@@ -631,7 +633,7 @@ __device__ __forceinline__ void vadv_async_column(const S* __restrict__ stage, c
             corr = X::sub(X::mul(-as_, ddown, site<4>{}), X::mul(cs, dup, site<5>{}), site<6>{});
             dv = X::add(X::add(X::add(X::mul(dtr, p0, site<7>{}), t0, site<8>{}), ts0, site<9>{}), corr, site<10>{});
             const P pas = to_p<P>(as_);
-            const P divided = AP::rcp(XP::sub(to_p<P>(bcol), XP::mul(cp, pas, site<11>{}), site<12>{}));
+            const P divided = XP::rcp(XP::sub(to_p<P>(bcol), XP::mul(cp, pas, site<11>{}), site<12>{}), site<21>{});
             cp = XP::mul(to_p<P>(cs), divided, site<13>{});
             dp = XP::mul(XP::sub(to_p<P>(dv), XP::mul(dp, pas, site<14>{}), site<15>{}), divided, site<16>{});
             sc[k * FS] = cp;

@@ -63,7 +63,8 @@ __global__ void __launch_bounds__(256)
 // Integer-pipe placements of float64 vadv's operation sites (bit K = site K
 // of vadv_async_column: 0 the wcon sum, 1 the stage difference, 2-3 bcol,
 // 4-6 the correction, 7-10 the right-hand side, 11-12 the pivot, 13 ccol,
-// 14-16 dcol, 17-18 the back substitution, 19-20 the output).  sb_tune.flags
+// 14-16 dcol, 17-18 the back substitution, 19-20 the output, 21 the pivot's
+// reciprocal).  sb_tune.flags
 // bits 4-7 pick one for the SLAB form: 0 the default, 1 every site on the
 // fp64 pipe, 2.. the mixes below; SLAB shapes other than 32 threads x depth 4
 // and the SMEM-async form use the default.
@@ -84,6 +85,12 @@ constexpr uint32_t kVadvPlacements[] = {
     vadv_sites({17, 20}),
     vadv_sites({4, 5, 7, 11, 13, 14, 16}),
     kVadvMuls | vadv_sites({0}),
+    kVadvMuls | kVadvRcpSite,
+    kVadvRcpSite,
+    vadv_sites({4, 5, 7, 14, 17, 20}) | kVadvRcpSite,
+    vadv_sites({4, 5, 7, 11, 13, 14, 16}) | kVadvRcpSite,
+    vadv_sites({4, 5, 7}) | kVadvRcpSite,
+    vadv_sites({17, 20}) | kVadvRcpSite,
 };
 // Measured at 512x512x80 (32-thread SLAB blocks, depth 4): every site on the
 // fp64 pipe 1171-1201 us whatever the blocks per SM; the nine products on the
@@ -324,6 +331,12 @@ int launch_slab(int bx, int depth, int blocks_per_sm, int placement, const Devic
                 SB_VADV_SLAB_PL(6)
                 SB_VADV_SLAB_PL(7)
                 SB_VADV_SLAB_PL(8)
+                SB_VADV_SLAB_PL(9)
+                SB_VADV_SLAB_PL(10)
+                SB_VADV_SLAB_PL(11)
+                SB_VADV_SLAB_PL(12)
+                SB_VADV_SLAB_PL(13)
+                SB_VADV_SLAB_PL(14)
 #undef SB_VADV_SLAB_PL
             }
         }

@@ -2,7 +2,9 @@
 (csrc/softf64.cuh): every placement preset of the hdiff TMA tile and of the
 vadv SLAB form must stay bit-identical to the oracle, on ordinary workload
 values and on values that take the integer path's fallbacks (zeros,
-subnormal operands and results, overflow to infinity, NaN)."""
+subnormal operands and results, overflow to infinity, NaN); and the device
+build of the integer operations themselves (the reciprocal seeds with the
+device's approximate instruction) against IEEE arithmetic."""
 
 from __future__ import annotations
 
@@ -25,7 +27,8 @@ from tests.gpu_helpers import (
 
 pytestmark = pytest.mark.gpu
 
-PRESETS = range(1, 9)
+HDIFF_PRESETS = range(1, 9)
+VADV_PRESETS = range(1, 15)
 
 
 def _specials(rng, shape, scale):
@@ -40,7 +43,7 @@ def _specials(rng, shape, scale):
     return v
 
 
-@pytest.mark.parametrize("preset", PRESETS)
+@pytest.mark.parametrize("preset", HDIFF_PRESETS)
 @pytest.mark.parametrize("special", [False, True])
 def test_hdiff_tma_placements(preset, special, lib):
     domain, halo = (130, 70, 6), (2, 2, 0)
@@ -58,7 +61,7 @@ def test_hdiff_tma_placements(preset, special, lib):
     assert bits_equal(got, want), f"preset {preset}: " + mismatch_report(got, want)
 
 
-@pytest.mark.parametrize("preset", PRESETS)
+@pytest.mark.parametrize("preset", VADV_PRESETS)
 @pytest.mark.parametrize("per_sm", [0, 24])
 @pytest.mark.parametrize("nk", [2, 3, 40])
 def test_vadv_slab_placements(preset, per_sm, nk, lib):
@@ -78,7 +81,7 @@ def test_vadv_slab_placements(preset, per_sm, nk, lib):
     assert bits_equal(got, want), f"preset {preset}, {per_sm} blocks/SM, nk {nk}: " + mismatch_report(got, want)
 
 
-@pytest.mark.parametrize("preset", [2, 5])
+@pytest.mark.parametrize("preset", [2, 5, 9, 10, 12])
 def test_vadv_slab_placements_with_specials(preset, lib):
     domain, halo = (64, 12, 30), (1, 1, 0)
     shape = tuple(d + 2 * h for d, h in zip(domain, halo))
@@ -111,3 +114,59 @@ def test_integer_arithmetic_rates(lib):
     """The probes of the integer binary64 add and multiply run and report rates."""
     for kind in (8, 9, 10, 11):
         assert kernels.arith_rate(kind) > 1e9
+
+
+def _soft_on_device(op, a, b):
+    """sb_debug_soft_f64 on the device, element-wise."""
+    import ctypes
+
+    from stencil_benchmarks_gb300.device import DeviceBuffer, copy_to_device, copy_to_host
+
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    b = np.ascontiguousarray(b, dtype=np.float64)
+    da, db, do = (DeviceBuffer(a.nbytes) for _ in range(3))
+    copy_to_device(da.ptr, a)
+    copy_to_device(db.ptr, b)
+    _native.call("sb_debug_soft_f64", op, ctypes.c_void_p(da.ptr), ctypes.c_void_p(db.ptr),
+                 ctypes.c_void_p(do.ptr), a.size, None)
+    _native.synchronize()
+    out = np.empty_like(a)
+    copy_to_host(out, do.ptr)
+    return out
+
+
+def _operands(rng, n, span):
+    e = rng.integers(-span, span + 1, size=(2, n)).astype(np.float64)
+    m = 1.0 + rng.integers(0, 2**52, size=(2, n), dtype=np.int64).astype(np.float64) * 2.0**-52
+    s = rng.choice([-1.0, 1.0], size=(2, n))
+    with np.errstate(over="ignore"):
+        return s[0] * m[0] * np.exp2(e[0]), s[1] * m[1] * np.exp2(e[1])
+
+
+@pytest.mark.parametrize("op", [0, 1, 2, 3])
+def test_soft_f64_on_device(op, lib):
+    """Each integer-arithmetic operation as compiled for sm_103a, on 2 M random
+    operands of every magnitude relation plus zeros, subnormals, huge values,
+    infinities and NaN: the same bits as numpy (any NaN for a NaN)."""
+    rng = np.random.Generator(np.random.PCG64(500 + op))
+    a, b = _operands(rng, 2_000_000, 1100 if op == 3 else 60)
+    sp = np.array([0.0, -0.0, 5e-324, -3e-310, 2.0**-1022, 1.0, -1.5, 2.0**1021, 1.5 * 2.0**1022,
+                   np.finfo(np.float64).max, np.inf, -np.inf, np.nan])
+    ga, gb = np.meshgrid(sp, sp)
+    a = np.concatenate([a, ga.ravel(), rng.uniform(0.1, 3.0, size=100_000)])
+    b = np.concatenate([b, gb.ravel(), rng.uniform(-1.0, 1.0, size=100_000)])
+    got = _soft_on_device(op, a, b)
+    with np.errstate(all="ignore"):
+        want = [a + b, a - b, a * b, 1.0 / a][op]
+    nan = np.isnan(want)
+    assert (np.isnan(got) == nan).all(), "NaN results differ"
+    same = got[~nan].view(np.uint64) == want[~nan].view(np.uint64)
+    assert same.all(), f"op {op}: {np.count_nonzero(~same)} differ, first operands {a[~nan][~same][:3]}"
+
+
+def test_soft_reciprocal_rate(lib):
+    """The integer-arithmetic reciprocal is faster than the fp64 sequence it
+    replaces (the reason the vadv pivot's reciprocal can move)."""
+    soft, hard = kernels.arith_rate(12), kernels.arith_rate(13)
+    assert soft > 0 and hard > 0
+    print(f"reciprocal: integer {soft / 1e9:.1f} G/s, fp64 {hard / 1e9:.1f} G/s")

@@ -1,4 +1,4 @@
-"""Integer-pipe binary64 add / sub / mul (csrc/softf64.cuh), built for the
+"""Integer-pipe binary64 add / sub / mul / reciprocal (csrc/softf64.cuh), built for the
 host and compared bit for bit with the host's IEEE 754 arithmetic (numpy) on
 random operands of every magnitude relation, on rounding ties, cancellations,
 zeros, subnormals, overflow and NaN/infinity.  Where the fast path declines
@@ -28,6 +28,7 @@ def sf(tmp_path_factory):
     lib = ctypes.CDLL(str(out))
     up = ctypes.POINTER(ctypes.c_uint64)
     lib.sf_binop.argtypes = [ctypes.c_int, up, up, up, ctypes.POINTER(ctypes.c_ubyte), ctypes.c_long]
+    lib.sf_set_rcp_perturb.argtypes = [ctypes.c_int]
     return lib
 
 
@@ -129,3 +130,74 @@ def test_zeros_subnormals_infinities_nans(sf):
     # products near the bottom of the normal range
     check(sf, 2, np.array([2.0**-511, 2.0**-512, 1.5 * 2.0**-511, 2.0**-1000]),
           np.array([2.0**-511, 2.0**-511, 1.5 * 2.0**-512, 2.0**-22]))
+
+
+# ---------------------------------------------------------------------------
+# reciprocal
+# ---------------------------------------------------------------------------
+
+
+def check_rcp(sf, a):
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    got, taken = run(sf, 3, a, a)
+    with np.errstate(all="ignore"):
+        want = (1.0 / a).view(np.uint64)
+    same = got[taken] == want[taken]
+    assert same.all(), f"rcp: {np.count_nonzero(~same)} of {taken.sum()} differ, first {a[taken][~same][:3]}"
+    # declined exactly for zeros, subnormals, inf/NaN and |a| >= 2^1022
+    absa = np.abs(a)
+    declined = ~np.isfinite(a) | (absa < 2.0**-1022) | (absa >= 2.0**1022)
+    assert taken[~declined].all(), "rcp declined an ordinary operand"
+    assert not taken[declined].any(), "rcp took an operand it must leave to the hardware"
+
+
+@pytest.mark.parametrize("perturb", [0, -8, -3, -1, 1, 3, 8])
+def test_rcp_random_significands(sf, perturb):
+    """Every significand region, with the float seed moved by up to 8 ulps
+    either way (the device seeds with rcp.approx, within about 1 ulp): the
+    two Newton steps and the remainder correction absorb it."""
+    sf.sf_set_rcp_perturb(perturb)
+    try:
+        rng = np.random.Generator(np.random.PCG64(100 + perturb))
+        n = 400_000
+        m = 1.0 + rng.integers(1, 2**52, size=n, dtype=np.int64).astype(np.float64) * 2.0**-52
+        e = rng.integers(-1000, 1000, size=n)
+        s = rng.choice([-1.0, 1.0], size=n)
+        check_rcp(sf, s * m * np.exp2(e.astype(np.float64)))
+    finally:
+        sf.sf_set_rcp_perturb(0)
+
+
+@pytest.mark.parametrize("perturb", [0, -8, 8])
+def test_rcp_edge_significands(sf, perturb):
+    """Significands at the ends of [1, 2), next to powers of two, halves and
+    thirds, and those whose seeds sit on float boundaries (the top 24 bits
+    all ones or 2^23), where the quotient's last bits are closest to a
+    rounding boundary."""
+    sf.sf_set_rcp_perturb(perturb)
+    try:
+        k = np.arange(0, 4096, dtype=np.int64)
+        frac = np.concatenate([
+            1 + k, 2**52 - 1 - k, 2**51 + k - 2048, (2**52 // 3) + k - 2048, (2 * 2**52 // 3) + k - 2048,
+            ((2**24 - 1) << 28) + k, ((2**24 - 1) << 28) - 1 - k, (1 << 28) + k - 2048,
+        ])
+        frac = frac[(frac > 0) & (frac < 2**52)]
+        a = (np.uint64(1023) << np.uint64(52) | frac.astype(np.uint64)).view(np.float64)
+        check_rcp(sf, np.concatenate([a, -a, a * 2.0**700, a * 2.0**-700]))
+    finally:
+        sf.sf_set_rcp_perturb(0)
+
+
+def test_rcp_stencil_like_values(sf):
+    """The denominators the vertical solve takes: U[0.1, 3) as its bcol
+    differences draw them, and powers of two."""
+    rng = np.random.Generator(np.random.PCG64(11))
+    check_rcp(sf, rng.uniform(0.1, 3.0, size=300_000))
+    check_rcp(sf, np.exp2(np.arange(-1022, 1024, dtype=np.float64)))
+
+
+def test_rcp_specials(sf):
+    vals = np.array([0.0, -0.0, 5e-324, -1e-310, 2.0**-1022, -2.0**-1022, 2.0**-1021, np.inf, -np.inf, np.nan,
+                     2.0**1020, 1.9 * 2.0**1020, 2.0**1021, 1.5 * 2.0**1021, 2.0**1022, 1.5 * 2.0**1022, 2.0**1023,
+                     np.finfo(np.float64).max])
+    check_rcp(sf, vals)
