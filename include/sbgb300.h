@@ -115,11 +115,12 @@ typedef struct sb_tune {
     int32_t flags;     /* STREAM: bit0 streaming (evict-first) stores;
                         * vadv TMEM: bit 10 / 11 stage through 32-bit shared
                         * addresses / generic pointers (neither: the default);
-                        * float64 hdiff TMA / vadv SLAB: bits 4-7 pick which
-                        * operations run as integer arithmetic instead of fp64
-                        * instructions (same bits either way; 0: the library's
-                        * default split, 1: all on the fp64 pipe, 2-8: other
-                        * splits)                                               */
+                        * float64 hdiff TMA / vadv SLAB / Laplacian strips:
+                        * bits 4-7 pick which operations run as integer
+                        * arithmetic instead of fp64 instructions (same bits
+                        * either way; 0: the library's default split, 1: all
+                        * on the fp64 pipe, 2-8 (hdiff), 2-15 (vadv), 2-4
+                        * (Laplacian): other splits)                          */
     int32_t reserved;
 } sb_tune;
 

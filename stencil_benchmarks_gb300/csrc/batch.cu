@@ -270,9 +270,10 @@ Kinds kinds_for() {
                           !(std::is_same<S, float>::value && std::is_same<P, float>::value);
     k.slab = SLAB;
     k.hdiff = &run_hdiff<S, HC, U, IDX>;
-    // float64 slab buckets: the products on the integer pipe (more blocks per SM, below)
+    // float64 slab buckets: the single-domain kernel's split between the fp64
+    // and integer pipes (more blocks per SM, below)
     constexpr uint32_t PL = SLAB && std::is_same<P, double>::value && std::is_same<VC, double>::value
-                                ? kVadvProductSites
+                                ? kVadvDefaultIntSites
                                 : 0u;
     k.int_products = PL != 0u;
     k.vadv32 = &run_vadv<S, VC, 32, IDX, P, SLAB, PL>;

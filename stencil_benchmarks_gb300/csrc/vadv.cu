@@ -79,28 +79,33 @@ constexpr uint32_t kVadvPlacements[] = {
     0u,
     0u,
     kVadvMuls,
-    vadv_sites({4, 5, 7, 14, 17, 20}),
-    vadv_sites({4, 5, 7, 14, 17, 20, 11}),
-    vadv_sites({4, 5, 7}),
-    vadv_sites({17, 20}),
-    vadv_sites({4, 5, 7, 11, 13, 14, 16}),
-    kVadvMuls | vadv_sites({0}),
+    vadv_sites({7, 14, 17, 20}) | kVadvRcpSite,
+    vadv_sites({5, 14, 17, 20}) | kVadvRcpSite,
+    vadv_sites({5, 7, 17, 20}) | kVadvRcpSite,
+    vadv_sites({5, 7, 14, 17}) | kVadvRcpSite,
+    vadv_sites({5, 7, 14, 20}) | kVadvRcpSite,
+    vadv_sites({14, 17, 20}) | kVadvRcpSite,
     kVadvMuls | kVadvRcpSite,
     kVadvRcpSite,
     vadv_sites({4, 5, 7, 14, 17, 20}) | kVadvRcpSite,
-    vadv_sites({4, 5, 7, 11, 13, 14, 16}) | kVadvRcpSite,
-    vadv_sites({4, 5, 7}) | kVadvRcpSite,
-    vadv_sites({17, 20}) | kVadvRcpSite,
+    vadv_sites({4, 5, 7, 14, 17}) | kVadvRcpSite,
+    vadv_sites({4, 5, 7, 17, 20}) | kVadvRcpSite,
+    vadv_sites({4, 5, 7, 14, 16, 17, 20}) | kVadvRcpSite,
+    kVadvDefaultIntSites,
 };
+static_assert(kVadvDefaultIntSites == (vadv_sites({5, 7, 14, 17, 20}) | kVadvRcpSite), "the default split");
 // Measured at 512x512x80 (32-thread SLAB blocks, depth 4): every site on the
 // fp64 pipe 1171-1201 us whatever the blocks per SM; the nine products on the
-// integer pipe (preset 2) 980 us with 24 blocks per SM (1019 with 16, 1189
-// with 8: the integer sequences need more warps in flight); additions on the
-// integer pipe cost more than they save (a binary64 add in integer
-// arithmetic runs at 0.31 Tops/s against 0.52 for the fp64 instruction, a
-// multiply at 0.56).  The default SLAB form therefore runs the products on
-// the integer pipe with 24 blocks per SM.
-constexpr int kVadvPlacementDefault = 2;
+// integer pipe (preset 2) 980-989 us with 24 blocks per SM (1019 with 16, 1189
+// with 8: the integer sequences need more warps in flight); the pivot's
+// reciprocal alone (preset 10) 991 us; the reciprocal with five or six of the
+// products (presets 3-7, 11-15) 859-892 us, five (preset 15, the default) 861
+// us; the reciprocal with all nine 940 us (the integer pipe becomes the
+// limit).  Additions on the integer pipe cost more than they save (a binary64
+// add in integer arithmetic runs at 0.31 Tops/s against 0.52 for the fp64
+// instruction, a multiply at 0.56, a reciprocal at 0.22 against 0.12 for the
+// fp64 sequence).  The default SLAB form runs with 24 blocks per SM.
+constexpr int kVadvPlacementDefault = 15;
 constexpr int kVadvSlabBlocksPerSm = 24;
 constexpr int kVadvPlacementCount = (int)(sizeof(kVadvPlacements) / sizeof(kVadvPlacements[0]));
 template <class C>
@@ -337,6 +342,7 @@ int launch_slab(int bx, int depth, int blocks_per_sm, int placement, const Devic
                 SB_VADV_SLAB_PL(12)
                 SB_VADV_SLAB_PL(13)
                 SB_VADV_SLAB_PL(14)
+                SB_VADV_SLAB_PL(15)
 #undef SB_VADV_SLAB_PL
             }
         }

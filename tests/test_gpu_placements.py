@@ -28,7 +28,7 @@ from tests.gpu_helpers import (
 pytestmark = pytest.mark.gpu
 
 HDIFF_PRESETS = range(1, 9)
-VADV_PRESETS = range(1, 15)
+VADV_PRESETS = range(1, 16)
 
 
 def _specials(rng, shape, scale):
@@ -81,7 +81,7 @@ def test_vadv_slab_placements(preset, per_sm, nk, lib):
     assert bits_equal(got, want), f"preset {preset}, {per_sm} blocks/SM, nk {nk}: " + mismatch_report(got, want)
 
 
-@pytest.mark.parametrize("preset", [2, 5, 9, 10, 12])
+@pytest.mark.parametrize("preset", [2, 5, 9, 10, 11, 15])
 def test_vadv_slab_placements_with_specials(preset, lib):
     domain, halo = (64, 12, 30), (1, 1, 0)
     shape = tuple(d + 2 * h for d, h in zip(domain, halo))
