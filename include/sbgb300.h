@@ -281,7 +281,8 @@ typedef struct sb_batch_tune {
     int32_t vadv_block;    /* threads (= columns) per vadv block: 32 or 64 (0: 32)   */
     int32_t vadv_blocks_per_sm; /* persistent vadv blocks per SM (0: as many as fit;
                                  * with a factor workspace at most 8, or 24 when the
-                                 * float64 products run in integer arithmetic)     */
+                                 * float64 products run in integer arithmetic; at
+                                 * most 28 when given)                             */
     int32_t reserved;
 } sb_batch_tune;
 typedef struct sb_batch sb_batch;

@@ -118,7 +118,7 @@ class Slab(VerticalAdvectionMixin, base.VerticalAdvectionStencil):
     block_size = Parameter("threads per block along i (32 or 64), persistent blocks per SM (0: the library's "
                            "choice: 24 when the float64 products run in integer arithmetic, otherwise as many as "
                            "keep the factor slabs within half of L2)", (32, 0))
-    unroll_factor = Parameter("levels of inputs kept in flight (2, 4 or 8)", 4, choices=[2, 4, 8])
+    unroll_factor = Parameter("levels of inputs kept in flight (2, 4 or 8)", 2, choices=[2, 4, 8])
 
     def check_parameters(self):
         super().check_parameters()

@@ -237,6 +237,7 @@ struct Kinds {
     const void* vadv64_fn;
     int storage_bytes, compute_bytes;
     bool int_products;  // float64 slab buckets run their products in integer arithmetic
+    int vadv_depth;     // levels of inputs the vadv ring keeps in flight
     // float32 vadv with factors in tensor memory (nullptr for other compute types)
     void (*vadv_tmem)(dim3, dim3, size_t, cudaStream_t, const DevTable*, unsigned long long*, int, int);
     const void* vadv_tmem_fn;
@@ -247,11 +248,16 @@ template <class S, class C, int U, class IDX>
 void run_hdiff(dim3 g, dim3 b, cudaStream_t s, const DevTable* t, unsigned long long* c) {
     batch_hdiff_kernel<S, C, U, IDX><<<g, b, 0, s>>>(t, c);
 }
+// ring depth of a bucket kernel: 2 for the float64 slabs with the integer
+// split (as the single-domain kernel), kVadvDepth otherwise
+template <uint32_t PL>
+constexpr int kBucketDepth = PL != 0u ? 2 : kVadvDepth;
+
 template <class S, class C, int BT, class IDX, class P, bool SLAB, uint32_t PL>
 void run_vadv(dim3 g, dim3 b, size_t smem, cudaStream_t s, const DevTable* t, unsigned long long* c, int bucket,
               int cap, int ring_offset, void* slab) {
-    batch_vadv_kernel<S, C, BT, kVadvDepth, IDX, P, SLAB, PL><<<g, b, smem, s>>>(t, c, bucket, cap, ring_offset,
-                                                                                 (P*)slab);
+    batch_vadv_kernel<S, C, BT, kBucketDepth<PL>, IDX, P, SLAB, PL><<<g, b, smem, s>>>(t, c, bucket, cap,
+                                                                                       ring_offset, (P*)slab);
 }
 
 template <class S>
@@ -276,10 +282,11 @@ Kinds kinds_for() {
                                 ? kVadvDefaultIntSites
                                 : 0u;
     k.int_products = PL != 0u;
+    k.vadv_depth = kBucketDepth<PL>;
     k.vadv32 = &run_vadv<S, VC, 32, IDX, P, SLAB, PL>;
     k.vadv64 = &run_vadv<S, VC, 64, IDX, P, SLAB, PL>;
-    k.vadv32_fn = (const void*)&batch_vadv_kernel<S, VC, 32, kVadvDepth, IDX, P, SLAB, PL>;
-    k.vadv64_fn = (const void*)&batch_vadv_kernel<S, VC, 64, kVadvDepth, IDX, P, SLAB, PL>;
+    k.vadv32_fn = (const void*)&batch_vadv_kernel<S, VC, 32, kBucketDepth<PL>, IDX, P, SLAB, PL>;
+    k.vadv64_fn = (const void*)&batch_vadv_kernel<S, VC, 64, kBucketDepth<PL>, IDX, P, SLAB, PL>;
     k.storage_bytes = sizeof(typename RingOf<S>::T);  // ring entry
     k.compute_bytes = sizeof(P);                      // factor entry
     if constexpr (std::is_same<VC, float>::value && std::is_same<P, float>::value && std::is_same<IDX, int>::value) {
@@ -367,10 +374,10 @@ void release(sb_batch* b) {
     delete b;
 }
 
-size_t vadv_smem_bytes(int cap, int bt, int cbytes, int sbytes, int* ring_offset) {
+size_t vadv_smem_bytes(int cap, int bt, int cbytes, int sbytes, int depth, int* ring_offset) {
     const size_t fac = ((2 * (size_t)cbytes * cap * bt) + 15) / 16 * 16;
     if (ring_offset) *ring_offset = (int)fac;
-    return fac + (size_t)(kVadvDepth + 1) * 6 * bt * sbytes;
+    return fac + (size_t)(depth + 1) * 6 * bt * sbytes;
 }
 
 int capture_graph(sb_batch* b) {
@@ -473,6 +480,7 @@ int sb_batch_create(sb_batch** out, int storage, int compute, int max_domains, i
         b->cap[q] = (int)std::max<int64_t>(2, ceil_div(max_nk * (q + 1), kBuckets));
         // slab mode: shared memory holds the ring only (cap 0 factor levels)
         b->vadv_smem[q] = vadv_smem_bytes(k.slab ? 0 : b->cap[q], b->vadv_block, k.compute_bytes, k.storage_bytes,
+                                          k.vadv_depth,
                                           &b->ring_offset[q]);
         if ((int64_t)b->vadv_smem[q] > p->smem_optin) {
             const size_t need = b->vadv_smem[q];
@@ -482,11 +490,12 @@ int sb_batch_create(sb_batch** out, int storage, int compute, int max_domains, i
                         "use a smaller max_nk or vadv block",
                         (long long)max_nk, need, p->smem_optin);
         }
-        const int fit = (int)std::min<int64_t>(k.int_products ? 24 : 16,
+        const int fit = (int)std::min<int64_t>(k.int_products ? 28 : 16,
                                                (p->smem_optin + 1024) / (int64_t)(b->vadv_smem[q] + 1024));
         // slab mode: 8 blocks per SM by default (the slabs grow with the grid);
-        // 24 with the products in integer arithmetic, which need more warps in
-        // flight (64 domains of 512x512x80: 17.46 ms at 24, 17.69 at 16, 18.40 at 8)
+        // 24 with the float64 integer split, which needs more warps in flight
+        // (64 domains of 512x512x80 with the products in integer arithmetic:
+        // 17.46 ms at 24, 17.69 at 16, 18.40 at 8)
         const int vdef = k.slab ? std::min(fit, k.int_products ? 24 : 8) : fit;
         const int vper = b->tune.vadv_blocks_per_sm > 0 ? std::min(b->tune.vadv_blocks_per_sm, fit) : vdef;
         b->vadv_grid[q] = p->sm_count * std::max(1, vper);

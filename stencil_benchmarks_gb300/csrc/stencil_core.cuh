@@ -555,11 +555,9 @@ constexpr uint32_t kVadvProductSites = (1u << 4) | (1u << 5) | (1u << 7) | (1u <
                                        (1u << 16) | (1u << 17) | (1u << 20);
 // The level's reciprocal (site 21).
 constexpr uint32_t kVadvRcpSite = 1u << 21;
-// The float64 default: five of the products (the correction's second, the
-// right-hand side's, dcol's, the back substitution's and the output's) and
-// the reciprocal in integer arithmetic, the rest on the fp64 pipe.
-constexpr uint32_t kVadvDefaultIntSites =
-    (1u << 5) | (1u << 7) | (1u << 14) | (1u << 17) | (1u << 20) | kVadvRcpSite;
+// The float64 default: the nine products and the reciprocal in integer
+// arithmetic, the additions on the fp64 pipe.
+constexpr uint32_t kVadvDefaultIntSites = kVadvProductSites | kVadvRcpSite;
 
 // PL: integer-pipe placement mask over the operation sites 0-21 below (Mix).
 template <class S, class C, int BT, int D, class IDX, bool SLAB = false, class P = C, uint32_t PL = 0u>

@@ -66,7 +66,7 @@ __global__ void __launch_bounds__(256)
 // 14-16 dcol, 17-18 the back substitution, 19-20 the output, 21 the pivot's
 // reciprocal).  sb_tune.flags
 // bits 4-7 pick one for the SLAB form: 0 the default, 1 every site on the
-// fp64 pipe, 2.. the mixes below; SLAB shapes other than 32 threads x depth 4
+// fp64 pipe, 2.. the mixes below; SLAB shapes other than 32 threads x depth 2
 // and the SMEM-async form use the default.
 constexpr uint32_t vadv_sites(std::initializer_list<int> ks) {
     uint32_t m = 0;
@@ -85,28 +85,32 @@ constexpr uint32_t kVadvPlacements[] = {
     vadv_sites({5, 7, 14, 17}) | kVadvRcpSite,
     vadv_sites({5, 7, 14, 20}) | kVadvRcpSite,
     vadv_sites({14, 17, 20}) | kVadvRcpSite,
-    kVadvMuls | kVadvRcpSite,
+    kVadvDefaultIntSites,
     kVadvRcpSite,
     vadv_sites({4, 5, 7, 14, 17, 20}) | kVadvRcpSite,
     vadv_sites({4, 5, 7, 14, 17}) | kVadvRcpSite,
     vadv_sites({4, 5, 7, 17, 20}) | kVadvRcpSite,
     vadv_sites({4, 5, 7, 14, 16, 17, 20}) | kVadvRcpSite,
-    kVadvDefaultIntSites,
+    vadv_sites({5, 7, 14, 17, 20}) | kVadvRcpSite,
 };
-static_assert(kVadvDefaultIntSites == (vadv_sites({5, 7, 14, 17, 20}) | kVadvRcpSite), "the default split");
-// Measured at 512x512x80 (32-thread SLAB blocks, depth 4): every site on the
-// fp64 pipe 1171-1201 us whatever the blocks per SM; the nine products on the
-// integer pipe (preset 2) 980-989 us with 24 blocks per SM (1019 with 16, 1189
-// with 8: the integer sequences need more warps in flight); the pivot's
-// reciprocal alone (preset 10) 991 us; the reciprocal with five or six of the
-// products (presets 3-7, 11-15) 859-892 us, five (preset 15, the default) 861
-// us; the reciprocal with all nine 940 us (the integer pipe becomes the
-// limit).  Additions on the integer pipe cost more than they save (a binary64
-// add in integer arithmetic runs at 0.31 Tops/s against 0.52 for the fp64
-// instruction, a multiply at 0.56, a reciprocal at 0.22 against 0.12 for the
-// fp64 sequence).  The default SLAB form runs with 24 blocks per SM.
-constexpr int kVadvPlacementDefault = 15;
-constexpr int kVadvSlabBlocksPerSm = 24;
+static_assert(kVadvDefaultIntSites == (kVadvMuls | kVadvRcpSite), "the default split");
+// Measured at 512x512x80 (32-thread SLAB blocks): every site on the fp64
+// pipe 1171-1201 us whatever the blocks per SM or ring depth.  Depth 4, 24
+// blocks per SM: the nine products on the integer pipe (preset 2) 980-989 us
+// (1019 with 16 blocks per SM, 1189 with 8: the integer sequences need more
+// warps in flight); the pivot's reciprocal alone (preset 10) 991 us; the
+// reciprocal with five or six products 859-892 us, with all nine 940 us.
+// Depth 2 (a smaller ring, fewer copies in flight, more blocks fit): preset 2
+// 912 us, five products + reciprocal 817 us, all nine + reciprocal (preset 9,
+// the default) 798 us at 24 blocks per SM and 776 us at 28, where 8192
+// column groups over 4256 blocks leave no block a third group.  Additions on
+// the integer pipe cost more than they save (a binary64 add in integer
+// arithmetic runs at 0.31 Tops/s against 0.52 for the fp64 instruction, a
+// multiply at 0.56, a reciprocal at 0.22 against 0.12 for the fp64
+// sequence).  The default float64 SLAB form: depth 2, up to 28 blocks per SM,
+// the grid balanced so that every block takes the same number of groups.
+constexpr int kVadvPlacementDefault = 9;
+constexpr int kVadvSlabBlocksPerSm = 28;
 constexpr int kVadvPlacementCount = (int)(sizeof(kVadvPlacements) / sizeof(kVadvPlacements[0]));
 template <class C>
 constexpr uint32_t kVadvDefaultPlacement = std::is_same<C, double>::value ? kVadvPlacements[kVadvPlacementDefault] : 0u;
@@ -299,6 +303,13 @@ int launch_slab_one(int blocks_per_sm, const DeviceProps* p, cudaStream_t stream
     int64_t grid = std::min<int64_t>((int64_t)per_sm * p->sm_count, ngroups);
     grid = std::min<int64_t>(grid, span / (nk * BT));
     if (grid < 1) return SB_ERR_UNSUPPORTED;
+    // balance: the fewest blocks that still take every group in the same
+    // number of rounds, so that no block runs an extra round alone -- where
+    // that keeps at least 90% of the blocks (fewer warps in flight cost more:
+    // 512x512x80 at 24 blocks per SM, balanced to 18, 798 -> 850 us; at 28,
+    // balanced to 27, 798 -> 777 us)
+    const int64_t balanced = ceil_div(ngroups, ceil_div(ngroups, grid));
+    if (balanced * 10 >= grid * 9) grid = balanced;
     kernel<<<(unsigned)grid, BT, smem, stream>>>((const S*)stage, (const S*)pos, (const S*)tens, (const S*)tensstage,
                                                  (const S*)wcon, (S*)out, (C*)ccol, (C*)dcol, (int)ni, (int)nj,
                                                  (int)nk, (int)si, (int)sj, (int)sk, (int)wsh);
@@ -322,10 +333,10 @@ int launch_slab(int bx, int depth, int blocks_per_sm, int placement, const Devic
         SB_CHECK(placement >= 0 && placement < kVadvPlacementCount, SB_ERR_INVALID,
                  "vadv SLAB: placement preset %d out of range [0, %d)", placement, kVadvPlacementCount);
         if constexpr (std::is_same<C, double>::value) {
-            if (bx == 32 && depth == 4 && placement != 0) {
+            if (bx == 32 && depth == 2 && placement != 0) {
 #define SB_VADV_SLAB_PL(Q)                                                                                         \
     if (placement == Q)                                                                                            \
-        return launch_slab_one<S, C, 32, 4, kVadvPlacements[Q]>(blocks_per_sm, p, stream, stage, pos, tens,        \
+        return launch_slab_one<S, C, 32, 2, kVadvPlacements[Q]>(blocks_per_sm, p, stream, stage, pos, tens,        \
                                                                 tensstage, wcon, out, ccol, dcol, ni, nj, nk, si, \
                                                                 sj, sk, wsh);
                 SB_VADV_SLAB_PL(1)
@@ -555,7 +566,7 @@ int launch_typed(const void* stage, const void* pos, const void* tens, const voi
                             ? launch_wslab<S, C>(32, 4, 0, p, stream, stage, pos, tens, tensstage, wcon, out, ccol,
                                                  dcol, ni, nj, nk, si, sj, sk, wsh)
                             : (std::is_same<C, double>::value
-                                   ? launch_slab<S, C>(32, 4, kVadvSlabBlocksPerSm, placement, p, stream, stage, pos,
+                                   ? launch_slab<S, C>(32, 2, kVadvSlabBlocksPerSm, placement, p, stream, stage, pos,
                                                        tens, tensstage, wcon, out, ccol, dcol, ni, nj, nk, si, sj,
                                                        sk, wsh)
                                    : launch_slab<S, C>(64, 2, 32, placement, p, stream, stage, pos, tens, tensstage,
