@@ -161,6 +161,10 @@ int sb_malloc_host(void** ptr, size_t bytes); /* page-locked host memory */
 int sb_free_host(void* ptr);
 int sb_memcpy(void* dst, const void* src, size_t bytes, int kind);
 int sb_memcpy_async(void* dst, const void* src, size_t bytes, int kind, void* stream);
+/* The same copy done by the SMs instead of a copy engine (asynchronous on
+ * `stream`): any mix of device and page-locked host memory (sb_malloc_host),
+ * 16-byte vectors where both pointers are 16-byte aligned. */
+int sb_memcpy_sm(void* dst, const void* src, size_t bytes, void* stream);
 int sb_memset(void* dst, int value, size_t bytes);
 int sb_mem_info(size_t* free_bytes, size_t* total_bytes);
 

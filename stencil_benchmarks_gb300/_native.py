@@ -106,6 +106,7 @@ SIGNATURES = {
     "sb_free_host": [_vp],
     "sb_memcpy": [_vp, _vp, _size, _int],
     "sb_memcpy_async": [_vp, _vp, _size, _int, _vp],
+    "sb_memcpy_sm": [_vp, _vp, _size, _vp],
     "sb_memset": [_vp, _int, _size],
     "sb_mem_info": [ctypes.POINTER(_size), ctypes.POINTER(_size)],
     "sb_stream_create": [ctypes.POINTER(_vp)],

@@ -83,7 +83,7 @@ class Tile(HorizontalDiffusionMixin, base.HorizontalDiffusionStencil):
 class TmaTile(HorizontalDiffusionMixin, base.HorizontalDiffusionStencil):
     alignment = Parameter("data alignment in bytes (rows padded so that TMA can describe them)", 64)
     block_size = Parameter("threads along i, threads along j, rows per tile", (128, 4, 16))
-    k_per_block = Parameter("k-planes per block (double-buffered)", 4)
+    k_per_block = Parameter("k-planes per block (double-buffered)", 1)
 
     def check_parameters(self):
         super().check_parameters()

@@ -568,11 +568,14 @@ int launch_typed(const void* inp, const void* coeff, void* out, int64_t ni, int6
     // With float64 storage too, the TMA-staged tile is faster still (its
     // loads leave the issue slots to the fp64 arithmetic and overlap the
     // previous plane's compute); it needs TMA-describable strides, else TILE.
+    // 128 x 4 threads, 16-row tiles, one k-plane per block at 512x512x80:
+    // 550 us, 560 with 2 planes, 566 with 4; 8- and 12-row tiles 552-582,
+    // 24 and 32 rows 652-716 (two blocks per SM no longer fit).
     const bool auto_tile = variant == SB_VARIANT_AUTO && std::is_same<C, double>::value;
     if constexpr (std::is_same<S, double>::value && std::is_same<C, double>::value) {
         if (variant == SB_VARIANT_AUTO) {
             const int rc_tma =
-                launch_tma_placed<S, C, 128, 4>(placement, inp, coeff, out, ni, nj, nk, si, sj, sk, 16, 2, stream, p);
+                launch_tma_placed<S, C, 128, 4>(placement, inp, coeff, out, ni, nj, nk, si, sj, sk, 16, 1, stream, p);
             if (rc_tma != SB_ERR_UNSUPPORTED) return rc_tma;
         }
     }

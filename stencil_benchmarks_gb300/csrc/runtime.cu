@@ -230,6 +230,25 @@ __global__ void arith_probe_kernel(double* out, int iters, double x) {
         if (s == 12345.678) out[0] = s;
     }
 }
+// Copy through the SMs (16-byte loads and stores, 4 in flight per thread):
+// either side may be page-locked host memory, which the loads or stores then
+// reach over the host link; the tail that is not a whole vector goes bytewise.
+__global__ void __launch_bounds__(512) sm_copy_kernel(uint4* __restrict__ dst, const uint4* __restrict__ src,
+                                                      size_t nvec, unsigned char* __restrict__ dtail,
+                                                      const unsigned char* __restrict__ stail, size_t ntail) {
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    for (; i + 3 * stride < nvec; i += 4 * stride) {
+        const uint4 a = src[i], b = src[i + stride], c = src[i + 2 * stride], d = src[i + 3 * stride];
+        dst[i] = a;
+        dst[i + stride] = b;
+        dst[i + 2 * stride] = c;
+        dst[i + 3 * stride] = d;
+    }
+    for (; i < nvec; i += stride) dst[i] = src[i];
+    for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < ntail; t += stride) dtail[t] = stail[t];
+}
+
 // The integer-arithmetic binary64 operations (softf64.cuh) element-wise, for
 // checking the device build against the host's IEEE arithmetic.
 __global__ void soft_f64_kernel(int op, const double* __restrict__ a, const double* __restrict__ b,
@@ -352,6 +371,24 @@ int sb_memcpy_async(void* dst, const void* src, size_t bytes, int kind, void* st
     SB_CHECK(kind >= 0 && kind <= 4, SB_ERR_INVALID, "bad memcpy kind %d", kind);
     if (bytes == 0) return SB_OK;
     SB_CUDA(cudaMemcpyAsync(dst, src, bytes, (cudaMemcpyKind)kind, (cudaStream_t)stream));
+    return SB_OK;
+}
+
+int sb_memcpy_sm(void* dst, const void* src, size_t bytes, void* stream) {
+    clear_error();
+    SB_CHECK((dst && src) || bytes == 0, SB_ERR_INVALID, "NULL pointer");
+    if (bytes == 0) return SB_OK;
+    const DeviceProps* p;
+    int rc = device_props(&p);
+    if (rc) return rc;
+    const bool vec = ((uintptr_t)dst % 16 == 0) && ((uintptr_t)src % 16 == 0);
+    const size_t nvec = vec ? bytes / 16 : 0;
+    const int blocks = p->sm_count * 4;
+    sm_copy_kernel<<<blocks, 512, 0, (cudaStream_t)stream>>>((uint4*)dst, (const uint4*)src, nvec,
+                                                            (unsigned char*)dst + nvec * 16,
+                                                            (const unsigned char*)src + nvec * 16,
+                                                            bytes - nvec * 16);
+    SB_CUDA(cudaGetLastError());
     return SB_OK;
 }
 

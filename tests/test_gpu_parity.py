@@ -587,3 +587,27 @@ def test_vadv_full_size_fp64_against_c_oracle(lib):
     got = interior(download_like(dev["utensstage"], hosts["utensstage"]), domain, halo)
     cport.vadv(hosts["ustage"], hosts["upos"], hosts["utens"], hosts["utensstage"], hosts["wcon"], domain, halo)
     _assert_bits(got, interior(hosts["utensstage"], domain, halo), "vadv 512x512x80")
+
+
+@pytest.mark.parametrize("nbytes,offset", [(1 << 20, 0), (12345, 0), (4096 + 7, 3), (16, 0), (1, 0)])
+def test_memcpy_sm(nbytes, offset, lib):
+    """sb_memcpy_sm between page-locked host and device memory, both ways and
+    device to device, with unaligned starts and ragged tails."""
+    import ctypes
+
+    from stencil_benchmarks_gb300.device import DeviceBuffer, PinnedBuffer
+
+    rng = np.random.Generator(np.random.PCG64(nbytes))
+    src = PinnedBuffer(nbytes + 32)
+    src.array(np.uint8, (nbytes + 32,))[...] = rng.integers(0, 256, size=nbytes + 32, dtype=np.uint8)
+    dev_a, dev_b = DeviceBuffer(nbytes + 32), DeviceBuffer(nbytes + 32)
+    back = PinnedBuffer(nbytes + 32)
+    back.array(np.uint8, (nbytes + 32,))[...] = 0
+    for dst, s in ((dev_a.ptr + offset, src.ptr + offset), (dev_b.ptr, dev_a.ptr + offset),
+                   (back.ptr + offset, dev_b.ptr)):
+        _native.call("sb_memcpy_sm", ctypes.c_void_p(dst), ctypes.c_void_p(s), ctypes.c_size_t(nbytes), None)
+    _native.synchronize()
+    want = src.array(np.uint8, (nbytes + 32,))[offset:offset + nbytes]
+    got = back.array(np.uint8, (nbytes + 32,))
+    assert np.array_equal(got[offset:offset + nbytes], want)
+    assert not got[:offset].any() and not got[offset + nbytes:].any()
