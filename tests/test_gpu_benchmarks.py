@@ -21,6 +21,7 @@ require()
 import stencil_benchmarks.benchmarks_collection  # noqa: E402,F401
 from stencil_benchmarks import benchmark  # noqa: E402
 from stencil_benchmarks.benchmarks_collection.stencils import base  # noqa: E402
+from stencil_benchmarks.tools.validation import ValidationError  # noqa: E402
 
 from stencil_benchmarks_gb300 import benchmarks_collection  # noqa: E402,F401
 from stencil_benchmarks_gb300.benchmarks_collection.stencils.gb300 import (  # noqa: E402
@@ -46,13 +47,32 @@ def run_checked(b, exact=True):
     return result
 
 
+def _run_default(instance):
+    """``run()`` with the reference's verification.  Its np.isclose rejects
+    NaN == NaN, and the unseeded uniform fields occasionally hold a singular
+    float32 vadv column (a zero pivot: NaN in numpy and on the GPU alike);
+    then the outputs must match the oracle bit for bit, NaN for NaN."""
+    stencil = isinstance(instance, base.Stencil)
+    if stencil:
+        index = instance._run % instance.data_sets
+        before = copy.deepcopy(instance._data[index])
+    try:
+        return instance.run()
+    except ValidationError as err:
+        if not stencil or "nan" not in str(err):
+            raise
+        check_bit_exact(instance, before, instance._data[index])
+        return None
+
+
 @pytest.mark.parametrize("bmark", OURS, ids=lambda b: f"{b.__module__.split('.')[-1]}.{b.__name__}")
 def test_default_construction_runs_and_verifies(bmark, lib):
     instance = bmark()
-    results = instance.run()
-    results = results if isinstance(results, list) else [results]
-    assert all(r["time"] > 0 for r in results)
-    instance.run()  # a second execution
+    results = _run_default(instance)
+    if results is not None:
+        results = results if isinstance(results, list) else [results]
+        assert all(r["time"] > 0 for r in results)
+    _run_default(instance)  # a second execution
 
 
 @pytest.mark.parametrize("cls", HDIFF, ids=lambda c: c.__name__)
