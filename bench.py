@@ -376,11 +376,11 @@ def run_gpu(args, dist):
               {n: Field.like_host(va[n], "float64", VADV_HALO)
                for n in ("ustage", "upos", "utens", "utensstage", "wcon", "out", "ccol", "dcol")})
     sets = [(dev_hd, dev_va), second]
-    # uploads spread over four streams and downloads over two: with both
-    # directions of the host link busy, several copies in flight per direction
-    # carry more of its bidirectional bandwidth (one stream each: 127 GB/s per
-    # direction, eight: 155; one direction alone: 211 H2D, 193 D2H)
-    s_ins, s_outs = [Stream() for _ in range(4)], [Stream() for _ in range(2)]
+    # uploads and downloads on one stream each (spreading them over four and
+    # two streams measured slower: 6.49 against 6.67 GPoints/s; the host link
+    # carries 211 GB/s H2D and 193 GB/s D2H alone, ~127 GB/s per direction
+    # when both are busy)
+    s_ins, s_outs = [Stream()], [Stream()]
     s_in, s_out = s_ins[0], s_outs[0]
     ev_ins = [[Event(), Event()] for _ in s_ins]
     ev_outs = [[Event(), Event()] for _ in s_outs]
@@ -914,7 +914,7 @@ def main(argv=None):
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": res["h2d"],
                     "d2h_bytes_per_step": res["d2h"], "steps": res["e2e_steps"],
                     "path": "C ABI: pinned host -> sb_memcpy_async -> sb_hdiff + sb_vadv -> pinned host; "
-                            "uploads (4 streams), kernels and downloads (2 streams) over two device sets; "
+                            "uploads, kernels and downloads on three streams over two device sets; "
                             "host link measured alone: 211 GB/s H2D, 193 GB/s D2H",
                     "serial_value": 2 * POINTS * res["e2e_steps"] * dist.world / res["e2e_serial_time"] / 1e9},
             "roofline": {"bound": "hbm", "limiter": "fp64 pipe: exact fp64 arithmetic runs at 1/73 of the fp32 "
