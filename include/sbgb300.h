@@ -249,6 +249,20 @@ int sb_vadv(int storage, int compute, const void* stage, const void* pos, const 
             const void* tensstage, const void* wcon, void* out, void* ccol, void* dcol, int64_t ni,
             int64_t nj, int64_t nk, int64_t si, int64_t sj, int64_t sk, int wshift_i, int wshift_j,
             const sb_tune* tune, void* stream, double* time_s);
+/* All three components of vertical advection on one wcon field (reference:
+ * all_components=True, stencils/base.py:475-483, and its fused kernel
+ * cuda_hip/templates/vertical_advection_localmemmerged.j2): stage, pos, tens,
+ * tensstage and out are arrays of three pointers (u, v, w), every field with
+ * the same layout; u reads wcon at (i+1, j), v at (i, j+1), w at (i, j).
+ * With float32 compute on a layout the tensor-memory form takes (variant
+ * AUTO with no explicit shape and at least 2048 column groups of 32, or
+ * SB_VADV_TMEM) one launch solves the three components of each column group
+ * in turn, so wcon comes from HBM once; otherwise one sb_vadv launch per
+ * component.  Same bits either way. */
+int sb_vadv3(int storage, int compute, const void* const* stage, const void* const* pos,
+             const void* const* tens, const void* const* tensstage, const void* wcon, void* const* out,
+             void* ccol, void* dcol, int64_t ni, int64_t nj, int64_t nk, int64_t si, int64_t sj, int64_t sk,
+             const sb_tune* tune, void* stream, double* time_s);
 
 /* ---- batched execution: many domains, one persistent launch ----------------
  * No single counterpart in the reference, which launches one generated kernel

@@ -3,7 +3,8 @@
     python profile_cases.py [--warmup W] [--launches L] CASE...
 
 CASE is ``<stencil>-<form>[:<variant>[@<placement>]]`` with stencil in hdiff, vadv, vadv3 (all
-three components, one launch each on a shared wcon), triad, copy, lap and
+three components on a shared wcon, one launch each, or ``vadv3-<form>:fused`` for
+the single sb_vadv3 launch), triad, copy, lap and
 form in f64, f32, bf16 (bf16 = bfloat16 storage, f32 compute), f32x2
 (float64 storage, float-pair compute) and fix64 (float64 storage, hdiff only,
 fixed-point sums); ``all`` runs every hdiff/vadv form plus triad-f64.  Stencil cases use the 512 x 512 x 80
@@ -110,6 +111,8 @@ def run_case(name, warmup, launches, rng):
             outs = [_field(rng, storage, (1, 1, 1), 0.0, 0.0) for _ in range(3)]
 
             def launch(timed):
+                if variant == "fused":  # one sb_vadv3 launch
+                    return kernels.vadv3(comps, wcon, outs=outs, compute=compute, timed=timed)
                 total = 0.0
                 for f, o, shift in zip(comps, outs, ((1, 0), (0, 1), (0, 0))):
                     t = kernels.vadv(*f, wcon, shift, out=o, compute=compute, timed=timed)

@@ -125,6 +125,9 @@ SIGNATURES = {
     "sb_average": [_int, _int, _vp, _vp] + [_i64] * 6 + [_int, _int, _tp, _vp, _dp],
     "sb_hdiff": [_int, _int, _vp, _vp, _vp] + [_i64] * 6 + [_tp, _vp, _dp],
     "sb_vadv": [_int, _int] + [_vp] * 8 + [_i64] * 6 + [_int, _int, _tp, _vp, _dp],
+    # stage, pos, tens, tensstage: arrays of three pointers; wcon; out: three pointers; ccol, dcol
+    "sb_vadv3": [_int, _int] + [ctypes.POINTER(_vp)] * 4 + [_vp, ctypes.POINTER(_vp), _vp, _vp] + [_i64] * 6
+                + [_tp, _vp, _dp],
     "sb_vadv_noalloc": [_int, _int] + [_vp] * 6 + [_i64] * 6 + [_int, _int, _vp, _dp],
     # batch entry points take struct pointers; batching.py narrows these types
     "sb_batch_create": [ctypes.POINTER(_vp), _int, _int, _int, _i64, _vp],

@@ -7,7 +7,9 @@ fields and the in-place update of
 ``utensstage`` (and, with ``all_components``, ``vtensstage``/``wtensstage``)
 are the reference's; each component is one ``sb_vadv`` launch, with wcon read
 at the column shifted by (1, 0), (0, 1) and (0, 0) for u, v and w
-(stencils/base.py:475-483).
+(stencils/base.py:475-483), except in ``TensorMem``, where ``sb_vadv3`` solves
+the three in one launch (the reference's fused kernel:
+cuda_hip/templates/vertical_advection_localmemmerged.j2).
 
 * ``SharedMem``     -- factors in shared memory, inputs staged with cp.async;
 * ``GlobalScratch`` -- factors in the ``ccol``/``dcol`` fields at each
@@ -173,3 +175,12 @@ class TensorMem(VerticalAdvectionMixin, base.VerticalAdvectionStencil):
 
     def launch_component(self, f, named, shift, timed):
         return kernels.vadv(*f, named["wcon"], shift, compute=self.compute, tune=self.current_tune(), timed=timed)
+
+    def launch(self, fields, timed):
+        if not self.all_components:
+            return super().launch(fields, timed)
+        # u, v and w in one launch (sb_vadv3): each column group's three
+        # solves in turn, wcon from HBM once
+        comps = [f for _, f, _ in self.components(fields)]
+        named = dict(zip(self.args, fields))
+        return kernels.vadv3(comps, named["wcon"], compute=self.compute, tune=self.current_tune(), timed=timed)

@@ -435,11 +435,25 @@ int launch_wslab(int bx, int depth, int blocks_per_sm, const DeviceProps* p, cud
 // The block allocates all 512 columns and asks for enough shared memory that
 // no second block shares its SM, so the allocation never waits.
 // ---------------------------------------------------------------------------
+// The fields of up to three components on one wcon (u, v, w of the
+// reference's all_components: wcon shifted by wsh[c] elements), all with the
+// same layout; nc components are solved for each column group in turn, so a
+// group's wcon rows come from HBM once and from L2 for the others.
+template <class S>
+struct TmemComponents {
+    const S* stage[3];
+    const S* pos[3];
+    const S* tens[3];
+    const S* tensstage[3];
+    S* out[3];
+    int wsh[3];
+    int nc;
+};
+
 template <class S, int D, int KP, bool SA>
 __global__ void __launch_bounds__(512, 1)
-    vadv_tmem_kernel(const S* __restrict__ stage, const S* __restrict__ pos, const S* __restrict__ tens,
-                     const S* tensstage, const S* __restrict__ wcon, S* out, int ni, int nj, int nk, int sj, int sk,
-                     int wsh, int cpw) {
+    vadv_tmem_kernel(const TmemComponents<S> f, const S* __restrict__ wcon, int ni, int nj, int nk, int sj, int sk,
+                     int cpw) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int nwarps = blockDim.x >> 5;
@@ -462,8 +476,9 @@ __global__ void __launch_bounds__(512, 1)
         const int i0 = (int)(g % gx) * 32;
         const int j = (int)(g / gx);
         const int nvalid = min(32, ni - i0);
-        vadv_tmem_column<S, D, KP, int, SA>(stage, pos, tens, tensstage, wcon, out, i0 + j * sj, lane, nvalid, nk,
-                                            sk, wsh, tcol, ring);
+        for (int c = 0; c < f.nc; ++c)
+            vadv_tmem_column<S, D, KP, int, SA>(f.stage[c], f.pos[c], f.tens[c], f.tensstage[c], wcon, f.out[c],
+                                                i0 + j * sj, lane, nvalid, nk, sk, f.wsh[c], tcol, ring);
     }
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
     __syncthreads();
@@ -480,9 +495,9 @@ __global__ void __launch_bounds__(512, 1)
 constexpr bool kTmemSharedAddr = true;
 
 template <class S, int D>
-int launch_tmem_one(int g4, int cpw, bool sa, const DeviceProps* p, cudaStream_t stream, const void* stage,
-                    const void* pos, const void* tens, const void* tensstage, const void* wcon, void* out, int64_t ni,
-                    int64_t nj, int64_t nk, int64_t sj, int64_t sk, int64_t wsh) {
+int launch_tmem_one(int g4, int cpw, bool sa, const DeviceProps* p, cudaStream_t stream,
+                    const TmemComponents<S>& comps, const void* wcon, int64_t ni, int64_t nj, int64_t nk, int64_t sj,
+                    int64_t sk) {
     const int64_t kmod = ((int64_t)sk * (int64_t)sizeof(S)) % 16;
     auto kernel = kmod == 0 ? (sa ? vadv_tmem_kernel<S, D, 1, true> : vadv_tmem_kernel<S, D, 1, false>)
                   : kmod == 8 ? (sa ? vadv_tmem_kernel<S, D, 2, true> : vadv_tmem_kernel<S, D, 2, false>)
@@ -497,9 +512,8 @@ int launch_tmem_one(int g4, int cpw, bool sa, const DeviceProps* p, cudaStream_t
     SB_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const int64_t ngroups = ceil_div(ni, (int64_t)32) * nj;
     const int64_t grid = std::min<int64_t>(p->sm_count, ceil_div(ngroups, (int64_t)nwarps));
-    kernel<<<(unsigned)grid, 32 * nwarps, smem, stream>>>((const S*)stage, (const S*)pos, (const S*)tens,
-                                                          (const S*)tensstage, (const S*)wcon, (S*)out, (int)ni,
-                                                          (int)nj, (int)nk, (int)sj, (int)sk, (int)wsh, cpw);
+    kernel<<<(unsigned)grid, 32 * nwarps, smem, stream>>>(comps, (const S*)wcon, (int)ni, (int)nj, (int)nk,
+                                                          (int)sj, (int)sk, cpw);
     return SB_OK;
 }
 
@@ -507,9 +521,8 @@ int launch_tmem_one(int g4, int cpw, bool sa, const DeviceProps* p, cudaStream_t
 // positive strides, 32-bit offsets, 2 <= nk <= 256); SB_ERR_UNSUPPORTED
 // otherwise.  depth 0 = the deepest ring that fits.
 template <class S, class C>
-int launch_tmem(int depth, bool sa, const DeviceProps* p, cudaStream_t stream, const void* stage, const void* pos,
-                const void* tens, const void* tensstage, const void* wcon, void* out, int64_t ni, int64_t nj,
-                int64_t nk, int64_t si, int64_t sj, int64_t sk, int64_t wsh) {
+int launch_tmem_comps(int depth, bool sa, const DeviceProps* p, cudaStream_t stream, const TmemComponents<S>& comps,
+                      const void* wcon, int64_t ni, int64_t nj, int64_t nk, int64_t si, int64_t sj, int64_t sk) {
     if constexpr (!std::is_same<C, float>::value) {
         return SB_ERR_UNSUPPORTED;
     } else {
@@ -520,13 +533,29 @@ int launch_tmem(int depth, bool sa, const DeviceProps* p, cudaStream_t stream, c
         const int g4 = std::min(4, 512 / cpw);             // warps per TMEM lane quarter
         int rc = SB_ERR_UNSUPPORTED;
         if ((depth == 0 || depth == 16) && rc == SB_ERR_UNSUPPORTED)
-            rc = launch_tmem_one<S, 16>(g4, cpw, sa, p, stream, stage, pos, tens, tensstage, wcon, out, ni, nj, nk, sj, sk, wsh);
+            rc = launch_tmem_one<S, 16>(g4, cpw, sa, p, stream, comps, wcon, ni, nj, nk, sj, sk);
         if ((depth == 0 || depth == 8) && rc == SB_ERR_UNSUPPORTED)
-            rc = launch_tmem_one<S, 8>(g4, cpw, sa, p, stream, stage, pos, tens, tensstage, wcon, out, ni, nj, nk, sj, sk, wsh);
+            rc = launch_tmem_one<S, 8>(g4, cpw, sa, p, stream, comps, wcon, ni, nj, nk, sj, sk);
         if (depth == 4 && rc == SB_ERR_UNSUPPORTED)
-            rc = launch_tmem_one<S, 4>(g4, cpw, sa, p, stream, stage, pos, tens, tensstage, wcon, out, ni, nj, nk, sj, sk, wsh);
+            rc = launch_tmem_one<S, 4>(g4, cpw, sa, p, stream, comps, wcon, ni, nj, nk, sj, sk);
         return rc;
     }
+}
+
+// one component
+template <class S, class C>
+int launch_tmem(int depth, bool sa, const DeviceProps* p, cudaStream_t stream, const void* stage, const void* pos,
+                const void* tens, const void* tensstage, const void* wcon, void* out, int64_t ni, int64_t nj,
+                int64_t nk, int64_t si, int64_t sj, int64_t sk, int64_t wsh) {
+    TmemComponents<S> comps{};
+    comps.stage[0] = (const S*)stage;
+    comps.pos[0] = (const S*)pos;
+    comps.tens[0] = (const S*)tens;
+    comps.tensstage[0] = (const S*)tensstage;
+    comps.out[0] = (S*)out;
+    comps.wsh[0] = (int)wsh;
+    comps.nc = 1;
+    return launch_tmem_comps<S, C>(depth, sa, p, stream, comps, wcon, ni, nj, nk, si, sj, sk);
 }
 
 template <class S, class C>
@@ -630,10 +659,94 @@ int launch_typed(const void* stage, const void* pos, const void* tens, const voi
                                     ccol, dcol, ni, nj, nk, si, sj, sk, wsh);
 }
 
+// All three components (the reference's all_components,
+// stencils/base.py:475-483; its fused kernel: cuda_hip/templates/
+// vertical_advection_localmemmerged.j2): with float32 compute on a layout the
+// tensor-memory form takes, one launch solves u, v and w of each column group
+// in turn (wcon read from HBM once); otherwise one launch per component.
+template <class S, class C>
+int launch_typed3(const void* const* stage, const void* const* pos, const void* const* tens,
+                  const void* const* tensstage, const void* wcon, void* const* out, void* ccol, void* dcol,
+                  int64_t ni, int64_t nj, int64_t nk, int64_t si, int64_t sj, int64_t sk, const sb_tune* tune,
+                  cudaStream_t stream) {
+    const int64_t wsh[3] = {si, sj, 0};  // u: wcon at (i+1, j); v: (i, j+1); w: (i, j)
+    const int variant = tune ? tune->variant : SB_VARIANT_AUTO;
+    if constexpr (std::is_same<C, float>::value) {
+        const bool auto_fused = variant == SB_VARIANT_AUTO &&
+                                !(tune && (tune->block_x || tune->block_y || tune->unroll)) &&
+                                ceil_div(ni, (int64_t)32) * nj >= 2048 &&
+                                (sizeof(S) == 4 || (sk * (int64_t)sizeof(S)) % 8 == 0);
+        if (auto_fused || variant == SB_VADV_TMEM) {
+            const DeviceProps* p;
+            int rc = device_props(&p);
+            if (rc) return rc;
+            TmemComponents<S> comps{};
+            for (int c = 0; c < 3; ++c) {
+                comps.stage[c] = (const S*)stage[c];
+                comps.pos[c] = (const S*)pos[c];
+                comps.tens[c] = (const S*)tens[c];
+                comps.tensstage[c] = (const S*)tensstage[c];
+                comps.out[c] = (S*)out[c];
+                comps.wsh[c] = (int)wsh[c];
+            }
+            comps.nc = 3;
+            const int d = (tune && tune->unroll > 0) ? tune->unroll : (variant == SB_VADV_TMEM ? 0 : 8);
+            SB_CHECK(d == 0 || d == 4 || d == 8 || d == 16, SB_ERR_INVALID, "vadv TMEM ring depth must be 4, 8 or 16");
+            const bool sa =
+                tune && (tune->flags & 0x400) ? true : (tune && (tune->flags & 0x800) ? false : kTmemSharedAddr);
+            const int arc = launch_tmem_comps<S, C>(d, sa, p, stream, comps, wcon, ni, nj, nk, si, sj, sk);
+            if (arc != SB_ERR_UNSUPPORTED) return arc;
+            SB_CHECK(variant != SB_VADV_TMEM, SB_ERR_UNSUPPORTED,
+                     "vadv TMEM variant: needs float32 compute, i unit-stride, positive strides, 32-bit offsets and "
+                     "2 <= nk <= 256");
+        }
+    }
+    for (int c = 0; c < 3; ++c) {
+        const int rc = launch_typed<S, C>(stage[c], pos[c], tens[c], tensstage[c], wcon, out[c], ccol, dcol, ni, nj,
+                                          nk, si, sj, sk, wsh[c], tune, stream);
+        if (rc) return rc;
+    }
+    return SB_OK;
+}
+
 }  // namespace
 }  // namespace sb
 
 using namespace sb;
+
+extern "C" int sb_vadv3(int storage, int compute, const void* const* stage, const void* const* pos,
+                        const void* const* tens, const void* const* tensstage, const void* wcon, void* const* out,
+                        void* ccol, void* dcol, int64_t ni, int64_t nj, int64_t nk, int64_t si, int64_t sj,
+                        int64_t sk, const sb_tune* tune, void* stream, double* time_s) {
+    clear_error();
+    int rc = check_domain(ni, nj, nk, si, sj, sk);
+    if (rc) return rc;
+    SB_CHECK(stage && pos && tens && tensstage && out && wcon, SB_ERR_INVALID, "NULL field array");
+    for (int c = 0; c < 3; ++c)
+        SB_CHECK(stage[c] && pos[c] && tens[c] && tensstage[c] && out[c], SB_ERR_INVALID,
+                 "NULL field pointer (component %d)", c);
+    SB_CHECK((storage == SB_F64 && (compute == SB_F64 || compute == SB_F32X2)) ||
+                 (storage == SB_F32 && (compute == SB_F32 || compute == SB_F64)) ||
+                 (storage == SB_BF16 && compute == SB_F32),
+             SB_ERR_UNSUPPORTED, "unsupported storage/compute combination (%d, %d)", storage, compute);
+    if (ni == 0 || nj == 0 || nk == 0) {
+        if (time_s) *time_s = 0.0;
+        return SB_OK;
+    }
+    SB_CHECK(nk >= 2, SB_ERR_INVALID, "vertical advection needs at least 2 levels (nk = %lld)", (long long)nk);
+    cudaStream_t s = (cudaStream_t)stream;
+    return timed(s, time_s, [&]() {
+        if (storage == SB_F64 && compute == SB_F64)
+            return launch_typed3<double, double>(stage, pos, tens, tensstage, wcon, out, ccol, dcol, ni, nj, nk, si, sj, sk, tune, s);
+        if (storage == SB_F64 && compute == SB_F32X2)
+            return launch_typed3<double, f32x2>(stage, pos, tens, tensstage, wcon, out, ccol, dcol, ni, nj, nk, si, sj, sk, tune, s);
+        if (storage == SB_F32 && compute == SB_F32)
+            return launch_typed3<float, float>(stage, pos, tens, tensstage, wcon, out, ccol, dcol, ni, nj, nk, si, sj, sk, tune, s);
+        if (storage == SB_F32 && compute == SB_F64)
+            return launch_typed3<float, double>(stage, pos, tens, tensstage, wcon, out, ccol, dcol, ni, nj, nk, si, sj, sk, tune, s);
+        return launch_typed3<bf16, float>(stage, pos, tens, tensstage, wcon, out, ccol, dcol, ni, nj, nk, si, sj, sk, tune, s);
+    });
+}
 
 extern "C" int sb_vadv(int storage, int compute, const void* stage, const void* pos, const void* tens,
                        const void* tensstage, const void* wcon, void* out, void* ccol, void* dcol,

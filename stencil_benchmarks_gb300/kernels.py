@@ -87,6 +87,40 @@ def vadv(stage: Field, pos: Field, tens: Field, tensstage: Field, wcon: Field, s
     return _launch("sb_vadv", args, timed)
 
 
+def vadv3(components, wcon: Field, ccol: Field | None = None, dcol: Field | None = None, outs=None, compute=None,
+          tune=None, stream=None, timed=False):
+    """All three components, u, v, w, on one wcon (wcon read at (1, 0), (0, 1)
+    and (0, 0)): ``components`` = three (stage, pos, tens, tensstage) tuples;
+    the new tensstages go to ``outs`` (default: the tensstages in place).  One
+    fused launch where the tensor-memory form applies (float32 compute), else
+    one launch per component."""
+    comps = [tuple(c) for c in components]
+    if len(comps) != 3 or any(len(c) != 4 for c in comps):
+        raise ValueError("vadv3 takes three (stage, pos, tens, tensstage) tuples")
+    outs = [c[3] for c in comps] if outs is None else list(outs)
+    fields = [f for c in comps for f in c] + [wcon] + outs
+    _check_same_layout(*fields)
+    if any(h < 1 for h in wcon.halo[:2]):
+        raise ValueError(f"vertical advection of u and v needs a halo >= 1 along i and j (got {wcon.halo})")
+    for scratch in (ccol, dcol):
+        if scratch is not None and scratch.strides != wcon.strides:
+            raise ValueError("ccol/dcol scratch fields must have the same strides as the other fields")
+    ni, nj, nk = _domain(wcon)
+    arr = ctypes.c_void_p * 3
+
+    def ptrs(k):
+        return arr(*(c[k].interior_ptr for c in comps))
+
+    args = [
+        _native.storage_code(wcon.storage), _compute_code(wcon.storage, compute),
+        ptrs(0), ptrs(1), ptrs(2), ptrs(3), ctypes.c_void_p(wcon.interior_ptr), arr(*(o.interior_ptr for o in outs)),
+        ctypes.c_void_p(ccol.interior_ptr) if ccol is not None else None,
+        ctypes.c_void_p(dcol.interior_ptr) if dcol is not None else None,
+        ni, nj, nk, *wcon.strides, _tune_arg(tune), _stream_arg(stream),
+    ]
+    return _launch("sb_vadv3", args, timed)
+
+
 def copy(inp: Field, out: Field, tune=None, stream=None, timed=False):
     _check_same_layout(inp, out)
     ni, nj, nk = _domain(inp)

@@ -611,3 +611,61 @@ def test_memcpy_sm(nbytes, offset, lib):
     got = back.array(np.uint8, (nbytes + 32,))
     assert np.array_equal(got[offset:offset + nbytes], want)
     assert not got[:offset].any() and not got[offset + nbytes:].any()
+
+
+def _run_vadv3(domain, halo, storage, compute, tune=None, seed=0, use_scratch=False):
+    """sb_vadv3 on u, v, w fields sharing one wcon; returns (got, want) lists."""
+    shape = tuple(d + 2 * h for d, h in zip(domain, halo))
+    names = [f"{c}{n}" for c in "uvw" for n in ("stage", "pos", "tens", "tensstage")] + ["wcon"]
+    dists = {n: (-1.0, 1.0) for n in names}
+    dists["wcon"] = (-0.5, 0.5)
+    vals = rng_fields(seed, shape, names, dists)
+    hosts = {n: host_field(v, storage, halo=halo) for n, v in vals.items()}
+    dev = {n: to_device(h, storage, halo) for n, h in hosts.items()}
+    scratch = {}
+    if use_scratch:
+        for n in ("ccol", "dcol"):
+            hosts[n] = host_field(np.zeros(shape), "float64" if compute == "float64" else storage, halo=halo)
+            scratch[n] = to_device(hosts[n], "float64" if compute == "float64" else storage, halo)
+    comps = [tuple(dev[f"{c}{n}"] for n in ("stage", "pos", "tens", "tensstage")) for c in "uvw"]
+    outs = []
+    for c in "uvw":
+        hosts[f"{c}out"] = host_field(np.zeros(shape), storage, halo=halo)
+        dev[f"{c}out"] = to_device(hosts[f"{c}out"], storage, halo)
+        outs.append(dev[f"{c}out"])
+    kernels.vadv3(comps, dev["wcon"], outs=outs, compute=compute, tune=tune, **scratch)
+    _native.synchronize()
+    got, want = [], []
+    oracle = "float64" if compute == "float32x2" else compute  # float pairs against the float64 oracle
+    for c, shift in zip("uvw", ((1, 0), (0, 1), (0, 0))):
+        got.append(interior(download_like(dev[f"{c}out"], hosts[f"{c}out"]), domain, halo))
+        f = {n: compute_view(hosts[f"{c}{n}"], storage, oracle) for n in ("stage", "pos", "tens", "tensstage")}
+        with np.errstate(all="ignore"):
+            comp = ora._vadv_component(f["stage"], f["pos"], f["tens"], f["tensstage"],
+                                       compute_view(hosts["wcon"], storage, oracle), domain, halo, *shift)
+        want.append(round_to_storage(comp, storage))
+    # the in-place inputs are untouched when outputs go elsewhere
+    return got, want
+
+
+@pytest.mark.parametrize("storage,compute,tune,domain", [
+    ("float32", "float32", {"variant": _native.VADV_TMEM}, (70, 33, 17)),    # fused, explicit, ragged
+    ("bfloat16", "float32", {"variant": _native.VADV_TMEM}, (64, 20, 9)),    # fused, 2-byte storage
+    ("float32", "float32", None, (128, 512, 12)),                            # fused under AUTO (2048 groups)
+    ("float32", "float32", None, (40, 30, 11)),                               # AUTO, small: three launches
+    ("float64", "float64", None, (45, 20, 13)),                               # three launches, exact fp64
+    ("float64", "float32x2", None, (33, 17, 7)),                              # three launches, float pair
+])
+def test_vadv3_all_components(storage, compute, tune, domain, lib):
+    """sb_vadv3 (u, v, w on one wcon; fused into one launch where the
+    tensor-memory form applies): every component bit-identical to the oracle,
+    or within the float-pair tolerance."""
+    t = _native.tune(**tune) if tune else None
+    got, want = _run_vadv3(domain, (1, 1, 1), storage, compute, tune=t, seed=sum(domain),
+                           use_scratch=compute == "float32x2")
+    for c, g, w in zip("uvw", got, want):
+        if compute == "float32x2":
+            scale = np.max(np.abs(w))
+            assert np.max(np.abs(g - w)) <= 1e-9 * scale, f"vadv3 {c} {storage}/{compute}"
+        else:
+            _assert_bits(g, w, f"vadv3 {c} {storage}/{compute} {tune}")
