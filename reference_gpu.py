@@ -1,7 +1,9 @@
 """The reference's own CUDA kernels and this package's kernels, timed on the
 same GPU through the same Benchmark API.
 
-    python reference_gpu.py [--dtypes float64,float32] [--runs 5] [--only hdiff,vadv,basic,stream]
+    python reference_gpu.py [--dtypes float64,float32] [--runs 5] [--only hdiff,vadv,vadv3,basic,stream]
+
+(vadv3: all three components, the reference's all_components=True)
 
 Reference side: the cuda_hip backend exactly as the reference ships it -- each
 class renders its template and compiles it with nvcc (`-arch sm_103a`) in
@@ -167,8 +169,11 @@ def stencil_cases(rows, dtypes, runs, only):
     ref_common = {"compiler": nvcc, "gpu_architecture": "sm_103a", "dry_runs": 1, "alignment": ALIGNMENT,
                   "verify": True}
     ours_common = {"dry_runs": 1, "alignment": ALIGNMENT, "verify": True}
+    all3 = {"all_components": True}
     groups = [("hdiff", rhd, REF_HDIFF, ohd, OURS_HDIFF, HALO),
               ("vadv", rva, REF_VADV, ova, OURS_VADV, HALO),
+              ("vadv3", rva, [(n, dict(k, **all3)) for n, k in REF_VADV], ova,
+               [(n, dict(k, **all3)) for n, k in OURS_VADV], HALO),
               ("basic", rbasic, REF_BASIC, obasic, [(n, dict(k)) for n, k in REF_BASIC], BASIC_HALO)]
     for dtype in dtypes:
         for seed, (stencil, rmod, rcases, omod, ocases, halo) in enumerate(groups):
@@ -176,12 +181,12 @@ def stencil_cases(rows, dtypes, runs, only):
                 continue
             for name, kw in rcases:
                 kw = dict(kw)
-                if stencil == "vadv" and name == "SharedMem" and dtype == "float64":
+                if stencil in ("vadv", "vadv3") and name == "SharedMem" and dtype == "float64":
                     kw["block_size"] = (32, 1)
                 if stencil == "basic":
                     kw.update(loop="3D", block_size=(128, 2, 1))
                 args = dict(ref_common, domain=kw.pop("domain", DOMAIN), halo=halo, dtype=dtype, **kw)
-                if stencil == "vadv":
+                if stencil in ("vadv", "vadv3"):
                     args["dry_runs"] = 0  # utensstage is read and written: a dry run changes the verified input
                 run_case(rows, f"{stencil}" if stencil != "basic" else name, dtype, "reference cuda_hip", name,
                          getattr(rmod, name), args, runs, seed)
@@ -189,7 +194,7 @@ def stencil_cases(rows, dtypes, runs, only):
                 if name == "TensorMem" and dtype == "float64":
                     continue
                 args = dict(ours_common, domain=DOMAIN, halo=halo, dtype=dtype, **kw)
-                if stencil == "vadv":
+                if stencil in ("vadv", "vadv3"):
                     args["dry_runs"] = 0
                 run_case(rows, f"{stencil}" if stencil != "basic" else name, dtype, "gb300", name,
                          getattr(omod, name), args, runs, seed)
@@ -259,7 +264,7 @@ def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
     ap.add_argument("--dtypes", default="float64,float32")
     ap.add_argument("--runs", type=int, default=5)
-    ap.add_argument("--only", default="hdiff,vadv,basic,stream")
+    ap.add_argument("--only", default="hdiff,vadv,vadv3,basic,stream")
     args = ap.parse_args(argv)
     _ensure_cudart()
     from stencil_benchmarks_gb300 import host
