@@ -156,7 +156,10 @@ SB_SF_HD bool mul(uint64_t a, uint64_t b, uint64_t& r) {
         }
         return false;
     }
-    const uint64_t xa = ((a & kMant) | kImplicit) << 11, xb = ((b & kMant) | kImplicit) << 11;
+    // significands with the implicit bit, shifted to the top: a << 11 moves the
+    // exponent out except its lowest bit, which lands on bit 63, where the
+    // implicit bit belongs (normal operands only, checked above)
+    const uint64_t xa = (a << 11) | kSign, xb = (b << 11) | kSign;
     uint64_t hi = mulhi64(xa, xb);
     hi |= (uint64_t)((xa * xb) != 0);  // sticky: the low half
     const int n = (int)(~hi >> 63);     // 1 when the product is below 2^127
@@ -238,7 +241,7 @@ SB_SF_HD bool rcp(uint64_t a, uint64_t& r) {
         r = sign | ((uint64_t)(2046u - ea) << 52);
         return true;
     }
-    const uint64_t d = (frac | kImplicit) << 11;
+    const uint64_t d = (a << 11) | kSign;  // the significand at the top (as in mul)
     // first step on d's top 32 bits: y0 ~ 2^62 / dh (31 bits), E = 2^62 - dh y0
     // (|E| < 2^43), y1 = y0 2^32 + y0 E / 2^30 ~ 2^94 / dh = u (1 + eta),
     // |eta| < 2^-30 (the truncation of d dominates the squared seed error)
