@@ -503,8 +503,15 @@ def _fma_exact(b, s, c):
     return out
 
 
+STREAM_GRIDS = [None, {"variant": _native.STREAM_GRID_STRIDE, "block_x": 512, "unroll": 4},
+                {"variant": _native.STREAM_GRID_CHUNK, "block_x": 1024, "unroll": 2},
+                {"variant": _native.STREAM_GRID_CHUNK, "block_x": 256, "unroll": 8},
+                {"variant": _native.STREAM_GRID_CHUNK, "block_x": 96, "unroll": 1}]
+
+
+@pytest.mark.parametrize("grid", range(len(STREAM_GRIDS)))
 @pytest.mark.parametrize("n,offset", [(1 << 16, 0), ((1 << 16) + 3, 0), (1000, 1), (5, 0)])
-def test_stream_ops(n, offset, lib):
+def test_stream_ops(n, offset, grid, lib):
     from stencil_benchmarks_gb300.device import DeviceBuffer, copy_to_device, copy_to_host
 
     rng = np.random.Generator(np.random.PCG64(31))
@@ -520,18 +527,19 @@ def test_stream_ops(n, offset, lib):
         copy_to_host(x, p)
         return x
 
+    t = _native.tune(**STREAM_GRIDS[grid]) if STREAM_GRIDS[grid] else None
     for p, x in zip(ptrs, (a0, b0, c0)):
         put(p, x)
-    kernels.stream_op(_native.STREAM_COPY, "float64", *ptrs, n)
+    kernels.stream_op(_native.STREAM_COPY, "float64", *ptrs, n, tune=t)
     assert np.array_equal(get(ptrs[2]), a0)
     put(ptrs[2], c0)
-    kernels.stream_op(_native.STREAM_SCALE, "float64", *ptrs, n, 3.0)
+    kernels.stream_op(_native.STREAM_SCALE, "float64", *ptrs, n, 3.0, tune=t)
     assert bits_equal(get(ptrs[1]), 3.0 * c0)
     put(ptrs[1], b0)
-    kernels.stream_op(_native.STREAM_ADD, "float64", *ptrs, n)
+    kernels.stream_op(_native.STREAM_ADD, "float64", *ptrs, n, tune=t)
     assert bits_equal(get(ptrs[2]), a0 + b0)
     put(ptrs[2], c0)
-    kernels.stream_op(_native.STREAM_TRIAD, "float64", *ptrs, n, 3.0)
+    kernels.stream_op(_native.STREAM_TRIAD, "float64", *ptrs, n, 3.0, tune=t)
     got = get(ptrs[0])
     sample = slice(0, min(n, 2000))
     assert bits_equal(got[sample], _fma_exact(b0[sample], 3.0, c0[sample]))
@@ -669,3 +677,15 @@ def test_vadv3_all_components(storage, compute, tune, domain, lib):
             assert np.max(np.abs(g - w)) <= 1e-9 * scale, f"vadv3 {c} {storage}/{compute}"
         else:
             _assert_bits(g, w, f"vadv3 {c} {storage}/{compute} {tune}")
+
+
+def test_stream_rejects_bad_grid(lib):
+    from stencil_benchmarks_gb300.device import DeviceBuffer
+
+    bufs = [DeviceBuffer(64 * 8) for _ in range(3)]
+    for bad in ({"variant": 3}, {"variant": _native.STREAM_GRID_STRIDE, "block_x": 1024},
+                {"variant": _native.STREAM_GRID_CHUNK, "block_x": 2048},
+                {"variant": _native.STREAM_GRID_CHUNK, "unroll": 3}):
+        with pytest.raises(_native.SbError) as err:
+            kernels.stream_op(_native.STREAM_COPY, "float64", *(b.ptr for b in bufs), 64, tune=_native.tune(**bad))
+        assert err.value.code == _native.SB_ERR_INVALID
