@@ -58,6 +58,32 @@ def test_vadv_argument_checks(lib):
     assert vadv(lib, F64, FIX64) == UNSUPPORTED  # fixed point is hdiff only
 
 
+def test_vadv3_checks(lib):
+    arr = ctypes.c_void_p * 3
+    good = arr(P, P, P)
+    holey = arr(P, NULL, P)
+
+    def call(stage=good, out=good, storage=F64, compute=F64, nk=4):
+        return lib.sb_vadv3(storage, compute, stage, good, good, good, P, out, None, None, 8, 8, nk, 1, 10, 100,
+                            None, None, None)
+
+    assert call(stage=holey) == INVALID and "component 1" in _msg()
+    assert call(out=holey) == INVALID
+    assert lib.sb_vadv3(F64, F64, None, good, good, good, P, good, None, None, 8, 8, 4, 1, 10, 100,
+                        None, None, None) == INVALID
+    assert call(nk=1) == INVALID and "2 levels" in _msg()
+    assert call(storage=BF16, compute=F64) == UNSUPPORTED
+    assert call(nk=0) == OK  # empty domain: no launch
+
+
+def test_copy_helpers_checks(lib):
+    assert lib.sb_memcpy_sm(NULL, P, 16, None) == INVALID
+    assert lib.sb_memcpy_sm(NULL, NULL, 0, None) == OK
+    assert lib.sb_debug_soft_f64(4, P, P, P, 8, None) == INVALID and "reciprocal" in _msg()
+    assert lib.sb_debug_soft_f64(0, P, NULL, P, 8, None) == INVALID  # add needs b
+    assert lib.sb_debug_soft_f64(3, P, NULL, P, 0, None) == OK  # the reciprocal ignores b
+
+
 def test_basic_and_stream_checks(lib):
     assert lib.sb_laplacian(F64, F64, P, P, 8, 8, 4, 1, 10, 100, 9, None, None, None) == INVALID
     assert lib.sb_average(F64, F64, P, P, 8, 8, 4, 1, 10, 100, 3, 0, None, None, None) == INVALID
