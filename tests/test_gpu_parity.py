@@ -574,7 +574,7 @@ def test_stream_reference_sequence(dtype, lib, golden):
 
 
 # ---------------------------------------------------------------------------
-# full-size BASELINE configurations (512 x 512 x 80, fp64)
+# the full-size workload (512 x 512 x 80, fp64)
 # ---------------------------------------------------------------------------
 
 
