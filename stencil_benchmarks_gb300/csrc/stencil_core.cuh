@@ -1125,7 +1125,7 @@ __device__ __forceinline__ void vadv_tmem_column(const S* __restrict__ stage, co
     }
     tmem_wait_st();
 
-    // ---- backward sweep: pos(k) of level k staged in slot (nk-2-k) % R
+    // ---- backward sweep: pos(k) of level k staged in row slot k % 8
     const unsigned char* const gb0 = (const unsigned char*)(pos + col0);
     const unsigned mis_p = (unsigned)((uintptr_t)gb0 & 15u);
     const unsigned char* bg[2][MB];
@@ -1144,7 +1144,13 @@ __device__ __forceinline__ void vadv_tmem_column(const S* __restrict__ stage, co
             bg[q][m] = KP ? gb0 - mq + 16 * (buse[q][m] ? bidx[m] : 0) : gb0;
         }
     }
-    auto issue_b = [&](int slot, int k) {
+    // backward ring: 8 row slots of ROWB bytes in the ring's memory, level k in
+    // slot k % 8 (so the slot of each level of an 8-level TMEM block is a
+    // constant), DB = 7 levels in flight: the slot refilled after reading level
+    // k is level k+1's, which every lane has read by the __syncwarp
+    constexpr int DB = 7;
+    static_assert(8 * ROWB <= R * SLOT, "the backward slots fit in the ring");
+    auto issue_b = [&](int bslot, int k) {
         if (k >= 0) {
             const int64_t kb = (int64_t)k * kstep;
 #pragma unroll
@@ -1153,15 +1159,15 @@ __device__ __forceinline__ void vadv_tmem_column(const S* __restrict__ stage, co
                     const bool odd = KP == 2 && (k & 1);
                     const bool use = odd ? buse[1][m] : buse[0][m];
                     if constexpr (SA) {
-                        if (use) cp_async16_s(ring_s + slot * SLOT + bdst[m], (const void*)((odd ? bg[1][m] : bg[0][m]) + kb));
+                        if (use) cp_async16_s(ring_s + bslot * ROWB + bdst[m], (const void*)((odd ? bg[1][m] : bg[0][m]) + kb));
                     } else {
-                        if (use) cp_async<16>(ring + slot * SLOT + bdst[m], (const void*)((odd ? bg[1][m] : bg[0][m]) + kb));
+                        if (use) cp_async<16>(ring + bslot * ROWB + bdst[m], (const void*)((odd ? bg[1][m] : bg[0][m]) + kb));
                     }
                 } else {
                     const uintptr_t a = (uintptr_t)(bg[0][m] + kb);
                     const int n = (int)(((a & 15u) + (unsigned)nbytes + 15u) >> 4);
                     if (bidx[m] < n)
-                        cp_async<16>(ring + slot * SLOT + bdst[m],
+                        cp_async<16>(ring + bslot * ROWB + bdst[m],
                                      (const void*)((a & ~(uintptr_t)15) + 16 * bidx[m]));
                 }
             }
@@ -1169,7 +1175,7 @@ __device__ __forceinline__ void vadv_tmem_column(const S* __restrict__ stage, co
         cp_async_commit();
     };
 #pragma unroll
-    for (int u = 0; u < D; ++u) issue_b(u, nk - 2 - u);
+    for (int u = 0; u < DB; ++u) issue_b((nk - 2 - u) & 7, nk - 2 - u);
     C data = dp;
     if (valid) {
         const IDX o = col + (IDX)(nk - 1) * sk;
@@ -1180,32 +1186,29 @@ __device__ __forceinline__ void vadv_tmem_column(const S* __restrict__ stage, co
     const uint32_t prow0_s = ring_s + mis_p + (uint32_t)(lane * ES);
     const uint32_t prow1_s = ring_s + ((mis_p + kph) & 15u) + (uint32_t)(lane * ES);
     S* optr = out + col;
-    int slot = 0;  // ring slot of the next level
     for (int w = (nk - 2) >> 3; w >= 0; --w) {
         float f[16];  // ccol, dcol of levels 8w .. 8w+7
         tmem_ld16(tcol + 16u * (uint32_t)w, f);
 #pragma unroll
         for (int q = 7; q >= 0; --q) {
-            const int k = 8 * w + q;
+            const int k = 8 * w + q;  // in slot q
             if (k > nk - 2) continue;  // uniform
-            cp_async_wait<D - 1>();
+            cp_async_wait<DB - 1>();
             __syncwarp();
             C p0;
             if constexpr (KP > 0 && SA) {
-                const bool odd = KP == 2 && (k & 1);
-                p0 = cvt<C, S>(lds<S>((odd ? prow1_s : prow0_s) + (uint32_t)(slot * SLOT)));
+                const bool odd = KP == 2 && (q & 1);
+                p0 = cvt<C, S>(lds<S>((odd ? prow1_s : prow0_s) + (uint32_t)(q * ROWB)));
             } else if constexpr (KP > 0) {
-                const bool odd = KP == 2 && (k & 1);
-                p0 = cvt<C, S>(*(const S*)((odd ? prow1 : prow0) + slot * SLOT));
+                const bool odd = KP == 2 && (q & 1);
+                p0 = cvt<C, S>(*(const S*)((odd ? prow1 : prow0) + q * ROWB));
             } else {
                 const unsigned kp = (unsigned)(((int64_t)k * kstep) & 15);
-                p0 = cvt<C, S>(((const S*)(ring + slot * SLOT + ((mis_p + kp) & 15u)))[lane]);
+                p0 = cvt<C, S>(((const S*)(ring + q * ROWB + ((mis_p + kp) & 15u)))[lane]);
             }
-            const int refill = slot + D >= R ? slot + D - R : slot + D;  // the previous level's slot
-            issue_b(refill, k - D);
+            issue_b((q + 1) & 7, k - DB);  // (k - 7) % 8: the slot of level k+1
             data = A::sub(f[2 * q + 1], A::mul(f[2 * q], data));
             if (valid) st<S, C>(optr + (IDX)k * sk, A::mul(dtr, A::sub(data, p0)));
-            slot = slot + 1 == R ? 0 : slot + 1;
         }
     }
     cp_async_wait<0>();
