@@ -68,9 +68,9 @@ CONFIG = {"workload": "hdiff+vadv fp64 512x512x80 (halo 2,2,0 / 1,1,0)",
 # most columns in flight and is the fastest exact form.  Its nine products and
 # its pivot reciprocal per level run as integer arithmetic (bit-identical),
 # which needs many blocks per SM to hide the longer integer sequences: a ring
-# of depth 2, the library's 28 blocks per SM balanced to 27 (k_per_cta 0):
-# about 780 us against 1175 us all-fp64.
-VADV_TUNE = {"variant": 3, "block_x": 32, "unroll": 2, "k_per_cta": 0}
+# of depth 1, the library's 28 blocks per SM balanced to 27 (k_per_cta 0):
+# about 740 us against 1175 us all-fp64.
+VADV_TUNE = {"variant": 3, "block_x": 32, "unroll": 1, "k_per_cta": 0}
 
 # The fast float64 step: hdiff with exact 64-bit fixed-point sums and one
 # float64 FMA per point (float64 rounding level), vadv in float-pair

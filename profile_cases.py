@@ -94,7 +94,7 @@ def run_case(name, warmup, launches, rng):
                 scratch = {"ccol": _field(rng, scratch_storage, (1, 1, 0), 0.0, 0.0),
                            "dcol": _field(rng, scratch_storage, (1, 1, 0), 0.0, 0.0)}
             if variant == "slab":  # the bench's tunings for f64 and f32x2
-                slab = {"f64": (32, 2, 0), "f32x2": (64, 2, 32)}.get(form, (64, 4, 16))
+                slab = {"f64": (32, 1, 0), "f32x2": (64, 2, 32)}.get(form, (64, 4, 16))
                 tune = _native.tune(variant=_native.VADV_SLAB, block_x=slab[0], unroll=slab[1], k_per_cta=slab[2],
                                     flags=flags)
             elif variant:

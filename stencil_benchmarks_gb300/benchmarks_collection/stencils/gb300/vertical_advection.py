@@ -120,10 +120,13 @@ class Slab(VerticalAdvectionMixin, base.VerticalAdvectionStencil):
     block_size = Parameter("threads per block along i (32 or 64), persistent blocks per SM (0: the library's "
                            "choice: 24 when the float64 products run in integer arithmetic, otherwise as many as "
                            "keep the factor slabs within half of L2)", (32, 0))
-    unroll_factor = Parameter("levels of inputs kept in flight (2, 4 or 8)", 2, choices=[2, 4, 8])
+    unroll_factor = Parameter("levels of inputs kept in flight (1 with 32-thread blocks, 2, 4 or 8)", 1,
+                              choices=[1, 2, 4, 8])
 
     def check_parameters(self):
         super().check_parameters()
+        if self.unroll_factor == 1 and self.block_size[0] != 32:
+            raise ParameterError("Slab keeps one level in flight with 32-thread blocks only")
         if self.dtype_size != {"float64": 8, "float32": 4, "float32x2": 8}.get(self.compute, 0) and not (
                 self.dtype == "bfloat16" and self.compute == "float32"):
             raise ParameterError("Slab stages its ccol/dcol factors in ring entries: compute type as wide as storage")
@@ -136,7 +139,8 @@ class Slab(VerticalAdvectionMixin, base.VerticalAdvectionStencil):
 
     def tune_candidates(self):
         return [self.tune()] + [_native.tune(variant=_native.VADV_SLAB, block_x=bx, k_per_cta=per, unroll=u)
-                                for bx in (32, 64) for per in (0, 8, 16) for u in (2, 4, 8)]
+                                for bx in (32, 64) for per in (0, 8, 16)
+                                for u in ((1, 2, 4, 8) if bx == 32 else (2, 4, 8))]
 
     def launch_component(self, f, named, shift, timed):
         return kernels.vadv(*f, named["wcon"], shift, ccol=named["ccol"], dcol=named["dcol"], compute=self.compute,

@@ -248,10 +248,10 @@ template <class S, class C, int U, class IDX>
 void run_hdiff(dim3 g, dim3 b, cudaStream_t s, const DevTable* t, unsigned long long* c) {
     batch_hdiff_kernel<S, C, U, IDX><<<g, b, 0, s>>>(t, c);
 }
-// ring depth of a bucket kernel: 2 for the float64 slabs with the integer
+// ring depth of a bucket kernel: 1 for the float64 slabs with the integer
 // split (as the single-domain kernel), kVadvDepth otherwise
 template <uint32_t PL>
-constexpr int kBucketDepth = PL != 0u ? 2 : kVadvDepth;
+constexpr int kBucketDepth = PL != 0u ? 1 : kVadvDepth;
 
 template <class S, class C, int BT, class IDX, class P, bool SLAB, uint32_t PL>
 void run_vadv(dim3 g, dim3 b, size_t smem, cudaStream_t s, const DevTable* t, unsigned long long* c, int bucket,

@@ -66,7 +66,7 @@ __global__ void __launch_bounds__(256)
 // 14-16 dcol, 17-18 the back substitution, 19-20 the output, 21 the pivot's
 // reciprocal).  sb_tune.flags
 // bits 4-7 pick one for the SLAB form: 0 the default, 1 every site on the
-// fp64 pipe, 2.. the mixes below; SLAB shapes other than 32 threads x depth 2
+// fp64 pipe, 2.. the mixes below; SLAB shapes other than 32 threads x depth 1
 // and the SMEM-async form use the default.
 constexpr uint32_t vadv_sites(std::initializer_list<int> ks) {
     uint32_t m = 0;
@@ -107,8 +107,10 @@ static_assert(kVadvDefaultIntSites == (kVadvMuls | kVadvRcpSite), "the default s
 // the integer pipe cost more than they save (a binary64 add in integer
 // arithmetic runs at 0.31 Tops/s against 0.52 for the fp64 instruction, a
 // multiply at 0.56, a reciprocal at 0.22 against 0.12 for the fp64
-// sequence).  The default float64 SLAB form: depth 2, up to 28 blocks per SM,
-// the grid balanced so that every block takes the same number of groups.
+// sequence).  Depth 1 (the next level's inputs in flight while one is
+// solved) is faster again: 742 us against 779 at depth 2, same bits.  The
+// default float64 SLAB form: depth 1, up to 28 blocks per SM, the grid
+// balanced so that every block takes the same number of groups.
 constexpr int kVadvPlacementDefault = 9;
 constexpr int kVadvSlabBlocksPerSm = 28;
 constexpr int kVadvPlacementCount = (int)(sizeof(kVadvPlacements) / sizeof(kVadvPlacements[0]));
@@ -333,10 +335,10 @@ int launch_slab(int bx, int depth, int blocks_per_sm, int placement, const Devic
         SB_CHECK(placement >= 0 && placement < kVadvPlacementCount, SB_ERR_INVALID,
                  "vadv SLAB: placement preset %d out of range [0, %d)", placement, kVadvPlacementCount);
         if constexpr (std::is_same<C, double>::value) {
-            if (bx == 32 && depth == 2 && placement != 0) {
+            if (bx == 32 && depth == 1 && placement != 0) {
 #define SB_VADV_SLAB_PL(Q)                                                                                         \
     if (placement == Q)                                                                                            \
-        return launch_slab_one<S, C, 32, 2, kVadvPlacements[Q]>(blocks_per_sm, p, stream, stage, pos, tens,        \
+        return launch_slab_one<S, C, 32, 1, kVadvPlacements[Q]>(blocks_per_sm, p, stream, stage, pos, tens,        \
                                                                 tensstage, wcon, out, ccol, dcol, ni, nj, nk, si, \
                                                                 sj, sk, wsh);
                 SB_VADV_SLAB_PL(1)
@@ -362,6 +364,7 @@ int launch_slab(int bx, int depth, int blocks_per_sm, int placement, const Devic
         return launch_slab_one<S, C, BTV, DV, kVadvDefaultPlacement<C>>(blocks_per_sm, p, stream, stage, pos,   \
                                                                            tens, tensstage, wcon, out, ccol, dcol, \
                                                                            ni, nj, nk, si, sj, sk, wsh);
+        SB_VADV_SLAB_CASE(32, 1)
         SB_VADV_SLAB_CASE(32, 2)
         SB_VADV_SLAB_CASE(32, 4)
         SB_VADV_SLAB_CASE(32, 8)
@@ -595,7 +598,7 @@ int launch_typed(const void* stage, const void* pos, const void* tens, const voi
                             ? launch_wslab<S, C>(32, 4, 0, p, stream, stage, pos, tens, tensstage, wcon, out, ccol,
                                                  dcol, ni, nj, nk, si, sj, sk, wsh)
                             : (std::is_same<C, double>::value
-                                   ? launch_slab<S, C>(32, 2, kVadvSlabBlocksPerSm, placement, p, stream, stage, pos,
+                                   ? launch_slab<S, C>(32, 1, kVadvSlabBlocksPerSm, placement, p, stream, stage, pos,
                                                        tens, tensstage, wcon, out, ccol, dcol, ni, nj, nk, si, sj,
                                                        sk, wsh)
                                    : launch_slab<S, C>(64, 2, 32, placement, p, stream, stage, pos, tens, tensstage,
@@ -635,7 +638,7 @@ int launch_typed(const void* stage, const void* pos, const void* tens, const voi
         const int rc2 = launch_slab<S, C>(bx, d, bpsm, placement, p, stream, stage, pos, tens, tensstage, wcon, out,
                                           ccol, dcol, ni, nj, nk, si, sj, sk, wsh);
         SB_CHECK(rc2 != SB_ERR_UNSUPPORTED, SB_ERR_UNSUPPORTED,
-                 "vadv SLAB variant: needs blocks of 32 or 64 threads, depth 2, 4 or 8, positive strides, "
+                 "vadv SLAB variant: needs blocks of 32 or 64 threads, depth 1 (32 threads), 2, 4 or 8, positive strides, "
                  "32-bit offsets and a compute type as wide as the storage ring entries");
         return rc2;
     }

@@ -109,7 +109,7 @@ def _vadv(domain, halo, tune=None, seed=0, shift=(1, 0), use_scratch=False):
 
 @pytest.mark.parametrize("variant,bx,by,depth", [(0, 0, 0, 0), (1, 32, 1, 4), (1, 64, 1, 8), (1, 32, 2, 2),
                                                  (2, 32, 1, 4), (2, 128, 2, 8), (3, 32, 1, 4), (3, 64, 1, 2),
-                                                 (4, 32, 1, 4), (4, 64, 1, 2)])
+                                                 (3, 32, 1, 1), (4, 32, 1, 4), (4, 64, 1, 2)])
 def test_vadv_pair_variants(variant, bx, by, depth, lib):
     t = _native.tune(variant=variant, block_x=bx, block_y=by, unroll=depth)
     for nk in (2, 3, 9, 40):

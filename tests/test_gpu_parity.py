@@ -324,6 +324,21 @@ def test_vadv_slab(variant, bx, depth, per_sm, storage, compute, lib):
         _assert_bits(got, want, f"vadv slab {variant} {bx} depth {depth} per_sm {per_sm} {domain}")
 
 
+@pytest.mark.parametrize("per_sm", [0, 1, 28])
+@pytest.mark.parametrize("storage,compute", [("float64", "float64"), ("float32", "float32"),
+                                             ("bfloat16", "float32")])
+def test_vadv_slab_depth_one(per_sm, storage, compute, lib):
+    """SLAB with one level of inputs in flight (the float64 default; float
+    pairs: tests/test_gpu_fast_f64.py): levels 2 and 3 (no full ring turn)
+    and longer columns, one block per SM (every thread many columns) up to
+    the default's balanced grid."""
+    t = _native.tune(variant=_native.VADV_SLAB, block_x=32, unroll=1, k_per_cta=per_sm)
+    for domain in ((97, 19, 2), (97, 19, 3), (33, 40, 9), (130, 7, 41)):
+        got, want = _run_vadv(domain, (1, 1, 0), storage, compute, tune=t, seed=23 + domain[2],
+                              use_scratch=True)
+        _assert_bits(got, want, f"vadv slab depth 1 per_sm {per_sm} {storage}/{compute} {domain}")
+
+
 @pytest.mark.parametrize("depth", [0, 4, 8, 16])
 @pytest.mark.parametrize("storage", ["float32", "bfloat16"])
 @pytest.mark.parametrize("staging", [0x400, 0x800], ids=["shared-addr", "generic"])

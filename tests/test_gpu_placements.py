@@ -72,7 +72,7 @@ def test_vadv_slab_placements(preset, per_sm, nk, lib):
     for n in ("out", "ccol", "dcol"):
         hosts[n] = host_field(np.zeros(shape), halo=halo)
     dev = {n: to_device(h, "float64", halo) for n, h in hosts.items()}
-    tune = _native.tune(variant=_native.VADV_SLAB, block_x=32, unroll=2, k_per_cta=per_sm, flags=preset << 4)
+    tune = _native.tune(variant=_native.VADV_SLAB, block_x=32, unroll=1, k_per_cta=per_sm, flags=preset << 4)
     kernels.vadv(dev["ustage"], dev["upos"], dev["utens"], dev["utensstage"], dev["wcon"], out=dev["out"],
                  ccol=dev["ccol"], dcol=dev["dcol"], tune=tune)
     _native.synchronize()
@@ -91,7 +91,7 @@ def test_vadv_slab_placements_with_specials(preset, lib):
     for n in ("out", "ccol", "dcol"):
         hosts[n] = host_field(np.zeros(shape), halo=halo)
     dev = {n: to_device(h, "float64", halo) for n, h in hosts.items()}
-    tune = _native.tune(variant=_native.VADV_SLAB, block_x=32, unroll=2, flags=preset << 4)
+    tune = _native.tune(variant=_native.VADV_SLAB, block_x=32, unroll=1, flags=preset << 4)
     kernels.vadv(dev["ustage"], dev["upos"], dev["utens"], dev["utensstage"], dev["wcon"], out=dev["out"],
                  ccol=dev["ccol"], dcol=dev["dcol"], tune=tune)
     _native.synchronize()
