@@ -84,8 +84,11 @@ extern "C" {
 #define SB_VADV_GLOBAL 2  /* one thread per column, ccol/dcol in caller scratch    */
 #define SB_VADV_SLAB 3    /* persistent threads, factors in compact per-thread slabs of
                            * the caller's ccol/dcol (L2-resident), cp.async staging;
-                           * tune: block_x 32/64, unroll = depth 2/4/8, k_per_cta =
-                           * blocks per SM (0: as many as fit with slabs <= L2/2)  */
+                           * tune: block_x 32/64, unroll = depth 1 (32-thread
+                           * blocks) / 2 / 4 / 8, k_per_cta = blocks per SM (0:
+                           * 28 with the float64 integer split, the grid balanced
+                           * so that every block takes as many column groups;
+                           * otherwise as many as fit with slabs <= L2/2)        */
 #define SB_VADV_WSLAB 4   /* SLAB with each warp's 32-column rows staged together in
                            * 16-byte copies (needs i unit-stride); same tune fields.
                            * SB_VARIANT_AUTO with ccol/dcol given and no block/unroll
