@@ -61,6 +61,8 @@ UNIT = "GPoints/s"
 # the workload, identical in both arms' lines
 CONFIG = {"workload": "hdiff+vadv fp64 512x512x80 (halo 2,2,0 / 1,1,0)",
           "l2": "inputs > L2 (1.35 GB of fields per step), no flush"}
+# timed repetitions of the pipelined end-to-end loop (median reported)
+E2E_REPS = 3
 
 
 # fp64 vadv on GB300 is bound by the fp64 pipe; the SLAB variant (persistent
@@ -423,22 +425,28 @@ def run_gpu(args, dist):
 
     for n in range(2):
         pipe_step(n)
-    _native.synchronize()
-    dist.barrier()
-    p0, p1 = Event(), Event()
-    p0.record(s_in)
-    for st in s_ins[1:]:
-        wait(st, p0)
-    for n in range(e2e_steps):
-        pipe_step(n)
-    for st in s_outs[1:]:
-        last = Event()
-        last.record(st)
-        wait(s_out, last)
-    p1.record(s_out)
-    p1.synchronize()
-    _native.synchronize()
-    e2e_time = dist.max(p0.elapsed(p1))
+    # three timed repetitions of e2e_steps steps, the median reported: the host
+    # link is shared with the machine's other GPUs, and a single repetition has
+    # measured 3.7 against 6.7 GPoints/s when it met their traffic
+    e2e_reps = []
+    for _ in range(E2E_REPS):
+        _native.synchronize()
+        dist.barrier()
+        p0, p1 = Event(), Event()
+        p0.record(s_in)
+        for st in s_ins[1:]:
+            wait(st, p0)
+        for n in range(e2e_steps):
+            pipe_step(n)
+        for st in s_outs[1:]:
+            last = Event()
+            last.record(st)
+            wait(s_out, last)
+        p1.record(s_out)
+        p1.synchronize()
+        _native.synchronize()
+        e2e_reps.append(dist.max(p0.elapsed(p1)))
+    e2e_time = statistics.median(e2e_reps)
     del second, sets
 
     # ---- the fast float64 step (same inputs, separate outputs), timed the same way
@@ -507,6 +515,7 @@ def run_gpu(args, dist):
     return {
         "info": info, "elapsed": elapsed_max, "t_hdiff": t_hdiff, "t_vadv": t_vadv, "clocks": clk,
         "gpu_launches": gpu_launches, "e2e_time": e2e_time, "e2e_serial_time": e2e_serial_time,
+        "e2e_reps": e2e_reps,
         "e2e_steps": e2e_steps, "h2d": h2d, "d2h": d2h,
         "triad": triad, "fast": fast, "fp64_peak": fp64_peak,
     }
@@ -916,6 +925,8 @@ def main(argv=None):
                     "path": "C ABI: pinned host -> sb_memcpy_async -> sb_hdiff + sb_vadv -> pinned host; "
                             "uploads, kernels and downloads on three streams over two device sets; "
                             "host link measured alone: 211 GB/s H2D, 193 GB/s D2H",
+                    "timing": f"median of {len(res['e2e_reps'])} timed repetitions of {res['e2e_steps']} steps",
+                    "rep_values": [2 * POINTS * res["e2e_steps"] * dist.world / t / 1e9 for t in res["e2e_reps"]],
                     "serial_value": 2 * POINTS * res["e2e_steps"] * dist.world / res["e2e_serial_time"] / 1e9},
             "roofline": {"bound": "hbm", "limiter": "fp64 pipe: exact fp64 arithmetic runs at 1/73 of the fp32 "
                                                    "rate on GB300 (0.52 Tops/s measured)",
