@@ -466,7 +466,10 @@ int sb_vadv_noalloc(int storage, int compute, const void* stage, const void* pos
  * add, counted as adds; 11: that integer work alone, counted the same way --
  * 10 runs at the rate of 0 if the two pipes overlap, and at
  * 1 / (1/rate(0) + 1/rate(11)) if they do not; 12: f64 reciprocal in integer
- * arithmetic, 13: the f64 reciprocal instruction sequence, __drcp_rn). */
+ * arithmetic, 13: the f64 reciprocal instruction sequence, __drcp_rn; 14:
+ * the 64-bit leading-zero instruction (the integer add's normalisation),
+ * 15: a leading-zero count from an int-to-float conversion, for comparison;
+ * 16 / 17: 14 / 15 with one f64 add beside each count, counted as adds). */
 int sb_probe_arith_rate(int kind, double* ops_per_s);
 /* The binary64 operations the kernels can run in integer arithmetic, applied
  * element-wise on the device to n doubles (op 0: a + b, 1: a - b, 2: a * b,

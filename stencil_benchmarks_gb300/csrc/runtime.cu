@@ -107,6 +107,17 @@ __global__ void flush_kernel(uint4* buf, size_t n, unsigned salt) {
     }
 }
 
+// A 64-bit leading-zero count from the exponent of a round-toward-zero
+// unsigned-to-float conversion of the upper (or, when it is zero, the lower)
+// 32-bit word, exactly floor(log2(w)) (H. S. Warren, Hacker's Delight, 2nd
+// ed., sec. 5-3): the rate probe's comparison for the leading-zero
+// instruction that the integer add uses.  x must be non-zero.
+__device__ __forceinline__ int clz64_by_conversion(uint64_t x) {
+    const uint32_t hi = (uint32_t)(x >> 32);
+    const uint32_t w = hi ? hi : (uint32_t)x;
+    return (hi ? 158 : 190) - (int)(__float_as_uint(__uint2float_rz(w)) >> 23);
+}
+
 // Dependent-free arithmetic chains for the rate probe: each thread runs 8
 // independent accumulators so the pipe, not latency, is the limit.
 template <int KIND>
@@ -206,6 +217,33 @@ __global__ void arith_probe_kernel(double* out, int iters, double x) {
         double s = 0.0;
         for (int u = 0; u < 8; ++u) s += a[u];
         if (s == 12345.678) out[0] = s;
+    } else if (KIND >= 14 && KIND <= 17) {
+        // 64-bit leading-zero counts: the instruction (__clzll; 14) or the
+        // conversion form (15), each in a chain with a rotate and an add;
+        // 16 / 17: the same chains with one f64 add beside each count
+        // (counted as adds: the fp64 rate if the two do not compete)
+        uint64_t v[8];
+        double a[8];
+        for (int u = 0; u < 8; ++u) {
+            v[u] = 0x9E3779B97F4A7C15ull * (uint64_t)(threadIdx.x + u + 1);
+            a[u] = x + (double)(threadIdx.x + u);
+        }
+        const double c = 1e-3;
+        for (int it = 0; it < iters; ++it) {
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                const int z = (KIND == 14 || KIND == 16) ? __clzll((long long)v[u]) : clz64_by_conversion(v[u]);
+                v[u] = (((v[u] << 5) | (v[u] >> 59)) + (uint64_t)z) | 1ull;
+                if (KIND >= 16) a[u] = __dadd_rn(a[u], c);
+            }
+        }
+        double s = 0.0;
+        uint64_t t = 0;
+        for (int u = 0; u < 8; ++u) {
+            s += a[u];
+            t += v[u];
+        }
+        if (s == 12345.678 || t == 12345u) out[0] = s;
     } else if (KIND == 8 || KIND == 9) {  // binary64 add / mul on the integer pipe (softf64.cuh)
         double a[8];
         for (int u = 0; u < 8; ++u) a[u] = x + (double)(threadIdx.x + u);
@@ -500,14 +538,15 @@ int sb_debug_soft_f64(int op, const void* a, const void* b, void* out, int64_t n
 }
 
 int sb_probe_arith_rate(int kind, double* ops_per_s) {
-    SB_CHECK(kind >= 0 && kind <= 13 && ops_per_s, SB_ERR_INVALID, "bad probe arguments");
+    SB_CHECK(kind >= 0 && kind <= 17 && ops_per_s, SB_ERR_INVALID, "bad probe arguments");
     const DeviceProps* p;
     int rc = device_props(&p);
     if (rc) return rc;
     double* out = nullptr;
     SB_CUDA(cudaMalloc(&out, sizeof(double)));
     const int blocks = p->sm_count * 8, threads = 256,
-              iters = (kind == 2 || (kind >= 5 && kind <= 9)) ? 8192 : (kind >= 12 ? 2048 : 512);
+              iters = (kind == 2 || (kind >= 5 && kind <= 9)) ? 8192
+                                                                 : (kind >= 12 && kind <= 15 ? 2048 : 512);
     auto launch = [&]() {
         if (kind == 0) arith_probe_kernel<0><<<blocks, threads>>>(out, iters, 0.5);
         if (kind == 1) arith_probe_kernel<1><<<blocks, threads>>>(out, iters, 0.5);
@@ -523,6 +562,10 @@ int sb_probe_arith_rate(int kind, double* ops_per_s) {
         if (kind == 11) arith_probe_kernel<11><<<blocks, threads>>>(out, iters, 0.5);
         if (kind == 12) arith_probe_kernel<12><<<blocks, threads>>>(out, iters, 0.5);
         if (kind == 13) arith_probe_kernel<13><<<blocks, threads>>>(out, iters, 0.5);
+        if (kind == 14) arith_probe_kernel<14><<<blocks, threads>>>(out, iters, 0.5);
+        if (kind == 15) arith_probe_kernel<15><<<blocks, threads>>>(out, iters, 0.5);
+        if (kind == 16) arith_probe_kernel<16><<<blocks, threads>>>(out, iters, 0.5);
+        if (kind == 17) arith_probe_kernel<17><<<blocks, threads>>>(out, iters, 0.5);
         return SB_OK;
     };
     double t = 0.0;

@@ -168,8 +168,10 @@ def arith_rate(kind: int) -> float:
     """Measured operations per second: 0 fp64 add, 1 fp64 fma, 2 fp32 fma, 3 f64->f32
     conversion, 4 f32->f64 conversion, 5 32-bit integer shift/xor/multiply, 6 u32->f32
     conversion, 7 s32->f32 conversion, 8 / 9 fp64 add / multiply in integer arithmetic,
-    10 fp64 adds beside independent integer work, 11 that integer work alone (see
-    sb_probe_arith_rate)."""
+    10 fp64 adds beside independent integer work, 11 that integer work alone, 12 / 13 the
+    fp64 reciprocal in integer arithmetic / as the fp64 sequence, 14 / 15 the 64-bit
+    leading-zero count as the instruction / from a conversion, 16 / 17 those beside one
+    fp64 add each (see sb_probe_arith_rate)."""
     out = ctypes.c_double()
     _native.call("sb_probe_arith_rate", int(kind), ctypes.byref(out))
     return out.value

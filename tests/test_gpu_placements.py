@@ -111,8 +111,9 @@ def test_placement_out_of_range_is_rejected(lib):
 
 
 def test_integer_arithmetic_rates(lib):
-    """The probes of the integer binary64 add and multiply run and report rates."""
-    for kind in (8, 9, 10, 11):
+    """The probes of the integer binary64 add and multiply and of the two
+    leading-zero counts run and report rates."""
+    for kind in (8, 9, 10, 11, 14, 15, 16, 17):
         assert kernels.arith_rate(kind) > 1e9
 
 
@@ -153,8 +154,17 @@ def test_soft_f64_on_device(op, lib):
     sp = np.array([0.0, -0.0, 5e-324, -3e-310, 2.0**-1022, 1.0, -1.5, 2.0**1021, 1.5 * 2.0**1022,
                    np.finfo(np.float64).max, np.inf, -np.inf, np.nan])
     ga, gb = np.meshgrid(sp, sp)
-    a = np.concatenate([a, ga.ravel(), rng.uniform(0.1, 3.0, size=100_000)])
-    b = np.concatenate([b, gb.ravel(), rng.uniform(-1.0, 1.0, size=100_000)])
+    # cancellations of every depth: b is a with its lowest t bits redrawn
+    # (t = 1..62, so exponent bits too), with the sign that makes op 0 and op 1
+    # subtract -- every leading-zero count of the difference, 0 to 63
+    near = rng.uniform(-4.0, 4.0, size=200_000)
+    t = rng.integers(1, 63, size=near.size).astype(np.uint64)
+    low = rng.integers(0, 2**62, size=near.size, dtype=np.int64).astype(np.uint64) & ((np.uint64(1) << t) - np.uint64(1))
+    nb = (near.view(np.uint64) & ~((np.uint64(1) << t) - np.uint64(1))) | low
+    nb = nb.view(np.float64)
+    nb = np.where(np.isfinite(nb), nb, near)
+    a = np.concatenate([a, ga.ravel(), rng.uniform(0.1, 3.0, size=100_000), near])
+    b = np.concatenate([b, gb.ravel(), rng.uniform(-1.0, 1.0, size=100_000), -nb if op == 0 else nb])
     got = _soft_on_device(op, a, b)
     with np.errstate(all="ignore"):
         want = [a + b, a - b, a * b, 1.0 / a][op]
@@ -165,8 +175,10 @@ def test_soft_f64_on_device(op, lib):
 
 
 def test_soft_reciprocal_rate(lib):
-    """The integer-arithmetic reciprocal is faster than the fp64 sequence it
-    replaces (the reason the vadv pivot's reciprocal can move)."""
+    """Both reciprocal rate probes run and report a rate: the integer-arithmetic
+    reciprocal and the fp64 sequence it replaces (the integer one measured
+    faster on GB300, the reason the vadv pivot's reciprocal moved).  No
+    ordering is asserted: the probes share the GPU with other work."""
     soft, hard = kernels.arith_rate(12), kernels.arith_rate(13)
     assert soft > 0 and hard > 0
     print(f"reciprocal: integer {soft / 1e9:.1f} G/s, fp64 {hard / 1e9:.1f} G/s")
