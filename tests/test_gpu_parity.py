@@ -459,23 +459,36 @@ def test_laplacian_variants(storage, compute, mask, shape, lib):
 
 @pytest.mark.parametrize("storage", ["float64", "float32"])
 @pytest.mark.parametrize("preset", [1, 2, 3, 4])
-def test_laplacian_float64_placements(storage, preset, lib):
+@pytest.mark.parametrize("special", [False, True])
+def test_laplacian_float64_placements(storage, preset, special, lib):
     """float64 Laplacian strips with their subtractions/addition split between
     the fp64 and the integer pipes: the same bits as the oracle, signed zeros
-    and cancellations included."""
+    and cancellations included; with `special`, a sprinkling of subnormal,
+    huge, infinite and NaN inputs that the integer path declines (those strips
+    are recomputed on the fp64 pipe)."""
     domain, halo = (64, 33, 5), (1, 1, 1)
     shape_ = tuple(d + 2 * h for d, h in zip(domain, halo))
     vals = rng_fields(77, shape_, ("inp", "out"), {})
     vals["inp"][::3, ::2, :] = 0.0  # exact cancellations and zero sums
     vals["inp"][1::5, :, ::2] *= -1.0
+    if special:
+        pick = np.random.Generator(np.random.PCG64(78)).random(size=shape_)
+        big = 1e38 if storage == "float32" else 1.5e308
+        tiny = 1e-40 if storage == "float32" else 3e-310
+        vals["inp"][pick < 0.01] = tiny
+        vals["inp"][(pick >= 0.01) & (pick < 0.015)] = -tiny
+        vals["inp"][(pick >= 0.015) & (pick < 0.02)] = big
+        vals["inp"][(pick >= 0.02) & (pick < 0.022)] = np.inf
+        vals["inp"][(pick >= 0.022) & (pick < 0.024)] = np.nan
     hosts = {n: host_field(v, storage, halo=halo) for n, v in vals.items()}
     dev = {n: to_device(h, storage, halo) for n, h in hosts.items()}
     t = _native.tune(variant=_native.BASIC_MARCH, flags=preset << 4)
     kernels.laplacian(dev["inp"], dev["out"], (True, True, False), compute="float64", tune=t)
     got = interior(download_like(dev["out"], hosts["out"]), domain, halo)
-    want = round_to_storage(ora.laplacian(compute_view(hosts["inp"], storage, "float64"), domain, halo,
-                                          (True, True, False)), storage)
-    _assert_bits(got, want, f"laplacian placement {preset} {storage}")
+    with np.errstate(all="ignore"):
+        want = round_to_storage(ora.laplacian(compute_view(hosts["inp"], storage, "float64"), domain, halo,
+                                              (True, True, False)), storage)
+    _assert_bits(got, want, f"laplacian placement {preset} {storage} special={special}")
 
 
 def test_laplacian_rejects_bad_strip(lib):
