@@ -16,8 +16,10 @@ library, except vadv-f64 and vadv-f32x2, which use the caller-scratch
 (GLOBAL) variant as ``bench.py`` does.  ``:<variant>`` picks another one
 (hdiff: tile, jscan, tma, vscan -- tma with rows padded to 64 bytes so that the
 j/k strides suit the tensor copies; vadv: smem, global, slab, wslab, tmem -- global,
-slab and wslab with ccol/dcol scratch fields); ``@<placement>`` sets the float64
-integer-pipe placement preset (sb_tune.flags bits 4-7) of tma and slab.
+slab and wslab with ccol/dcol scratch fields; lap: point, march); ``@<placement>``
+sets the float64 integer-pipe placement preset (sb_tune.flags bits 4-7) of tma
+(then on the library's default 128 x 4 tile, 16 rows, one k-plane per block: the
+tile the presets apply to), slab and march.
 """
 
 from __future__ import annotations
@@ -57,7 +59,8 @@ def _field(rng, storage, halo, lo, hi, alignment=0):
 VARIANTS = {"tile": _native.HDIFF_TILE, "jscan": _native.HDIFF_JSCAN, "tma": _native.HDIFF_TMA,
             "vscan": _native.HDIFF_VSCAN,
             "smem": _native.VADV_SMEM, "wslab": _native.VADV_WSLAB, "tmem": _native.VADV_TMEM,
-            "global": _native.VADV_GLOBAL, "slab": _native.VADV_SLAB}
+            "global": _native.VADV_GLOBAL, "slab": _native.VADV_SLAB,
+            "point": _native.BASIC_POINT, "march": _native.BASIC_MARCH}
 
 
 def run_case(name, warmup, launches, rng):
@@ -79,7 +82,12 @@ def run_case(name, warmup, launches, rng):
             align = 64 if variant == "tma" else 0
             f = [_field(rng, storage, (2, 2, 0), 0.0, 1.0, align) for _ in range(3)]
 
-            htune = _native.tune(variant=VARIANTS[variant], flags=flags) if variant else None
+            htune = None
+            if variant == "tma" and placement:
+                htune = _native.tune(variant=VARIANTS[variant], block_x=128, block_y=4, tile_y=16, k_per_cta=1,
+                                     flags=flags)
+            elif variant:
+                htune = _native.tune(variant=VARIANTS[variant], flags=flags)
 
             def launch(timed):
                 return kernels.hdiff(*f, compute=compute, tune=htune, timed=timed)
@@ -120,11 +128,12 @@ def run_case(name, warmup, launches, rng):
                 return total
         elif stencil in ("copy", "lap"):
             f = [_field(rng, storage, (1, 1, 1), 0.0, 1.0) for _ in range(2)]
+            ltune = _native.tune(variant=VARIANTS[variant], flags=flags) if variant else None
 
             def launch(timed):
                 if stencil == "copy":
                     return kernels.copy(*f, timed=timed)
-                return kernels.laplacian(*f, compute=compute, timed=timed)
+                return kernels.laplacian(*f, compute=compute, tune=ltune, timed=timed)
         else:
             raise SystemExit(f"unknown case {name!r}")
     for _ in range(warmup):
