@@ -469,7 +469,9 @@ int sb_vadv_noalloc(int storage, int compute, const void* stage, const void* pos
  * arithmetic, 13: the f64 reciprocal instruction sequence, __drcp_rn; 14:
  * the 64-bit leading-zero instruction (the integer add's normalisation),
  * 15: a leading-zero count from an int-to-float conversion, for comparison;
- * 16 / 17: 14 / 15 with one f64 add beside each count, counted as adds). */
+ * 16 / 17: 14 / 15 with one f64 add beside each count, counted as adds;
+ * 18 / 19 / 20: f64 adds beside one integer binary64 add, one 64-bit
+ * variable shift, or one 64-bit add and compare each, counted as adds). */
 int sb_probe_arith_rate(int kind, double* ops_per_s);
 /* The binary64 operations the kernels can run in integer arithmetic, applied
  * element-wise on the device to n doubles (op 0: a + b, 1: a - b, 2: a * b,

@@ -244,6 +244,41 @@ __global__ void arith_probe_kernel(double* out, int iters, double x) {
             t += v[u];
         }
         if (s == 12345.678 || t == 12345u) out[0] = s;
+    } else if (KIND >= 18 && KIND <= 20) {
+        // one f64 add per step beside: the integer-arithmetic binary64 add
+        // (18), a 64-bit shift by a variable amount (19), or a 64-bit add and
+        // a 64-bit compare (20); counted as f64 adds, so each runs at the fp64
+        // rate (kind 0) unless the integer work also occupies the fp64 pipe
+        double a[8], b[8];
+        uint64_t v[8];
+        for (int u = 0; u < 8; ++u) {
+            a[u] = x + (double)(threadIdx.x + u);
+            b[u] = 1.5 + (double)u;
+            v[u] = 0x9E3779B97F4A7C15ull * (uint64_t)(threadIdx.x + u + 1);
+        }
+        const double c = 1e-3;
+        for (int it = 0; it < iters; ++it) {
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                a[u] = __dadd_rn(a[u], c);
+                if (KIND == 18) {
+                    b[u] = iadd(b[u], 1e-7);
+                } else if (KIND == 19) {
+                    const unsigned s = (unsigned)v[u] & 63u;
+                    v[u] = (v[u] << s) ^ (v[u] >> (63u - s)) ^ 0x5bd1e995ull;
+                } else {
+                    const uint64_t w = v[u] + 0x9E3779B97F4A7C15ull;
+                    v[u] = (w < v[u]) ? w ^ 0x2545F4914F6CDD1Dull : w;
+                }
+            }
+        }
+        double s = 0.0;
+        uint64_t t = 0;
+        for (int u = 0; u < 8; ++u) {
+            s += a[u] + b[u];
+            t += v[u];
+        }
+        if (s == 12345.678 || t == 12345u) out[0] = s;
     } else if (KIND == 8 || KIND == 9) {  // binary64 add / mul on the integer pipe (softf64.cuh)
         double a[8];
         for (int u = 0; u < 8; ++u) a[u] = x + (double)(threadIdx.x + u);
@@ -538,7 +573,7 @@ int sb_debug_soft_f64(int op, const void* a, const void* b, void* out, int64_t n
 }
 
 int sb_probe_arith_rate(int kind, double* ops_per_s) {
-    SB_CHECK(kind >= 0 && kind <= 17 && ops_per_s, SB_ERR_INVALID, "bad probe arguments");
+    SB_CHECK(kind >= 0 && kind <= 20 && ops_per_s, SB_ERR_INVALID, "bad probe arguments");
     const DeviceProps* p;
     int rc = device_props(&p);
     if (rc) return rc;
@@ -566,6 +601,9 @@ int sb_probe_arith_rate(int kind, double* ops_per_s) {
         if (kind == 15) arith_probe_kernel<15><<<blocks, threads>>>(out, iters, 0.5);
         if (kind == 16) arith_probe_kernel<16><<<blocks, threads>>>(out, iters, 0.5);
         if (kind == 17) arith_probe_kernel<17><<<blocks, threads>>>(out, iters, 0.5);
+        if (kind == 18) arith_probe_kernel<18><<<blocks, threads>>>(out, iters, 0.5);
+        if (kind == 19) arith_probe_kernel<19><<<blocks, threads>>>(out, iters, 0.5);
+        if (kind == 20) arith_probe_kernel<20><<<blocks, threads>>>(out, iters, 0.5);
         return SB_OK;
     };
     double t = 0.0;

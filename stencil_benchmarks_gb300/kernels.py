@@ -171,7 +171,8 @@ def arith_rate(kind: int) -> float:
     10 fp64 adds beside independent integer work, 11 that integer work alone, 12 / 13 the
     fp64 reciprocal in integer arithmetic / as the fp64 sequence, 14 / 15 the 64-bit
     leading-zero count as the instruction / from a conversion, 16 / 17 those beside one
-    fp64 add each (see sb_probe_arith_rate)."""
+    fp64 add each, 18 / 19 / 20 fp64 adds beside an integer binary64 add / a 64-bit variable
+    shift / a 64-bit add and compare (see sb_probe_arith_rate)."""
     out = ctypes.c_double()
     _native.call("sb_probe_arith_rate", int(kind), ctypes.byref(out))
     return out.value
